@@ -1,0 +1,89 @@
+"""ctypes binding of libdgcu.so (include/dgcu.h).  Fails loudly when the
+library is missing: there is no CPU fallback."""
+import ctypes
+import os
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "lib", "libdgcu.so")
+
+DG_OK, DG_ERR_ARG, DG_ERR_CUDA, DG_ERR_TIMEOUT, DG_ERR_NOT_CONVERGED, DG_ERR_NONFINITE, DG_ERR_UNSUPPORTED, \
+    DG_ERR_NOMEM = range(8)
+ERR_NAMES = {0: "DG_OK", 1: "DG_ERR_ARG", 2: "DG_ERR_CUDA", 3: "DG_ERR_TIMEOUT", 4: "DG_ERR_NOT_CONVERGED",
+             5: "DG_ERR_NONFINITE", 6: "DG_ERR_UNSUPPORTED", 7: "DG_ERR_NOMEM"}
+DG_FLUX_LF, DG_FLUX_ROE = 0, 1
+DG_PREC_FP64, DG_PREC_SPLIT = 0, 1
+DG_PC_NONE, DG_PC_BLOCK_JACOBI, DG_PC_LEARNED = 0, 1, 2
+
+_dp = ctypes.POINTER(ctypes.c_double)
+_ip = ctypes.POINTER(ctypes.c_int32)
+_vp = ctypes.c_void_p
+
+
+class MeshDesc(ctypes.Structure):
+    _fields_ = [("K", ctypes.c_int32), ("EToV", _ip), ("VXY", _dp), ("EToE", _ip), ("EToF", _ip), ("ROT", _ip),
+                ("BC", _ip)]
+
+
+class Opts(ctypes.Structure):
+    _fields_ = [("order", ctypes.c_int32), ("cubature", _dp), ("n_cubature", ctypes.c_int32),
+                ("gamma", ctypes.c_double), ("stream", _vp)]
+
+
+class Info(ctypes.Structure):
+    _fields_ = [("K", ctypes.c_int32), ("order", ctypes.c_int32), ("Np", ctypes.c_int32), ("Ng", ctypes.c_int32),
+                ("Nfp", ctypes.c_int32), ("Nfq", ctypes.c_int32), ("n_bfaces", ctypes.c_int32), ("stream", _vp),
+                ("device_bytes", ctypes.c_size_t)]
+
+
+class SolveStats(ctypes.Structure):
+    _fields_ = [("iterations", ctypes.c_int32), ("rel_residual", ctypes.c_double), ("ms", ctypes.c_double)]
+
+
+# name -> (restype, argtypes); every symbol declared in include/dgcu.h
+SIGNATURES = {
+    "dg_ctx_create": (ctypes.c_int, [ctypes.POINTER(MeshDesc), ctypes.POINTER(Opts), ctypes.POINTER(_vp)]),
+    "dg_ctx_destroy": (ctypes.c_int, [_vp]),
+    "dg_get_info": (ctypes.c_int, [_vp, ctypes.POINTER(Info)]),
+    "dg_last_error": (ctypes.c_char_p, [_vp]),
+    "dg_upload_state": (ctypes.c_int, [_vp, _dp]),
+    "dg_download_state": (ctypes.c_int, [_vp, _dp]),
+    "dg_upload_state_device": (ctypes.c_int, [_vp, _vp]),
+    "dg_download_state_device": (ctypes.c_int, [_vp, _vp]),
+    "dg_set_boundary_traces": (ctypes.c_int, [_vp, _dp]),
+    "dg_euler_rhs": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, _dp]),
+    "dg_lserk4_step": (ctypes.c_int, [_vp, ctypes.c_double, ctypes.c_int, ctypes.c_int, ctypes.c_int]),
+    "dg_ssprk2_step": (ctypes.c_int, [_vp, ctypes.c_double, ctypes.c_int, ctypes.c_int, ctypes.c_int]),
+    "dg_cfl_dt": (ctypes.c_int, [_vp, ctypes.c_double, _dp]),
+    "dg_reference_operators": (ctypes.c_int, [ctypes.c_int, _dp, ctypes.c_int, _dp, _dp, _dp, _dp, _dp, _dp, _dp]),
+}
+
+_lib = None
+
+
+class DGError(RuntimeError):
+    def __init__(self, code, msg=""):
+        super().__init__("%s%s" % (ERR_NAMES.get(code, str(code)), (": " + msg) if msg else ""))
+        self.code = code
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError("libdgcu.so not built (%s): run __graft_entry__.build() or "
+                               "python -m hopefoam_gb300.build" % LIB_PATH)
+        L = ctypes.CDLL(LIB_PATH)
+        for name, (res, args) in SIGNATURES.items():
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = L
+    return _lib
+
+
+def dptr(a):
+    return a.ctypes.data_as(_dp)
+
+
+def iptr(a):
+    return a.ctypes.data_as(_ip)

@@ -1,0 +1,54 @@
+// dg_ctx.hpp -- the context behind the opaque dg_ctx handle.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <string>
+#include <vector>
+
+#include "dg_basis.hpp"
+#include "dg_internal.hpp"
+
+namespace dgk {
+
+// device operators and launch shape of the split-precision path
+struct SplitPlan {
+    bool ready = false;
+    int N = 0;
+    void* d_ops = nullptr;  // packed operator image (see euler_split.cu)
+    size_t ops_bytes = 0;
+    int* d_status = nullptr;
+};
+
+cudaError_t launch_euler_split(int N, const EulerArgs& a, const SplitPlan& plan, cudaStream_t s);
+
+}  // namespace dgk
+
+struct dg_ctx {
+    int K = 0, N = 0, Np = 0, Ng = 0, Nfp = 0, Nfq = 0, nb = 0;
+    double gamma = 1.4;
+    double min_h = 0;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    dgb::RefOps ops;
+    std::vector<double> geo_host;
+    std::vector<int> conn_host;
+    // device buffers
+    double* d_q[2] = {nullptr, nullptr};
+    double* d_res = nullptr;
+    double* d_stage = nullptr;
+    double* d_geo = nullptr;
+    double* d_btrace = nullptr;
+    int* d_conn = nullptr;
+    int* d_ring = nullptr;
+    double *d_Vg = nullptr, *d_Sr = nullptr, *d_Ss = nullptr, *d_Lift = nullptr, *d_If = nullptr;
+    int cur = 0;
+    bool btrace_set = false;
+    dgk::SplitPlan split;
+    std::vector<void*> allocs;
+    size_t bytes = 0;
+    std::string err;
+};
+
+int split_setup(dg_ctx* c);
+void split_teardown(dg_ctx* c);

@@ -1,0 +1,155 @@
+/*
+ * dgcu.h -- C ABI of the GB300-native 2D nodal-DG hot path (libdgcu.so).
+ *
+ * Drop-in boundary for HopeFOAM's DG Euler right-hand side and SIPG pressure
+ * solve.  Every entry point returns an int status (DG_OK or a DG_ERR_* code);
+ * no C++ exception crosses this boundary.  A context is used by one host
+ * thread at a time and issues all of its GPU work on one CUDA stream.
+ *
+ * Reference layouts kept at this boundary (paths relative to HopeFOAM-0.1/src/DG):
+ *  - state: the conserved fields rho, rhoU (x, y), Ener of
+ *    GeometricDofField (fields/GeometricDofField/GeometricDofField.H:301-341),
+ *    each K*Np doubles, element-contiguous (dofStart = k*Np), nodes in the
+ *    reference order of triangleBaseFunction::initDofLocation
+ *    (element/baseFunctions/straightBaseFunctions/triangleBaseFunction/
+ *    triangleBaseFunction.C:122-186).  Host arrays are packed as
+ *    q[v*K*Np + k*Np + i], v = 0 rho, 1 rhoU.x, 2 rhoU.y, 3 Ener.
+ *  - boundary traces: fixed values at the owner's face nodes in
+ *    faceToCellIndex order (triangleBaseFunction.C:75-94), as the
+ *    fixed-value patch data consumed by dgGaussField::initField
+ *    (fields/dgGaussField/dgGaussField.C:240-266).
+ */
+#ifndef DGCU_H
+#define DGCU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes */
+enum {
+    DG_OK = 0,
+    DG_ERR_ARG = 1,           /* invalid argument or mesh */
+    DG_ERR_CUDA = 2,          /* a CUDA call failed */
+    DG_ERR_TIMEOUT = 3,       /* a bounded device wait gave up */
+    DG_ERR_NOT_CONVERGED = 4, /* iterative solve hit its iteration limit */
+    DG_ERR_NONFINITE = 5,     /* NaN/Inf detected */
+    DG_ERR_UNSUPPORTED = 6,   /* order / option not built */
+    DG_ERR_NOMEM = 7          /* device allocation failed */
+};
+
+/* numerical flux (DG/godunovFlux/fluxSchemes/scheme/RoeFlux/RoeFlux.C:46-191
+ * for Roe; Lax-Friedrichs/Rusanov for Euler has no reference counterpart) */
+enum { DG_FLUX_LF = 0, DG_FLUX_ROE = 1 };
+
+/* arithmetic of the right-hand side */
+enum {
+    DG_PREC_FP64 = 0,  /* plain FP64 everywhere */
+    DG_PREC_SPLIT = 1  /* split-precision tensor-core volume/lift, FP64 state */
+};
+
+/* boundary kind per element face */
+enum { DG_BC_INTERIOR = 0, DG_BC_FIXED = 1 };
+
+/* preconditioners for dg_pcg_solve */
+enum { DG_PC_NONE = 0, DG_PC_BLOCK_JACOBI = 1, DG_PC_LEARNED = 2 };
+
+typedef struct dg_ctx dg_ctx;
+
+/* Triangle mesh.  Faces of element k are (v0,v1), (v1,v2), (v2,v0) of its
+ * counter-clockwise vertices (dgMesh/dgPolyMesh.C:486-506, :601-613). */
+typedef struct dg_mesh_desc {
+    int32_t K;             /* number of triangles */
+    const int32_t* EToV;   /* K*3 global vertex ids (periodic images share ids) */
+    const double* VXY;     /* K*3*2 element vertex coordinates */
+    const int32_t* EToE;   /* K*3 neighbour element, -1 on a boundary */
+    const int32_t* EToF;   /* K*3 neighbour's local face */
+    const int32_t* ROT;    /* K*3 face rotation (firstPointIndex, dgPolyMesh.C:866-893); NULL: from EToV */
+    const int32_t* BC;     /* K*3 DG_BC_* kind; NULL: DG_BC_FIXED exactly where EToE < 0 */
+} dg_mesh_desc;
+
+typedef struct dg_opts {
+    int32_t order;           /* polynomial order N, 1..7 */
+    const double* cubature;  /* n_cubature x 3 (r, s, w): triangle rule of strength 3(N+1),
+                                (gaussIntegration.C:66, gaussTriangleIntegration.C:48-63) */
+    int32_t n_cubature;
+    double gamma;            /* ratio of specific heats (transportProperties) */
+    void* stream;            /* cudaStream_t to use; NULL: the context creates one */
+} dg_opts;
+
+typedef struct dg_info {
+    int32_t K, order, Np, Ng, Nfp, Nfq, n_bfaces;
+    void* stream;            /* the context's cudaStream_t */
+    size_t device_bytes;     /* device memory held by the context */
+} dg_info;
+
+typedef struct dg_solve_stats {
+    int32_t iterations;
+    double rel_residual;     /* final ||b - A x|| / ||b|| */
+    double ms;               /* device time of the solve */
+} dg_solve_stats;
+
+/* Builds the per-order reference operators and the per-element geometry and
+ * connectivity on the device.  Replaces dgMesh::dgMesh (dgMesh/dgMesh.C:71-116)
+ * and physicalElementData::initElements
+ * (element/physicalElementData/physicalElementData.C:60-161, :228-263). */
+int dg_ctx_create(const dg_mesh_desc* mesh, const dg_opts* opts, dg_ctx** out);
+int dg_ctx_destroy(dg_ctx* ctx);
+int dg_get_info(const dg_ctx* ctx, dg_info* info);
+/* Message of the last error on this context (static storage of the context). */
+const char* dg_last_error(const dg_ctx* ctx);
+
+/* State transfer (host arrays, reference layout above).  Replaces the
+ * GeometricDofField internal fields read/written by the solver loop. */
+int dg_upload_state(dg_ctx* ctx, const double* q_host);
+int dg_download_state(dg_ctx* ctx, double* q_host);
+/* Same with device pointers (reference layout), stream-ordered. */
+int dg_upload_state_device(dg_ctx* ctx, const double* q_dev);
+int dg_download_state_device(dg_ctx* ctx, double* q_dev);
+
+/* Fixed-value boundary traces, n_bfaces x 4 x Nfp doubles; boundary faces
+ * ordered by (k, f).  Replaces setBoundaryValues / fixedValue patch data
+ * (tutorials/DG/2D/isentropicVortex/dgEulerFoam/setBoundaryValues.H). */
+int dg_set_boundary_traces(dg_ctx* ctx, const double* traces_host);
+
+/* R(q) = M^-1 [ volume(dgc::div + dgc::grad) - surface lift(flux) ] of the
+ * current state into rhs_host (reference layout).  Replaces one
+ * Equation::evaluate of the three solveEquation calls of dgEulerFoam.C:86-90
+ * without the ddt part: Equation/Equation.C:39-75,
+ * DG/convectionSchemes/defaultConvectionScheme/defaultConvectionScheme.C:48-129,
+ * DG/gradSchemes/defaultGrad/defaultGrad.C:87-166,
+ * DG/divSchemes/defaultDivScheme/defaultDivScheme.C:85-166. */
+int dg_euler_rhs(dg_ctx* ctx, int flux, int precision, double* rhs_host);
+
+/* nsteps low-storage RK4 steps (5 stages each, coefficients of
+ * tutorials/DG/2D/isentropicVortex/dgEulerFoam/createFields.H:119-138). */
+int dg_lserk4_step(dg_ctx* ctx, double dt, int nsteps, int flux, int precision);
+
+/* nsteps SSP-RK2 steps exactly as the reference solver's time loop
+ * (tutorials/DG/2D/isentropicVortex/dgEulerFoam/dgEulerFoam.C:64-131): each
+ * stage is dg::solveEquation(dgm::ddt(q) + R(q)) = q + dt M^-1 R_weak
+ * (DG/ddtSchemes/EulerDdtScheme/EulerDdtScheme.C:118-144). */
+int dg_ssprk2_step(dg_ctx* ctx, double dt, int nsteps, int flux, int precision);
+
+/* Largest stable time step by the build's CFL rule:
+ * dt = cfl * min_k h_k / ((N+1)^2 * max_nodes(|u| + c)), h_k = 2 area / longest edge
+ * (the reference uses a fixed dt, controlDict). */
+int dg_cfl_dt(dg_ctx* ctx, double cfl, double* dt);
+
+/* Host-only (no GPU needed): the reference-element operators this library
+ * builds for order N from a cubature rule, in the reference node order.
+ * Arrays are caller-allocated: r, s [Np]; Dr, Ds, Mref [Np*Np] (row-major);
+ * Vg [Ng*Np]; If [Nfq*Nfp]; any may be NULL.  Replaces the operator set of
+ * triangleBaseFunction (triangleBaseFunction.C:46-71, :236-246) and
+ * gaussTriangleIntegration (gaussTriangleIntegration.C:45-97). */
+int dg_reference_operators(int order, const double* cubature, int n_cubature, double* r, double* s, double* Dr,
+                           double* Ds, double* Vg, double* If, double* Mref);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* DGCU_H */

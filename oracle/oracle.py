@@ -1,0 +1,187 @@
+"""ctypes wrapper of the CPU oracle (test infrastructure: only tests/,
+__graft_entry__.smoke() and bench.py's CPU baseline use it)."""
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_LIB = os.path.join(_HERE, "_build", "libdgoracle.so")
+_lib = None
+
+_dp = ctypes.POINTER(ctypes.c_double)
+_ip = ctypes.POINTER(ctypes.c_int)
+
+
+def build():
+    subprocess.check_call(["make", "-s", "-C", _HERE])
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(_LIB):
+            build()
+        L = ctypes.CDLL(_LIB)
+        L.orc_create.restype = ctypes.c_void_p
+        L.orc_create.argtypes = [ctypes.c_int, ctypes.c_int, _ip, _dp, _dp, ctypes.c_int]
+        L.orc_destroy.argtypes = [ctypes.c_void_p]
+        L.orc_sizes.argtypes = [ctypes.c_void_p, _ip]
+        L.orc_ref_operators.argtypes = [ctypes.c_void_p] + [_dp] * 11 + [_ip]
+        L.orc_nodes.argtypes = [ctypes.c_void_p, _dp, _dp]
+        L.orc_connectivity.argtypes = [ctypes.c_void_p, _ip, _ip, _ip]
+        L.orc_mass.argtypes = [ctypes.c_void_p, _dp]
+        L.orc_euler_rhs.argtypes = [ctypes.c_void_p, _dp, _dp, ctypes.c_int, ctypes.c_double, _dp]
+        L.orc_euler_weak.argtypes = [ctypes.c_void_p, _dp, _dp, ctypes.c_int, ctypes.c_double, _dp]
+        L.orc_ssprk2.argtypes = [ctypes.c_void_p, _dp, ctypes.c_double, ctypes.c_int, ctypes.c_int,
+                                 ctypes.c_double, _dp, ctypes.c_double]
+        L.orc_lserk4.argtypes = [ctypes.c_void_p, _dp, _dp, ctypes.c_double, ctypes.c_int, ctypes.c_int,
+                                 ctypes.c_double]
+        L.orc_lserk4_coeffs.argtypes = [_dp, _dp, _dp]
+        L.orc_face_geom.argtypes = [ctypes.c_void_p, _dp]
+        L.orc_ipdg_blocks.argtypes = [ctypes.c_void_p, ctypes.c_double, _dp, _dp, _dp, _dp]
+        L.orc_blk_apply.argtypes = [ctypes.c_void_p, _dp, _dp, _dp, _dp]
+        L.orc_pcg_bj.restype = ctypes.c_int
+        L.orc_pcg_bj.argtypes = [ctypes.c_void_p, _dp, _dp, _dp, _dp, ctypes.c_double, ctypes.c_int, _dp]
+        L.orc_set_threads.argtypes = [ctypes.c_int]
+        L.orc_max_threads.restype = ctypes.c_int
+        _lib = L
+    return _lib
+
+
+def _d(a):
+    return a.ctypes.data_as(_dp)
+
+
+def _i(a):
+    return a.ctypes.data_as(_ip)
+
+
+FLUX_LF, FLUX_ROE = 0, 1
+
+
+class Oracle:
+    """FP64 CPU restatement of the reference's DG discretisation on one mesh."""
+
+    def __init__(self, mesh, order, cub):
+        self.L = lib()
+        self.mesh = mesh
+        self.N = order
+        EToV = np.ascontiguousarray(mesh.EToV, np.int32)
+        VXY = np.ascontiguousarray(mesh.VXY, np.float64)
+        self.cub = np.ascontiguousarray(cub, np.float64)
+        self.h = self.L.orc_create(order, mesh.K, _i(EToV), _d(VXY), _d(self.cub), self.cub.shape[0])
+        s = np.zeros(6, np.int32)
+        self.L.orc_sizes(self.h, _i(s))
+        self.Np, self.Ng, self.Nfp, self.Nfq, self.nfaces, self.nfacegauss = [int(v) for v in s]
+        self.K = mesh.K
+
+    def __del__(self):
+        try:
+            self.L.orc_destroy(self.h)
+        except Exception:
+            pass
+
+    def operators(self):
+        Np, Ng, Nfq, Nfp = self.Np, self.Ng, self.Nfq, self.Nfp
+        out = dict(r=np.zeros(Np), s=np.zeros(Np), V=np.zeros((Np, Np)), Dr=np.zeros((Np, Np)),
+                   Ds=np.zeros((Np, Np)), cellV=np.zeros((Ng, Np)), cellDr=np.zeros((Ng, Np)),
+                   cellDs=np.zeros((Ng, Np)), fq=np.zeros(Nfq), fw=np.zeros(Nfq),
+                   faceInterp=np.zeros((Nfq, Nfp)))
+        fci = np.zeros((3, 2, Nfp), np.int32)
+        self.L.orc_ref_operators(self.h, *[_d(out[k]) for k in ["r", "s", "V", "Dr", "Ds", "cellV", "cellDr",
+                                                                  "cellDs", "fq", "fw", "faceInterp"]], _i(fci))
+        out["fci"] = fci
+        return out
+
+    def nodes(self):
+        x = np.zeros(self.K * self.Np)
+        y = np.zeros(self.K * self.Np)
+        self.L.orc_nodes(self.h, _d(x), _d(y))
+        return x.reshape(self.K, self.Np), y.reshape(self.K, self.Np)
+
+    def connectivity(self):
+        E = np.zeros((self.K, 3), np.int32)
+        F = np.zeros((self.K, 3), np.int32)
+        R = np.zeros((self.K, 3), np.int32)
+        self.L.orc_connectivity(self.h, _i(E), _i(F), _i(R))
+        return E, F, R
+
+    def mass(self):
+        M = np.zeros((self.K, self.Np, self.Np))
+        self.L.orc_mass(self.h, _d(M))
+        return M
+
+    def face_geom(self):
+        g = np.zeros((self.K, 3, 3))
+        self.L.orc_face_geom(self.h, _d(g))
+        return g
+
+    @staticmethod
+    def _bc(bc):
+        if bc is None:
+            return None
+        return np.ascontiguousarray(bc, np.float64)
+
+    def euler_rhs(self, q, flux=FLUX_LF, gamma=1.4, bc=None):
+        q = np.ascontiguousarray(q, np.float64)
+        out = np.zeros_like(q)
+        b = self._bc(bc)
+        self.L.orc_euler_rhs(self.h, _d(q), _d(out), flux, gamma, _d(b) if b is not None else None)
+        return out
+
+    def euler_weak(self, q, flux=FLUX_LF, gamma=1.4, bc=None):
+        q = np.ascontiguousarray(q, np.float64)
+        out = np.zeros_like(q)
+        b = self._bc(bc)
+        self.L.orc_euler_weak(self.h, _d(q), _d(out), flux, gamma, _d(b) if b is not None else None)
+        return out
+
+    def ssprk2(self, q, dt, nsteps, flux=FLUX_ROE, gamma=1.4, bc=None, t0=0.0):
+        q = np.array(q, np.float64, copy=True)
+        b = self._bc(bc)
+        self.L.orc_ssprk2(self.h, _d(q), dt, nsteps, flux, gamma, _d(b) if b is not None else None, t0)
+        return q
+
+    def lserk4(self, q, dt, nsteps, flux=FLUX_LF, gamma=1.4, res=None):
+        q = np.array(q, np.float64, copy=True)
+        res = np.zeros_like(q) if res is None else np.array(res, np.float64, copy=True)
+        self.L.orc_lserk4(self.h, _d(q), _d(res), dt, nsteps, flux, gamma)
+        return q, res
+
+    def ipdg_blocks(self, tau_coef=20.0, gD=None):
+        Np = self.Np
+        diag = np.zeros((self.K, Np, Np))
+        off = np.zeros((self.K, 3, Np, Np))
+        b = np.zeros(self.K * Np)
+        g = None if gD is None else np.ascontiguousarray(gD, np.float64)
+        self.L.orc_ipdg_blocks(self.h, tau_coef, _d(g) if g is not None else None, _d(diag), _d(off), _d(b))
+        return diag, off, b
+
+    def blk_apply(self, diag, off, x):
+        x = np.ascontiguousarray(x, np.float64)
+        y = np.zeros_like(x)
+        self.L.orc_blk_apply(self.h, _d(diag), _d(off), _d(x), _d(y))
+        return y
+
+    def pcg_bj(self, diag, off, rhs, x0=None, rtol=1e-10, maxit=10000):
+        rhs = np.ascontiguousarray(rhs, np.float64)
+        x = np.zeros_like(rhs) if x0 is None else np.array(x0, np.float64, copy=True)
+        rr = np.zeros(1)
+        it = self.L.orc_pcg_bj(self.h, _d(diag), _d(off), _d(rhs), _d(x), rtol, maxit, _d(rr))
+        return x, int(it), float(rr[0])
+
+
+def lserk4_coeffs():
+    a, b, c = np.zeros(5), np.zeros(5), np.zeros(5)
+    lib().orc_lserk4_coeffs(_d(a), _d(b), _d(c))
+    return a, b, c
+
+
+def set_threads(n):
+    lib().orc_set_threads(int(n))
+
+
+def max_threads():
+    return int(lib().orc_max_threads())

@@ -1,0 +1,41 @@
+import os
+import sys
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+GOLDEN = os.path.join(ROOT, "tests", "golden")
+
+
+def pytest_configure(config):
+    config.addinivalue_line("markers", "gpu: needs a CUDA GPU (GB300, sm_103a) and the built libdgcu.so")
+
+
+def golden_mesh(name):
+    from hopefoam_gb300.mesh import Mesh, connect
+
+    d = np.load(os.path.join(GOLDEN, name + ".npz"))
+    EToV, VXY = d["EToV"], d["VXY"]
+    EToE, EToF, ROT, BC = connect(EToV)
+    return Mesh(EToV, VXY, EToE, EToF, ROT, BC, name=name)
+
+
+def rel_l2(a, b):
+    a = np.asarray(a, np.float64)
+    b = np.asarray(b, np.float64)
+    return float(np.linalg.norm((a - b).ravel()) / max(np.linalg.norm(b.ravel()), 1e-300))
+
+
+@pytest.fixture(scope="session")
+def gpu_lib():
+    """The product library on a GPU; fails (not skips) when it cannot load."""
+    import __graft_entry__ as g
+
+    g.build()
+    from hopefoam_gb300 import _lib
+
+    return _lib.lib()

@@ -1,0 +1,127 @@
+"""GPU parity of the Euler hot path (FP64) against the CPU oracle, through the
+C ABI.
+
+Tolerances (FP64 path, round-off only): states (fields) 1e-12 relative L2;
+right-hand sides 1e-11 relative L2 -- R is a difference of O(|F|/h) volume
+and face terms, so its relative round-off is the conditioning of that
+cancellation times eps (observed up to ~1e-12)."""
+import json
+import os
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN, golden_mesh, rel_l2
+
+pytestmark = pytest.mark.gpu
+
+TOL_FP64 = 1e-12
+TOL_RHS = 1e-11
+
+
+def _setup(mesh, N):
+    from hopefoam_gb300 import euler
+    from hopefoam_gb300.mesh import load_cubature
+    from oracle import oracle
+
+    ctx = euler.EulerContext(mesh, N)
+    orc = oracle.Oracle(mesh, N, load_cubature(3 * (N + 1)))
+    ops = euler.reference_operators(N)
+    x, y = euler.node_coords(mesh, ops["r"], ops["s"])
+    return ctx, orc, x, y
+
+
+@pytest.mark.parametrize("N", [1, 2, 3, 4, 5, 6, 7])
+@pytest.mark.parametrize("flux", [0, 1])
+def test_rhs_periodic_perturbed(gpu_lib, N, flux):
+    from hopefoam_gb300 import euler
+    from hopefoam_gb300.mesh import periodic_square
+
+    m = periodic_square(6, 5, 10.0, 10.0, perturb=0.1, seed=N)
+    ctx, orc, x, y = _setup(m, N)
+    q = euler.isentropic_vortex(x, y, x0=5.0, y0=5.0, uinf=0.7, vinf=0.2)
+    ctx.upload(q)
+    g = ctx.rhs(flux=flux)
+    r = orc.euler_rhs(q.reshape(-1), flux=flux).reshape(g.shape)
+    err = rel_l2(g, r)
+    print("N=%d flux=%d rhs rel L2 %.3e" % (N, flux, err))
+    assert err < TOL_RHS
+    # per-variable check too (energy dominates the norm otherwise)
+    for v in range(4):
+        assert rel_l2(g[v], r[v]) < 10 * TOL_RHS
+    # state round trip through the ring layout is exact
+    assert np.array_equal(ctx.download(), q)
+
+
+def test_rhs_fixed_value_boundary(gpu_lib):
+    from hopefoam_gb300 import euler
+
+    m = golden_mesh("vortex0256")
+    N = 3
+    ctx, orc, x, y = _setup(m, N)
+    q = euler.isentropic_vortex(x, y)
+    tr = euler.boundary_traces_from_nodes(m, N, lambda a, b: euler.isentropic_vortex(a, b, t=0.1), x, y)
+    ctx.set_boundary_traces(tr)
+    ctx.upload(q)
+    for flux in (0, 1):
+        g = ctx.rhs(flux=flux)
+        # oracle boundary descriptor: beta, x0, y0, u_inf, gamma, t
+        r = orc.euler_rhs(q.reshape(-1), flux=flux, bc=[5.0, 5.0, 0.0, 1.0, 1.4, 0.1]).reshape(g.shape)
+        assert rel_l2(g, r) < TOL_RHS
+
+
+@pytest.mark.parametrize("N", [2, 5])
+def test_lserk4_steps(gpu_lib, N):
+    from hopefoam_gb300 import euler
+    from hopefoam_gb300.mesh import periodic_square
+
+    m = periodic_square(8, 8, 10.0, 10.0, perturb=0.1, seed=3)
+    ctx, orc, x, y = _setup(m, N)
+    q = euler.isentropic_vortex(x, y, x0=5.0, y0=5.0)
+    ctx.upload(q)
+    dt = 0.5 * ctx.cfl_dt(0.5)
+    ctx.lserk4(dt, 4, flux=0)
+    qo, _ = orc.lserk4(q.reshape(-1), dt, 4, flux=0)
+    assert rel_l2(ctx.download().reshape(-1), qo) < TOL_FP64
+
+
+def test_ssprk2_vortex_kat(gpu_lib):
+    """The reference's isentropic-vortex case end to end on the GPU: Roe flux,
+    SSP-RK2, exact boundary values set at t^n each step, t = 2 on the 256
+    triangle tutorial mesh.  Matches the oracle to round-off and the published
+    error (slide 18) to 1%."""
+    from hopefoam_gb300 import euler
+
+    kat = json.load(open(os.path.join(GOLDEN, "vortex_kat.json")))
+    m = golden_mesh("vortex0256")
+    N = 2
+    ctx, orc, x, y = _setup(m, N)
+    q0 = euler.isentropic_vortex(x, y)
+    ctx.upload(q0)
+    dt, nsteps = 0.008, 250
+    for n in range(nsteps):
+        t = n * dt
+        ctx.set_boundary_traces(euler.boundary_traces_from_nodes(m, N, lambda a, b: euler.isentropic_vortex(a, b, t=t),
+                                                                 x, y))
+        ctx.ssprk2(dt, 1, flux=1)
+    qg = ctx.download()
+    qo = orc.ssprk2(q0.reshape(-1), dt, nsteps, flux=1, bc=[5.0, 5.0, 0.0, 1.0, 1.4, 0.0]).reshape(qg.shape)
+    assert rel_l2(qg, qo) < 1e-11
+    qe = euler.isentropic_vortex(x, y, t=nsteps * dt)
+    err_rho = np.abs(qg[0] - qe[0]).mean()
+    pub = kat["table"][str(N)]["rho"][0]
+    assert abs(err_rho - pub) / pub < 0.01, (err_rho, pub)
+
+
+def test_errors_are_reported(gpu_lib):
+    from hopefoam_gb300 import _lib as L
+    from hopefoam_gb300 import euler
+    from hopefoam_gb300.mesh import periodic_square
+
+    m = periodic_square(4, 4, 1.0, 1.0)
+    ctx = euler.EulerContext(m, 3)
+    with pytest.raises(L.DGError) as e:
+        ctx.rhs(flux=7)
+    assert e.value.code == L.DG_ERR_ARG
+    with pytest.raises(L.DGError):
+        ctx.lserk4(-1.0, 1)

@@ -77,6 +77,19 @@ int run_stage(dg_ctx* c, const EulerArgs& a, int precision) {
     return DG_OK;
 }
 
+// The split kernel reports bounded-wait timeouts in a device status word.
+int check_split_status(dg_ctx* c, int precision) {
+    if (precision != DG_PREC_SPLIT) return DG_OK;
+    int st = 0;
+    DG_CUDA(c, cudaMemcpyAsync(&st, c->split.d_status, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+    DG_CUDA(c, cudaStreamSynchronize(c->stream));
+    if (st != 0) {
+        cudaMemsetAsync(c->split.d_status, 0, sizeof(int), c->stream);
+        return fail(c, DG_ERR_TIMEOUT, "split kernel: tensor-core completion wait timed out");
+    }
+    return DG_OK;
+}
+
 int check_run_args(dg_ctx* c, int flux, int precision) {
     if (!c) return DG_ERR_ARG;
     if (flux != DG_FLUX_LF && flux != DG_FLUX_ROE) return fail(c, DG_ERR_ARG, "unknown flux");
@@ -279,6 +292,8 @@ int dg_euler_rhs(dg_ctx* c, int flux, int precision, double* rhs_host) {
     a.mode = MODE_RHS;
     rc = run_stage(c, a, precision);
     if (rc) return rc;
+    rc = check_split_status(c, precision);
+    if (rc) return rc;
     cudaError_t e = launch_to_reference(a.rhs, c->d_stage, c->d_ring, c->K, c->Np, c->stream);
     if (e != cudaSuccess) return cuda_fail(c, e, "to_reference");
     DG_CUDA(c, cudaMemcpyAsync(rhs_host, c->d_stage, (size_t)c->K * 4 * c->Np * sizeof(double), cudaMemcpyDeviceToHost,
@@ -305,7 +320,7 @@ int dg_lserk4_step(dg_ctx* c, double dt, int nsteps, int flux, int precision) {
             if (rc) return rc;
             c->cur ^= 1;
         }
-    return DG_OK;
+    return check_split_status(c, precision);
 }
 
 int dg_ssprk2_step(dg_ctx* c, double dt, int nsteps, int flux, int precision) {
@@ -329,7 +344,7 @@ int dg_ssprk2_step(dg_ctx* c, double dt, int nsteps, int flux, int precision) {
         rc = run_stage(c, a, precision);
         if (rc) return rc;
     }
-    return DG_OK;
+    return check_split_status(c, precision);
 }
 
 int dg_cfl_dt(dg_ctx* c, double cfl, double* dt) {

@@ -15,9 +15,12 @@ namespace dgk {
 struct SplitPlan {
     bool ready = false;
     int N = 0;
-    void* d_ops = nullptr;  // packed operator image (see euler_split.cu)
+    int sms = 0;
+    void* d_ops = nullptr;    // operator images B1 | B2 (see euler_split.cu)
     size_t ops_bytes = 0;
-    int* d_status = nullptr;
+    size_t b2_offset = 0;     // in floats
+    int* d_status = nullptr;  // bounded-wait timeout flag
+    float* d_res32 = nullptr; // FP32 low-storage RK register
 };
 
 cudaError_t launch_euler_split(int N, const EulerArgs& a, const SplitPlan& plan, cudaStream_t s);

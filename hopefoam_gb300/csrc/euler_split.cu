@@ -1,17 +1,528 @@
-// euler_split.cu -- split-precision DG Euler stage (placeholder until the
-// tensor-core kernel lands: reports "not built").
+// euler_split.cu -- split-precision fused DG Euler stage on the tcgen05 tensor
+// cores (sm_103a).
+//
+// Arithmetic: the two contractions of the quadrature-form DG right-hand side
+// run as TF32 GEMMs with 3-pass split products (hi*hi + lo*hi + hi*lo) and
+// FP32 accumulation in tensor memory:
+//   GEMM1 (cubature interpolation, dgGaussField.C:193-202):
+//     Qg[r][g] = sum_p Q[r][p] Vg[g][p],        M = 128 rows r = v*32 + e
+//                                               (4 variables x 32 elements),
+//                                               N = Ng padded, K = Np padded
+//   GEMM2 (volume term + surface lift with the affine mass inverse folded in,
+//          defaultConvectionScheme.C:79-128, defaultGrad.C:120-165,
+//          defaultDivScheme.C:118-165):
+//     R[r][p] = sum_g Fr[r][g] Sr[p][g] + Fs[r][g] Ss[p][g]
+//             + sum_c (-sJ/J F*)[r][c] Lift[p][c],   N = Np padded
+// Point-wise fluxes (volume and face) are FP32 SIMT.  The state q stays FP64
+// in HBM; the low-storage RK register is FP32 (it carries dt*R, whose own
+// precision is FP32); q += b*res is the only FP64 instruction per value.
+//
+// Structure: persistent CTAs (one per SM, 256 threads), 32 elements per tile.
+// Per tile: stage q (FP64 -> FP32 -> TF32 hi/lo in the canonical no-swizzle
+// K-major layout, see umma.cuh) -> GEMM1 (issued by one thread, completion on
+// an mbarrier) -> face fluxes while GEMM1 runs -> for each chunk of 16
+// cubature points: tensor memory -> shared exchange -> FP32 flux -> TF32
+// split -> GEMM2 MMAs for that K chunk -> epilogue: tensor memory -> shared ->
+// coalesced LSERK update.  All mbarrier waits are bounded; a timeout sets the
+// status word, the CTA drains its MMAs, frees tensor memory and returns.
+#include <cstdio>
+#include <cstring>
+#include <vector>
+
 #include "../../include/dgcu.h"
 #include "dg_ctx.hpp"
+#include "euler_flux.cuh"
+#include "umma.cuh"
 
 namespace dgk {
 
-cudaError_t launch_euler_split(int, const EulerArgs&, const SplitPlan&, cudaStream_t) { return cudaErrorNotSupported; }
+template <int N>
+struct SplitDims {
+    static constexpr int Np = Dims<N>::Np, Ng = Dims<N>::Ng, Nfp = Dims<N>::Nfp, Nfq = Dims<N>::Nfq;
+    static constexpr int E = 32, ROWS = 128, THREADS = 256;
+    static constexpr int KP1 = (Np + 7) / 8 * 8;      // GEMM1 K (padded nodes)
+    static constexpr int NG = (Ng + 15) / 16 * 16;    // GEMM1 N (padded cubature points)
+    static constexpr int NF = (3 * Nfq + 7) / 8 * 8;  // face-flux K
+    static constexpr int KP2 = 2 * NG + NF;           // GEMM2 K
+    static constexpr int NP2 = (Np + 15) / 16 * 16;   // GEMM2 N
+    static constexpr int CH = 16;                     // cubature points per chunk
+    static constexpr int NCH = NG / CH;
+    static constexpr int KC = 2 * CH;                 // chunk buffer K: [Fr 16 | Fs 16]
+    // shared-memory layout (bytes, operand buffers 1024-aligned)
+    static constexpr int SZ_B1 = 2 * NG * KP1 * 4;    // Vg hi/lo
+    static constexpr int SZ_B2 = 2 * NP2 * KP2 * 4;   // [Sr|Ss|Lift] hi/lo
+    static constexpr int SZ_A1 = 2 * ROWS * KP1 * 4;  // Q hi/lo
+    static constexpr int SZ_AC = 2 * ROWS * KC * 4;   // flux chunk hi/lo
+    static constexpr int SZ_AF = 2 * ROWS * NF * 4;   // face flux hi/lo
+    static constexpr int SZ_X = 4 * CH * E * 4;       // exchange q at cubature points
+    static constexpr int SZ_QF = E * 4 * Np * 4;      // FP32 copy of the tile state
+    static constexpr int al(int x) { return (x + 1023) / 1024 * 1024; }
+    static constexpr int OFF_B1 = 0;
+    static constexpr int OFF_B2 = OFF_B1 + al(SZ_B1);
+    static constexpr int OFF_A1 = OFF_B2 + al(SZ_B2);
+    static constexpr int OFF_AC = OFF_A1 + al(SZ_A1);
+    static constexpr int OFF_AF = OFF_AC + al(SZ_AC);
+    static constexpr int OFF_X = OFF_AF + al(SZ_AF);
+    static constexpr int OFF_QF = OFF_X + al(SZ_X);
+    static constexpr int OFF_BAR = OFF_QF + al(SZ_QF);
+    static constexpr int SMEM = OFF_BAR + 64;
+    static constexpr int RS_FLOATS = E * 4 * Np;      // epilogue staging (aliases the chunk buffer)
+    static_assert(RS_FLOATS * 4 <= SZ_AC, "epilogue staging does not fit");
+    static constexpr int TMEM_COLS = 256;
+    static constexpr int D2_COL = 128;
+    static_assert(NG <= 128 && NP2 <= 128, "tensor memory layout");
+};
+
+struct SplitArgs {
+    EulerArgs e;
+    const float* res32;  // FP32 low-storage RK register (read)
+    float* res32_out;    // (write, may alias res32: element-local)
+    const float* b1;     // device image of B1 (canonical layout, hi then lo)
+    const float* b2;     // device image of B2
+    int* status;         // nonzero on a bounded-wait timeout
+};
+
+constexpr uint32_t kWaitLimit = 1u << 22;
+
+template <int N>
+__global__ void __launch_bounds__(256, 1) euler_stage_split_kernel(SplitArgs sa) {
+    using D = SplitDims<N>;
+    constexpr int Np = D::Np, Ng = D::Ng, Nfp = D::Nfp, Nfq = D::Nfq, E = D::E;
+    constexpr int KP1 = D::KP1, NG = D::NG, NF = D::NF, NP2 = D::NP2, KP2 = D::KP2, CH = D::CH, KC = D::KC;
+    constexpr int NB = 3 * N;
+    extern __shared__ __align__(1024) unsigned char smem[];
+    float* sB1 = reinterpret_cast<float*>(smem + D::OFF_B1);
+    float* sB2 = reinterpret_cast<float*>(smem + D::OFF_B2);
+    float* sA1 = reinterpret_cast<float*>(smem + D::OFF_A1);
+    float* sAC = reinterpret_cast<float*>(smem + D::OFF_AC);
+    float* sAF = reinterpret_cast<float*>(smem + D::OFF_AF);
+    float* sX = reinterpret_cast<float*>(smem + D::OFF_X);
+    float* sQF = reinterpret_cast<float*>(smem + D::OFF_QF);
+    float* sRS = sAC;  // epilogue staging, used only after GEMM2 completed
+    uint64_t* bar1 = reinterpret_cast<uint64_t*>(smem + D::OFF_BAR);
+    uint64_t* bar2 = bar1 + 1;
+    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bar1 + 2);
+
+    const EulerArgs& a = sa.e;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int ntiles = (a.K + E - 1) / E;
+    const float gamma = (float)a.gamma;
+
+    // constant operands and zero padding, once per CTA
+    {
+        const int4* src1 = reinterpret_cast<const int4*>(sa.b1);
+        int4* dst1 = reinterpret_cast<int4*>(sB1);
+        for (int i = tid; i < D::SZ_B1 / 16; i += blockDim.x) dst1[i] = src1[i];
+        const int4* src2 = reinterpret_cast<const int4*>(sa.b2);
+        int4* dst2 = reinterpret_cast<int4*>(sB2);
+        for (int i = tid; i < D::SZ_B2 / 16; i += blockDim.x) dst2[i] = src2[i];
+        for (int i = tid; i < D::SZ_A1 / 4; i += blockDim.x) sA1[i] = 0.f;
+        for (int i = tid; i < D::SZ_AF / 4; i += blockDim.x) sAF[i] = 0.f;
+    }
+    if (tid == 0) {
+        umma::mbar_init(bar1, 1);
+        umma::mbar_init(bar2, 1);
+        umma::fence_mbar_init();
+    }
+    if (warp == 0) {
+        umma::tmem_alloc(tmem_slot, D::TMEM_COLS);
+        umma::tmem_relinquish();
+    }
+    umma::fence_async_smem();
+    umma::fence_before_sync();
+    __syncthreads();
+    umma::fence_after_sync();
+    const uint32_t tmem = *tmem_slot;
+    const uint32_t tD1 = tmem, tD2 = tmem + D::D2_COL;
+    const uint32_t idesc1 = umma::idesc_tf32(128, NG);
+    const uint32_t idesc2 = umma::idesc_tf32(128, NP2);
+    const uint32_t aB1 = umma::smem_u32(sB1), aB2 = umma::smem_u32(sB2);
+    const uint32_t aA1 = umma::smem_u32(sA1), aAC = umma::smem_u32(sAC), aAF = umma::smem_u32(sAF);
+    constexpr uint32_t LO_B1 = NG * KP1 * 4, LO_B2 = NP2 * KP2 * 4, LO_A1 = 128 * KP1 * 4, LO_AC = 128 * KC * 4,
+                       LO_AF = 128 * NF * 4;
+    uint32_t ph1 = 0, ph2 = 0;
+    bool failed = false;
+
+    for (int tile = blockIdx.x; tile < ntiles && !failed; tile += gridDim.x) {
+        const int k0 = tile * E;
+        const int ne = min(E, a.K - k0);
+        // ---- (A) stage the tile: FP64 -> FP32 copy + TF32 hi/lo operand
+        const double* qin = a.qin + (size_t)k0 * 4 * Np;
+        for (int i = tid; i < ne * 4 * Np; i += blockDim.x) {
+            const float x = (float)qin[i];
+            sQF[i] = x;
+            const int e = i / (4 * Np), rem = i - e * 4 * Np, v = rem / Np, p = rem - v * Np;
+            const int r = v * 32 + e;
+            float hi, lo;
+            umma::split_tf32(x, hi, lo);
+            const uint32_t off = umma::kmajor_offset(r, p, KP1) >> 2;
+            sA1[off] = hi;
+            sA1[off + LO_A1 / 4] = lo;
+        }
+        umma::fence_async_smem();
+        umma::fence_before_sync();
+        __syncthreads();
+        umma::fence_after_sync();
+        if (tid == 0) {
+            // GEMM1: D1 = Q (hi,lo) x Vg (hi,lo)^T, 3 passes per K=8 step
+#pragma unroll
+            for (int s = 0; s < KP1 / 8; s++) {
+                const uint64_t ah = umma::smem_desc(aA1 + s * 256, 128, (KP1 / 4) * 128);
+                const uint64_t al = umma::smem_desc(aA1 + LO_A1 + s * 256, 128, (KP1 / 4) * 128);
+                const uint64_t bh = umma::smem_desc(aB1 + s * 256, 128, (KP1 / 4) * 128);
+                const uint64_t bl = umma::smem_desc(aB1 + LO_B1 + s * 256, 128, (KP1 / 4) * 128);
+                umma::mma_tf32(tD1, ah, bh, idesc1, s > 0);
+                umma::mma_tf32(tD1, al, bh, idesc1, 1);
+                umma::mma_tf32(tD1, ah, bl, idesc1, 1);
+            }
+            umma::commit(bar1);
+        }
+        // ---- (B) face fluxes while GEMM1 runs: one thread per (element, face)
+        if (tid < 3 * E) {
+            const int e = tid / 3, f = tid - 3 * e;
+            if (e < ne) {
+                const int k = k0 + e;
+                double nxd, nyd, fscd;
+                const double* gk = a.geo + (size_t)k * 4;
+                face_normal(f, gk[0], gk[1], gk[2], gk[3], nxd, nyd, fscd);
+                const float nx = (float)nxd, ny = (float)nyd, fsc = (float)fscd;
+                float um[4][Nfp], up[4][Nfp];
+                const float* qe = sQF + e * 4 * Np;
+#pragma unroll
+                for (int j = 0; j < Nfp; j++) {
+                    const int pos = (f * N + j) % NB;
+#pragma unroll
+                    for (int v = 0; v < 4; v++) um[v][j] = qe[v * Np + pos];
+                }
+                const int c = __ldg(a.conn + (size_t)k * 3 + f);
+                if (c >= 0) {
+                    const int nb = c >> 3, fn = c & 3, rot = (c >> 2) & 1;
+                    const double* qn = a.qin + (size_t)nb * 4 * Np;
+#pragma unroll
+                    for (int j = 0; j < Nfp; j++) {
+                        const int jj = rot ? (N - j) : j;
+                        const int pos = (fn * N + jj) % NB;
+#pragma unroll
+                        for (int v = 0; v < 4; v++) up[v][j] = (float)__ldg(qn + v * Np + pos);
+                    }
+                } else {
+                    const double* bt = a.btrace + (size_t)(-1 - c) * 4 * Nfp;
+#pragma unroll
+                    for (int j = 0; j < Nfp; j++)
+#pragma unroll
+                        for (int v = 0; v < 4; v++) up[v][j] = (float)__ldg(bt + v * Nfp + j);
+                }
+                float qm[Nfq][4], qp[Nfq][4];
+#pragma unroll
+                for (int i = 0; i < Nfq; i++)
+#pragma unroll
+                    for (int v = 0; v < 4; v++) {
+                        float s1 = 0.f, s2 = 0.f;
+#pragma unroll
+                        for (int j = 0; j < Nfp; j++) {
+                            const float w = (float)__ldg(a.ops.If + i * Nfp + j);
+                            s1 = fmaf(w, um[v][j], s1);
+                            s2 = fmaf(w, up[v][j], s2);
+                        }
+                        qm[i][v] = s1;
+                        qp[i][v] = s2;
+                    }
+                float lam = 0.f;
+                if (a.flux != 1) {
+#pragma unroll
+                    for (int i = 0; i < Nfq; i++) {
+                        lam = fmaxf(lam, wave_speed(gamma, nx, ny, qm[i]));
+                        lam = fmaxf(lam, wave_speed(gamma, nx, ny, qp[i]));
+                    }
+                }
+#pragma unroll
+                for (int i = 0; i < Nfq; i++) {
+                    float F[4];
+                    if (a.flux == 1) roe_flux(gamma, nx, ny, qm[i], qp[i], F);
+                    else lf_flux(gamma, nx, ny, lam, qm[i], qp[i], F);
+#pragma unroll
+                    for (int v = 0; v < 4; v++) {
+                        float hi, lo;
+                        umma::split_tf32(-fsc * F[v], hi, lo);
+                        const uint32_t off = umma::kmajor_offset(v * 32 + e, f * Nfq + i, NF) >> 2;
+                        sAF[off] = hi;
+                        sAF[off + LO_AF / 4] = lo;
+                    }
+                }
+            }
+        }
+        // ---- (C) wait for GEMM1, then the volume flux per chunk of cubature points
+        bool ok = umma::mbar_wait(bar1, ph1, kWaitLimit);
+        ph1 ^= 1;
+        if (__syncthreads_or(!ok)) { failed = true; break; }
+        umma::fence_after_sync();
+        // metrics of this thread's flux points (same element for both points: e = lane)
+        float rx = 0.f, sx = 0.f, ry = 0.f, sy = 0.f;
+        if (lane < ne) {
+            const double* gk = a.geo + (size_t)(k0 + lane) * 4;
+            rx = (float)gk[0]; sx = (float)gk[1]; ry = (float)gk[2]; sy = (float)gk[3];
+        }
+        for (int ch = 0; ch < D::NCH; ch++) {
+            // tensor memory -> exchange buffer: warp w reads lanes of quarter (w & 3) = variable v
+            {
+                const int v = warp & 3, half = warp >> 2;
+                float val[8];
+                umma::tmem_ld8(tD1 + ((uint32_t)(32 * v) << 16) + ch * CH + half * 8, val);
+                umma::tmem_ld_wait();
+#pragma unroll
+                for (int j = 0; j < 8; j++) sX[(v * CH + half * 8 + j) * E + lane] = val[j];
+            }
+            __syncthreads();
+            // FP32 flux for 2 points per thread: (g = warp*2 + j, e = lane)
+            float fr[2][4], fs[2][4];
+#pragma unroll
+            for (int j = 0; j < 2; j++) {
+                const int gl = warp * 2 + j;
+                const int g = ch * CH + gl;
+                if (g < Ng && lane < ne) {
+                    float q[4], fx[4], fy[4];
+#pragma unroll
+                    for (int v = 0; v < 4; v++) q[v] = sX[(v * CH + gl) * E + lane];
+                    euler_phys_flux(gamma, q, fx, fy);
+#pragma unroll
+                    for (int v = 0; v < 4; v++) {
+                        fr[j][v] = rx * fx[v] + ry * fy[v];
+                        fs[j][v] = sx * fx[v] + sy * fy[v];
+                    }
+                } else {
+#pragma unroll
+                    for (int v = 0; v < 4; v++) fr[j][v] = fs[j][v] = 0.f;
+                }
+            }
+            // the previous chunk's MMAs must have consumed the chunk buffer
+            if (ch > 0) {
+                ok = umma::mbar_wait(bar2, ph2, kWaitLimit);
+                ph2 ^= 1;
+                if (__syncthreads_or(!ok)) { failed = true; break; }
+            }
+#pragma unroll
+            for (int j = 0; j < 2; j++) {
+                const int gl = warp * 2 + j;
+#pragma unroll
+                for (int v = 0; v < 4; v++) {
+                    const int r = v * 32 + lane;
+                    float hi, lo;
+                    umma::split_tf32(fr[j][v], hi, lo);
+                    uint32_t off = umma::kmajor_offset(r, gl, KC) >> 2;
+                    sAC[off] = hi;
+                    sAC[off + LO_AC / 4] = lo;
+                    umma::split_tf32(fs[j][v], hi, lo);
+                    off = umma::kmajor_offset(r, CH + gl, KC) >> 2;
+                    sAC[off] = hi;
+                    sAC[off + LO_AC / 4] = lo;
+                }
+            }
+            umma::fence_async_smem();
+            umma::fence_before_sync();
+            __syncthreads();
+            umma::fence_after_sync();
+            if (tid == 0) {
+                constexpr uint32_t sboA = (KC / 4) * 128, sboB = (KP2 / 4) * 128;
+#pragma unroll
+                for (int s = 0; s < KC / 8; s++) {
+                    // chunk K step s: Fr part (s < 2) at B2 k = ch*CH + 8s, Fs part at NG + ch*CH + 8(s-2)
+                    const int kb = (s < CH / 8) ? (ch * CH + 8 * s) : (NG + ch * CH + 8 * (s - CH / 8));
+                    const uint64_t ah = umma::smem_desc(aAC + s * 256, 128, sboA);
+                    const uint64_t al = umma::smem_desc(aAC + LO_AC + s * 256, 128, sboA);
+                    const uint64_t bh = umma::smem_desc(aB2 + kb * 32, 128, sboB);
+                    const uint64_t bl = umma::smem_desc(aB2 + LO_B2 + kb * 32, 128, sboB);
+                    const uint32_t acc = (ch > 0 || s > 0) ? 1u : 0u;
+                    umma::mma_tf32(tD2, ah, bh, idesc2, acc);
+                    umma::mma_tf32(tD2, al, bh, idesc2, 1);
+                    umma::mma_tf32(tD2, ah, bl, idesc2, 1);
+                }
+                if (ch == D::NCH - 1) {
+                    constexpr uint32_t sboF = (NF / 4) * 128;
+#pragma unroll
+                    for (int s = 0; s < NF / 8; s++) {
+                        const int kb = 2 * NG + 8 * s;
+                        const uint64_t ah = umma::smem_desc(aAF + s * 256, 128, sboF);
+                        const uint64_t al = umma::smem_desc(aAF + LO_AF + s * 256, 128, sboF);
+                        const uint64_t bh = umma::smem_desc(aB2 + kb * 32, 128, sboB);
+                        const uint64_t bl = umma::smem_desc(aB2 + LO_B2 + kb * 32, 128, sboB);
+                        umma::mma_tf32(tD2, ah, bh, idesc2, 1);
+                        umma::mma_tf32(tD2, al, bh, idesc2, 1);
+                        umma::mma_tf32(tD2, ah, bl, idesc2, 1);
+                    }
+                }
+                umma::commit(bar2);
+            }
+        }
+        if (failed) break;
+        ok = umma::mbar_wait(bar2, ph2, kWaitLimit);
+        ph2 ^= 1;
+        if (__syncthreads_or(!ok)) { failed = true; break; }
+        umma::fence_after_sync();
+        // ---- (D) epilogue: R (tensor memory) -> staging -> coalesced stage update
+        {
+            const int v = warp & 3, half = warp >> 2;
+#pragma unroll
+            for (int c0 = 0; c0 < NP2 / 2; c0 += 8) {
+                const int col = half * (NP2 / 2) + c0;
+                float val[8];
+                umma::tmem_ld8(tD2 + ((uint32_t)(32 * v) << 16) + col, val);
+                umma::tmem_ld_wait();
+#pragma unroll
+                for (int j = 0; j < 8; j++) {
+                    const int p = col + j;
+                    if (p < Np && lane < ne) sRS[(lane * 4 + v) * Np + p] = val[j];
+                }
+            }
+        }
+        umma::fence_before_sync();
+        __syncthreads();
+        {
+            const size_t base = (size_t)k0 * 4 * Np;
+            const bool first = (a.rka == 0.0);
+            const float rka = (float)a.rka, dtf = (float)a.dt, rkb = (float)a.rkb;
+            for (int i = tid; i < ne * 4 * Np; i += blockDim.x) {
+                const float R = sRS[i];
+                const size_t idx = base + i;
+                switch (a.mode) {
+                    case MODE_RHS: a.rhs[idx] = (double)R; break;
+                    case MODE_LSERK: {
+                        const float r = first ? dtf * R : fmaf(rka, sa.res32[idx], dtf * R);
+                        sa.res32_out[idx] = r;
+                        a.qout[idx] = a.qin[idx] + (double)(rkb * r);
+                    } break;
+                    case MODE_EULER: a.qout[idx] = a.qin[idx] + (double)(dtf * R); break;
+                    default: a.qout[idx] = 0.5 * a.qold[idx] + 0.5 * (a.qin[idx] + (double)(dtf * R)); break;
+                }
+            }
+        }
+        __syncthreads();  // staging buffers are rewritten by the next tile
+    }
+    if (failed && tid == 0) atomicExch(sa.status, 1);
+    // drain: make sure no MMA is still writing tensor memory before freeing it
+    umma::fence_before_sync();
+    __syncthreads();
+    if (warp == 0) umma::tmem_dealloc(tmem, D::TMEM_COLS);
+}
+
+// ---------------------------------------------------------------------------
+// host side: operator images and launch
+
+static inline float tf32_rna(float x) {
+    uint32_t u;
+    memcpy(&u, &x, 4);
+    u = (u + 0x1000u) & 0xFFFFE000u;
+    float r;
+    memcpy(&r, &u, 4);
+    return r;
+}
+
+// canonical K-major image of an (rows x KP) operand given by f(row, k) (double),
+// hi part then lo part
+template <typename F>
+static std::vector<float> operand_image(int rows, int KP, F f) {
+    std::vector<float> img((size_t)2 * rows * KP, 0.f);
+    const size_t lo = (size_t)rows * KP;
+    for (int r = 0; r < rows; r++)
+        for (int k = 0; k < KP; k++) {
+            const double x = f(r, k);
+            const float hi = tf32_rna((float)x);
+            const float l = (float)(x - (double)hi);
+            const size_t off = umma::kmajor_offset(r, k, KP) >> 2;
+            img[off] = hi;
+            img[lo + off] = l;
+        }
+    return img;
+}
+
+template <int N>
+static int setup_n(dg_ctx* c) {
+    using D = SplitDims<N>;
+    const dgb::RefOps& o = c->ops;
+    const int Np = D::Np, Ng = D::Ng, Nfq = D::Nfq, NG = D::NG;
+    std::vector<float> b1 = operand_image(D::NG, D::KP1, [&](int g, int p) {
+        return (g < Ng && p < Np) ? o.dVg[(size_t)g * Np + p] : 0.0;
+    });
+    std::vector<float> b2 = operand_image(D::NP2, D::KP2, [&](int p, int k) {
+        if (p >= Np) return 0.0;
+        if (k < NG) return k < Ng ? o.dSr[(size_t)p * Ng + k] : 0.0;
+        if (k < 2 * NG) return (k - NG) < Ng ? o.dSs[(size_t)p * Ng + (k - NG)] : 0.0;
+        const int cc = k - 2 * NG;
+        return cc < 3 * Nfq ? o.dLift[(size_t)p * 3 * Nfq + cc] : 0.0;
+    });
+    size_t bytes = (b1.size() + b2.size()) * sizeof(float);
+    float* d = nullptr;
+    if (cudaMalloc(&d, bytes) != cudaSuccess) return DG_ERR_NOMEM;
+    cudaMemcpy(d, b1.data(), b1.size() * 4, cudaMemcpyHostToDevice);
+    cudaMemcpy(d + b1.size(), b2.data(), b2.size() * 4, cudaMemcpyHostToDevice);
+    c->split.d_ops = d;
+    c->split.ops_bytes = bytes;
+    c->split.b2_offset = b1.size();
+    if (cudaMalloc(&c->split.d_status, sizeof(int)) != cudaSuccess) return DG_ERR_NOMEM;
+    cudaMemset(c->split.d_status, 0, sizeof(int));
+    if (cudaMalloc(&c->split.d_res32, (size_t)c->K * 4 * Np * sizeof(float)) != cudaSuccess) return DG_ERR_NOMEM;
+    cudaMemset(c->split.d_res32, 0, (size_t)c->K * 4 * Np * sizeof(float));
+    if (cudaFuncSetAttribute(euler_stage_split_kernel<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, D::SMEM) !=
+        cudaSuccess)
+        return DG_ERR_CUDA;
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    c->split.sms = sms;
+    c->split.N = N;
+    c->split.ready = true;
+    return DG_OK;
+}
+
+template <int N>
+static cudaError_t launch_split_n(const EulerArgs& a, const SplitPlan& plan, cudaStream_t s) {
+    using D = SplitDims<N>;
+    SplitArgs sa;
+    sa.e = a;
+    sa.res32 = plan.d_res32;
+    sa.res32_out = plan.d_res32;
+    sa.b1 = static_cast<const float*>(plan.d_ops);
+    sa.b2 = static_cast<const float*>(plan.d_ops) + plan.b2_offset;
+    sa.status = plan.d_status;
+    const int ntiles = (a.K + D::E - 1) / D::E;
+    const int grid = ntiles < plan.sms ? ntiles : plan.sms;
+    euler_stage_split_kernel<N><<<grid, D::THREADS, D::SMEM, s>>>(sa);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_euler_split(int N, const EulerArgs& a, const SplitPlan& plan, cudaStream_t s) {
+    if (!plan.ready || plan.N != N) return cudaErrorNotSupported;
+    switch (N) {
+        case 1: return launch_split_n<1>(a, plan, s);
+        case 2: return launch_split_n<2>(a, plan, s);
+        case 3: return launch_split_n<3>(a, plan, s);
+        case 4: return launch_split_n<4>(a, plan, s);
+        case 5: return launch_split_n<5>(a, plan, s);
+        case 6: return launch_split_n<6>(a, plan, s);
+        default: return cudaErrorNotSupported;
+    }
+}
 
 }  // namespace dgk
 
 int split_setup(dg_ctx* c) {
     c->split.ready = false;
-    return DG_ERR_UNSUPPORTED;
+    switch (c->N) {
+        case 1: return dgk::setup_n<1>(c);
+        case 2: return dgk::setup_n<2>(c);
+        case 3: return dgk::setup_n<3>(c);
+        case 4: return dgk::setup_n<4>(c);
+        case 5: return dgk::setup_n<5>(c);
+        case 6: return dgk::setup_n<6>(c);
+        default: return DG_ERR_UNSUPPORTED;  // N = 7 needs a streamed operator (does not fit shared memory)
+    }
 }
 
-void split_teardown(dg_ctx*) {}
+void split_teardown(dg_ctx* c) {
+    if (c->split.d_ops) cudaFree(c->split.d_ops);
+    if (c->split.d_status) cudaFree(c->split.d_status);
+    if (c->split.d_res32) cudaFree(c->split.d_res32);
+    c->split.d_ops = nullptr;
+    c->split.d_status = nullptr;
+    c->split.d_res32 = nullptr;
+    c->split.ready = false;
+}

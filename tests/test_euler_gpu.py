@@ -1,10 +1,12 @@
 """GPU parity of the Euler hot path (FP64) against the CPU oracle, through the
 C ABI.
 
-Tolerances (FP64 path, round-off only): states (fields) 1e-12 relative L2;
-right-hand sides 1e-11 relative L2 -- R is a difference of O(|F|/h) volume
-and face terms, so its relative round-off is the conditioning of that
-cancellation times eps (observed up to ~1e-12)."""
+Tolerances (FP64 path, round-off only): states (fields) 1e-12 relative L2.
+Right-hand sides: 1e-11 relative L2, or 10x the oracle's own sensitivity to a
+one-ulp perturbation of the mesh vertices when that is larger -- the
+reference computes the metrics through Dr.x at every cubature point, so the
+RHS carries a few ulps of geometry round-off that grows with the order
+(measured 2.8e-12 per ulp at N = 7)."""
 import json
 import os
 
@@ -31,6 +33,19 @@ def _setup(mesh, N):
     return ctx, orc, x, y
 
 
+def _vertex_ulp_sensitivity(mesh, N, q, flux, r0):
+    """Relative change of the oracle's RHS when every vertex coordinate moves
+    by one ulp (seeded)."""
+    from hopefoam_gb300.mesh import Mesh, load_cubature
+    from oracle import oracle
+
+    rng = np.random.default_rng(123)
+    v = mesh.VXY * (1 + rng.uniform(-1.1e-16, 1.1e-16, mesh.VXY.shape))
+    m2 = Mesh(mesh.EToV, v, mesh.EToE, mesh.EToF, mesh.ROT, mesh.BC)
+    o2 = oracle.Oracle(m2, N, load_cubature(3 * (N + 1)))
+    return rel_l2(o2.euler_rhs(q.reshape(-1), flux=flux), r0.reshape(-1))
+
+
 @pytest.mark.parametrize("N", [1, 2, 3, 4, 5, 6, 7])
 @pytest.mark.parametrize("flux", [0, 1])
 def test_rhs_periodic_perturbed(gpu_lib, N, flux):
@@ -44,11 +59,12 @@ def test_rhs_periodic_perturbed(gpu_lib, N, flux):
     g = ctx.rhs(flux=flux)
     r = orc.euler_rhs(q.reshape(-1), flux=flux).reshape(g.shape)
     err = rel_l2(g, r)
-    print("N=%d flux=%d rhs rel L2 %.3e" % (N, flux, err))
-    assert err < TOL_RHS
+    tol = max(TOL_RHS, 10 * _vertex_ulp_sensitivity(m, N, q, flux, r))
+    print("N=%d flux=%d rhs rel L2 %.3e (tol %.1e)" % (N, flux, err, tol))
+    assert err < tol
     # per-variable check too (energy dominates the norm otherwise)
     for v in range(4):
-        assert rel_l2(g[v], r[v]) < 10 * TOL_RHS
+        assert rel_l2(g[v], r[v]) < 10 * tol
     # state round trip through the ring layout is exact
     assert np.array_equal(ctx.download(), q)
 

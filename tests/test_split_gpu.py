@@ -1,0 +1,101 @@
+"""Split-precision (tcgen05 TF32 3-pass, FP32 accumulation, FP64 state)
+Euler path against the FP64 oracle, through the C ABI.
+
+Tolerances: the right-hand side carries FP32-level round-off amplified by the
+volume/face cancellation, bounded here at 5e-5 relative L2; the state after
+one LSERK4 step (5 stages) must stay within 1e-9 relative L2 of the FP64
+oracle (the per-step target)."""
+import numpy as np
+import pytest
+
+from conftest import golden_mesh, rel_l2
+
+pytestmark = pytest.mark.gpu
+
+TOL_RHS_SPLIT = 5e-5
+TOL_STEP_SPLIT = 1e-9
+
+
+def _setup(mesh, N):
+    from hopefoam_gb300 import euler
+    from hopefoam_gb300.mesh import load_cubature
+    from oracle import oracle
+
+    ctx = euler.EulerContext(mesh, N)
+    orc = oracle.Oracle(mesh, N, load_cubature(3 * (N + 1)))
+    ops = euler.reference_operators(N)
+    x, y = euler.node_coords(mesh, ops["r"], ops["s"])
+    return ctx, orc, x, y
+
+
+@pytest.mark.parametrize("N", [1, 2, 3, 4, 5, 6])
+@pytest.mark.parametrize("flux", [0, 1])
+def test_split_rhs(gpu_lib, N, flux):
+    from hopefoam_gb300 import _lib as L
+    from hopefoam_gb300 import euler
+    from hopefoam_gb300.mesh import periodic_square
+
+    nx = 24 if N <= 4 else 16
+    m = periodic_square(nx, nx, 10.0, 10.0, perturb=0.1, seed=N)
+    ctx, orc, x, y = _setup(m, N)
+    q = euler.isentropic_vortex(x, y, x0=5.0, y0=5.0, uinf=0.7, vinf=0.2)
+    ctx.upload(q)
+    g = ctx.rhs(flux=flux, precision=L.DG_PREC_SPLIT)
+    r = orc.euler_rhs(q.reshape(-1), flux=flux).reshape(g.shape)
+    err = rel_l2(g, r)
+    print("split N=%d flux=%d rhs rel L2 %.3e  max %.3e" % (N, flux, err, np.abs(g - r).max() / np.abs(r).max()))
+    assert np.isfinite(g).all()
+    assert err < TOL_RHS_SPLIT
+
+
+@pytest.mark.parametrize("N", [3, 5])
+def test_split_lserk4_step(gpu_lib, N):
+    from hopefoam_gb300 import _lib as L
+    from hopefoam_gb300 import euler
+    from hopefoam_gb300.mesh import periodic_square
+
+    m = periodic_square(32, 32, 10.0, 10.0, perturb=0.1, seed=0)
+    ctx, orc, x, y = _setup(m, N)
+    q = euler.isentropic_vortex(x, y, x0=5.0, y0=5.0)
+    ctx.upload(q)
+    dt = ctx.cfl_dt(0.5)
+    ctx.lserk4(dt, 1, flux=0, precision=L.DG_PREC_SPLIT)
+    qs = ctx.download()
+    qo, _ = orc.lserk4(q.reshape(-1), dt, 1, flux=0)
+    err = rel_l2(qs.reshape(-1), qo)
+    dq = rel_l2(qo, q.reshape(-1))
+    print("split N=%d one LSERK4 step: state rel L2 %.3e (change of state %.3e)" % (N, err, dq))
+    assert err < TOL_STEP_SPLIT
+
+
+def test_split_tail_tile_and_boundary(gpu_lib):
+    """K not a multiple of the 32-element tile, fixed-value boundary faces."""
+    from hopefoam_gb300 import _lib as L
+    from hopefoam_gb300 import euler
+
+    m = golden_mesh("vortex0256")
+    m2 = m
+    N = 3
+    ctx, orc, x, y = _setup(m2, N)
+    q = euler.isentropic_vortex(x, y)
+    tr = euler.boundary_traces_from_nodes(m2, N, lambda a, b: euler.isentropic_vortex(a, b, t=0.05), x, y)
+    ctx.set_boundary_traces(tr)
+    ctx.upload(q)
+    for flux in (0, 1):
+        g = ctx.rhs(flux=flux, precision=L.DG_PREC_SPLIT)
+        r = orc.euler_rhs(q.reshape(-1), flux=flux, bc=[5.0, 5.0, 0.0, 1.0, 1.4, 0.05]).reshape(g.shape)
+        assert rel_l2(g, r) < TOL_RHS_SPLIT
+
+
+def test_split_small_odd_mesh(gpu_lib):
+    from hopefoam_gb300 import _lib as L
+    from hopefoam_gb300 import euler
+    from hopefoam_gb300.mesh import periodic_square
+
+    m = periodic_square(5, 3, 10.0, 6.0, perturb=0.05, seed=9)  # K = 30 < one tile
+    ctx, orc, x, y = _setup(m, 4)
+    q = euler.isentropic_vortex(x, y, x0=5.0, y0=3.0, beta=1.0)
+    ctx.upload(q)
+    g = ctx.rhs(flux=1, precision=L.DG_PREC_SPLIT)
+    r = orc.euler_rhs(q.reshape(-1), flux=1).reshape(g.shape)
+    assert rel_l2(g, r) < TOL_RHS_SPLIT

@@ -55,6 +55,10 @@ SIGNATURES = {
     "dg_ssprk2_step": (ctypes.c_int, [_vp, ctypes.c_double, ctypes.c_int, ctypes.c_int, ctypes.c_int]),
     "dg_cfl_dt": (ctypes.c_int, [_vp, ctypes.c_double, _dp]),
     "dg_reference_operators": (ctypes.c_int, [ctypes.c_int, _dp, ctypes.c_int, _dp, _dp, _dp, _dp, _dp, _dp, _dp]),
+    "dg_ipdg_setup": (ctypes.c_int, [_vp, ctypes.c_double]),
+    "dg_ipdg_apply": (ctypes.c_int, [_vp, _dp, _dp]),
+    "dg_pcg_solve": (ctypes.c_int, [_vp, _dp, _dp, ctypes.c_double, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                    ctypes.POINTER(SolveStats)]),
 }
 
 _lib = None

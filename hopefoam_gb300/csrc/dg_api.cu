@@ -215,6 +215,7 @@ int dg_ctx_destroy(dg_ctx* c) {
     if (!c) return DG_OK;
     if (c->stream) cudaStreamSynchronize(c->stream);
     split_teardown(c);
+    ipdg_teardown(c);
     for (void* p : c->allocs) cudaFree(p);
     if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
     delete c;

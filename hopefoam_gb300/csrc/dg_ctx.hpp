@@ -48,6 +48,7 @@ struct dg_ctx {
     int cur = 0;
     bool btrace_set = false;
     dgk::SplitPlan split;
+    struct IpdgState* ipdg = nullptr;
     std::vector<void*> allocs;
     size_t bytes = 0;
     std::string err;
@@ -55,3 +56,7 @@ struct dg_ctx {
 
 int split_setup(dg_ctx* c);
 void split_teardown(dg_ctx* c);
+
+// SIPG / PCG state (ipdg_api.cu)
+struct IpdgState;
+void ipdg_teardown(dg_ctx* c);

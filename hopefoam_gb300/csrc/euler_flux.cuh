@@ -36,6 +36,20 @@ __device__ __forceinline__ void face_normal(int f, double rx, double sx, double 
     ny = gy / fsc;
 }
 
+// FP32 version for the split path (GB300 runs FP64 sqrt/divide as long DFMA
+// sequences at 1/70 of the FP32 rate)
+__device__ __forceinline__ void face_normal_f(int f, float rx, float sx, float ry, float sy, float& nx, float& ny,
+                                              float& fsc) {
+    float gx, gy;
+    if (f == 0) { gx = -sx; gy = -sy; }
+    else if (f == 1) { gx = rx + sx; gy = ry + sy; }
+    else { gx = -rx; gy = -ry; }
+    fsc = sqrtf(gx * gx + gy * gy);
+    const float inv = 1.f / fsc;
+    nx = gx * inv;
+    ny = gy * inv;
+}
+
 template <typename T>
 __device__ __forceinline__ T wave_speed(T gamma, T nx, T ny, const T q[4]) {
     const T rho = q[0], u = q[1] / rho, v = q[2] / rho;
@@ -89,6 +103,118 @@ __device__ __forceinline__ void roe_flux(T gamma, T nx, T ny, const T qO[4], con
     F[1] = nx * fu - ny * fv;
     F[2] = ny * fu + nx * fv;
     F[3] = fe;
+}
+
+// ---------------------------------------------------------------------------
+// Delta (product-rule) forms used by the split-precision path.  With a
+// per-element reference state qb and q = qb + dq, the weak right-hand side
+// satisfies R(F) = R(F - F(qb)) exactly (the discrete divergence of a
+// constant flux cancels against its own surface term), so the kernels feed the
+// contractions with dF = F(qb + dq) - F(qb).  Written as below, dF carries
+// FP32 round-off relative to |dq| instead of |q|: no cancellation.
+
+struct RefState {
+    float rho, m, n, E, u, v, p, H;  // H = E + p
+};
+
+__device__ __forceinline__ RefState make_ref(float gamma, const float qb[4]) {
+    RefState b;
+    b.rho = qb[0];
+    b.m = qb[1];
+    b.n = qb[2];
+    b.E = qb[3];
+    b.u = b.m / b.rho;
+    b.v = b.n / b.rho;
+    b.p = (gamma - 1.f) * (b.E - 0.5f * (b.m * b.u + b.n * b.v));
+    b.H = b.E + b.p;
+    return b;
+}
+
+// full velocities and pressure delta of q = qb + dq (helpers shared by the fluxes)
+struct DeltaPrim {
+    float rho, u, v, du, dv, dp, E;
+};
+
+__device__ __forceinline__ DeltaPrim delta_prim(float gamma, const RefState& b, const float dq[4]) {
+    DeltaPrim d;
+    d.rho = b.rho + dq[0];
+    const float m = b.m + dq[1], n = b.n + dq[2];
+    d.du = (dq[1] - b.u * dq[0]) / d.rho;
+    d.dv = (dq[2] - b.v * dq[0]) / d.rho;
+    d.u = b.u + d.du;
+    d.v = b.v + d.dv;
+    const float dK = 0.5f * (dq[1] * b.u + m * d.du + dq[2] * b.v + n * d.dv);
+    d.dp = (gamma - 1.f) * (dq[3] - dK);
+    d.E = b.E + dq[3];
+    return d;
+}
+
+__device__ __forceinline__ void flux_delta(const RefState& b, const float dq[4], const DeltaPrim& d, float dFx[4],
+                                           float dFy[4]) {
+    const float m = b.m + dq[1], n = b.n + dq[2];
+    const float dH = dq[3] + d.dp;
+    dFx[0] = dq[1];
+    dFx[1] = dq[1] * b.u + m * d.du + d.dp;
+    dFx[2] = dq[2] * b.u + n * d.du;
+    dFx[3] = d.du * b.H + d.u * dH;
+    dFy[0] = dq[2];
+    dFy[1] = dq[1] * b.v + m * d.dv;
+    dFy[2] = dq[2] * b.v + n * d.dv + d.dp;
+    dFy[3] = d.dv * b.H + d.v * dH;
+}
+
+__device__ __forceinline__ float wave_speed_delta(float gamma, float nx, float ny, const RefState& b, const DeltaPrim& d) {
+    const float p = b.p + d.dp;
+    return fabsf(d.u * nx + d.v * ny) + sqrtf(fabsf(gamma * p / d.rho));
+}
+
+// n.F*(q-, q+) - n.F(qb), Lax-Friedrichs
+__device__ __forceinline__ void lf_flux_delta(float nx, float ny, float lam, const RefState& b, const float dm[4],
+                                              const DeltaPrim& pm, const float dpq[4], const DeltaPrim& pp, float F[4]) {
+    float fxm[4], fym[4], fxp[4], fyp[4];
+    flux_delta(b, dm, pm, fxm, fym);
+    flux_delta(b, dpq, pp, fxp, fyp);
+#pragma unroll
+    for (int v = 0; v < 4; v++)
+        F[v] = 0.5f * ((fxm[v] + fxp[v]) * nx + (fym[v] + fyp[v]) * ny) + 0.5f * lam * (dm[v] - dpq[v]);
+}
+
+// n.F*(q-, q+) - n.F(qb), Roe (RoeFlux.C:129-178 rearranged: central part in
+// delta form, wave strengths from side-to-side jumps of the deltas)
+__device__ __forceinline__ void roe_flux_delta(float gamma, float nx, float ny, const RefState& b, const float dm[4],
+                                               const DeltaPrim& pm, const float dpq[4], const DeltaPrim& pp,
+                                               float F[4]) {
+    float fxm[4], fym[4], fxp[4], fyp[4];
+    flux_delta(b, dm, pm, fxm, fym);
+    flux_delta(b, dpq, pp, fxp, fyp);
+    const float unM = nx * pm.u + ny * pm.v, unP = nx * pp.u + ny * pp.v;
+    const float utM = nx * pm.v - ny * pm.u, utP = nx * pp.v - ny * pp.u;
+    const float pM = b.p + pm.dp, pP = b.p + pp.dp;
+    const float HM = (pm.E + pM) / pm.rho, HP = (pp.E + pP) / pp.rho;
+    const float sM = sqrtf(pm.rho), sP = sqrtf(pp.rho);
+    const float rhob = sM * sP;
+    const float inv = 1.f / (sM + sP);
+    const float u = (sM * unM + sP * unP) * inv;
+    const float v = (sM * utM + sP * utP) * inv;
+    const float H = (sM * HM + sP * HP) * inv;
+    const float c2 = (gamma - 1.f) * (H - 0.5f * (u * u + v * v));
+    const float c = sqrtf(fabsf(c2));
+    const float jr = dpq[0] - dm[0];
+    const float jdu = pp.du - pm.du, jdv = pp.dv - pm.dv;
+    const float jun = nx * jdu + ny * jdv, jut = nx * jdv - ny * jdu;
+    const float jp = pp.dp - pm.dp;
+    const float dw1 = (-0.5f * rhob * jun / c + 0.5f * jp / c2) * fabsf(u - c);
+    const float dw2 = (jr - jp / c2) * fabsf(u);
+    const float dw3 = (rhob * jut) * fabsf(u);
+    const float dw4 = (0.5f * rhob * jun / c + 0.5f * jp / c2) * fabsf(u + c);
+    const float dr = dw1 + dw2 + dw4;
+    const float du = dw1 * (u - c) + dw2 * u + dw4 * (u + c);
+    const float dv = dr * v + dw3;
+    const float de = dw1 * (H - u * c) + dw2 * (u * u + v * v) * 0.5f + dw3 * v + dw4 * (H + u * c);
+    F[0] = 0.5f * ((fxm[0] + fxp[0]) * nx + (fym[0] + fyp[0]) * ny) - 0.5f * dr;
+    F[1] = 0.5f * ((fxm[1] + fxp[1]) * nx + (fym[1] + fyp[1]) * ny) - 0.5f * (nx * du - ny * dv);
+    F[2] = 0.5f * ((fxm[2] + fxp[2]) * nx + (fym[2] + fyp[2]) * ny) - 0.5f * (ny * du + nx * dv);
+    F[3] = 0.5f * ((fxm[3] + fxp[3]) * nx + (fym[3] + fyp[3]) * ny) - 0.5f * de;
 }
 
 }  // namespace dgk

@@ -3,28 +3,38 @@
 //
 // Arithmetic: the two contractions of the quadrature-form DG right-hand side
 // run as TF32 GEMMs with 3-pass split products (hi*hi + lo*hi + hi*lo) and
-// FP32 accumulation in tensor memory:
+// FP32 accumulation in tensor memory, on deltas against a per-element
+// reference state qb (the row mean):
 //   GEMM1 (cubature interpolation, dgGaussField.C:193-202):
-//     Qg[r][g] = sum_p Q[r][p] Vg[g][p],        M = 128 rows r = v*32 + e
-//                                               (4 variables x 32 elements),
+//     dQg[r][g] = sum_p dQ[r][p] Vg[g][p],      M = 128 rows r = 4 e + v
+//                                               (32 elements x 4 variables),
 //                                               N = Ng padded, K = Np padded
 //   GEMM2 (volume term + surface lift with the affine mass inverse folded in,
 //          defaultConvectionScheme.C:79-128, defaultGrad.C:120-165,
 //          defaultDivScheme.C:118-165):
-//     R[r][p] = sum_g Fr[r][g] Sr[p][g] + Fs[r][g] Ss[p][g]
-//             + sum_c (-sJ/J F*)[r][c] Lift[p][c],   N = Np padded
-// Point-wise fluxes (volume and face) are FP32 SIMT.  The state q stays FP64
-// in HBM; the low-storage RK register is FP32 (it carries dt*R, whose own
-// precision is FP32); q += b*res is the only FP64 instruction per value.
+//     R[r][p] = sum_g dFr[r][g] Sr[p][g] + dFs[r][g] Ss[p][g]
+//             + sum_c (-sJ/J dF*)[r][c] Lift[p][c],   N = Np padded
+// with dF = F(qb + dQ) - F(qb) and dF* = n.F*(q-, q+) - n.F(qb) evaluated
+// point-wise in FP32 in cancellation-free product-rule form (euler_flux.cuh).
+// Because the weak divergence of a constant flux cancels against its own
+// surface term, R is unchanged by the shift, but the FP32 round-off now
+// scales with the variation inside an element instead of with |F| N^2 / h.
+// The state q stays FP64 in HBM (dQ = q - qb is formed in FP64); the
+// low-storage RK register is FP32 (it carries dt*R, whose own precision is
+// FP32); q += b*res is the only FP64 arithmetic per value in the update.
 //
 // Structure: persistent CTAs (one per SM, 256 threads), 32 elements per tile.
-// Per tile: stage q (FP64 -> FP32 -> TF32 hi/lo in the canonical no-swizzle
-// K-major layout, see umma.cuh) -> GEMM1 (issued by one thread, completion on
-// an mbarrier) -> face fluxes while GEMM1 runs -> for each chunk of 16
-// cubature points: tensor memory -> shared exchange -> FP32 flux -> TF32
-// split -> GEMM2 MMAs for that K chunk -> epilogue: tensor memory -> shared ->
-// coalesced LSERK update.  All mbarrier waits are bounded; a timeout sets the
-// status word, the CTA drains its MMAs, frees tensor memory and returns.
+// Per tile: stage q (FP64 tile in shared memory, reference state, FP32 deltas,
+// TF32 hi/lo in the canonical no-swizzle K-major layout, see umma.cuh) ->
+// GEMM1 (issued by one thread, completion on an mbarrier) -> face fluxes in
+// 8-lane groups (gather, Gauss interpolation and wave-speed max by shuffles)
+// while GEMM1 runs -> per chunk of 16 cubature points: tensor memory ->
+// registers, the 4 variables of a point exchanged by warp shuffles within
+// the element's 4 lanes -> FP32 delta flux -> TF32 split into a
+// double-buffered chunk operand -> GEMM2 MMAs for that K chunk -> epilogue:
+// tensor memory -> shared -> coalesced LSERK update.  All mbarrier waits are
+// bounded; a timeout sets the status word, the CTA frees tensor memory and
+// returns.
 #include <cstdio>
 #include <cstring>
 #include <vector>
@@ -48,26 +58,32 @@ struct SplitDims {
     static constexpr int CH = 16;                     // cubature points per chunk
     static constexpr int NCH = NG / CH;
     static constexpr int KC = 2 * CH;                 // chunk buffer K: [Fr 16 | Fs 16]
+    static constexpr int NBUF = (N <= 5) ? 2 : 1;     // chunk buffers
     // shared-memory layout (bytes, operand buffers 1024-aligned)
     static constexpr int SZ_B1 = 2 * NG * KP1 * 4;    // Vg hi/lo
     static constexpr int SZ_B2 = 2 * NP2 * KP2 * 4;   // [Sr|Ss|Lift] hi/lo
-    static constexpr int SZ_A1 = 2 * ROWS * KP1 * 4;  // Q hi/lo
-    static constexpr int SZ_AC = 2 * ROWS * KC * 4;   // flux chunk hi/lo
+    static constexpr int SZ_A1 = 2 * ROWS * KP1 * 4;  // dQ hi/lo
+    static constexpr int SZ_AC = 2 * ROWS * KC * 4;   // one flux chunk hi/lo
     static constexpr int SZ_AF = 2 * ROWS * NF * 4;   // face flux hi/lo
-    static constexpr int SZ_X = 4 * CH * E * 4;       // exchange q at cubature points
-    static constexpr int SZ_QF = E * 4 * Np * 4;      // FP32 copy of the tile state
+    static constexpr int SZ_QF = E * 4 * Np * 4;      // FP32 deltas of the tile state
+    static constexpr int SZ_Q64 = E * 4 * Np * 8;     // FP64 tile state
+    static constexpr int SZ_QB = ROWS * 4;            // FP32 reference state per (element, variable)
     static constexpr int al(int x) { return (x + 1023) / 1024 * 1024; }
     static constexpr int OFF_B1 = 0;
     static constexpr int OFF_B2 = OFF_B1 + al(SZ_B1);
     static constexpr int OFF_A1 = OFF_B2 + al(SZ_B2);
     static constexpr int OFF_AC = OFF_A1 + al(SZ_A1);
-    static constexpr int OFF_AF = OFF_AC + al(SZ_AC);
-    static constexpr int OFF_X = OFF_AF + al(SZ_AF);
-    static constexpr int OFF_QF = OFF_X + al(SZ_X);
-    static constexpr int OFF_BAR = OFF_QF + al(SZ_QF);
+    static constexpr int AL_AC = al(SZ_AC);           // stride between chunk buffers
+    static constexpr int OFF_AF = OFF_AC + NBUF * AL_AC;
+    static constexpr int OFF_QF = OFF_AF + al(SZ_AF);
+    static constexpr int OFF_Q64 = OFF_QF + al(SZ_QF);
+    static constexpr int OFF_QB = OFF_Q64 + al(SZ_Q64);
+    static constexpr int OFF_BAR = OFF_QB + al(SZ_QB);
     static constexpr int SMEM = OFF_BAR + 64;
-    static constexpr int RS_FLOATS = E * 4 * Np;      // epilogue staging (aliases the chunk buffer)
+    static constexpr int RS_FLOATS = E * 4 * Np;      // epilogue staging (aliases chunk buffer 0)
     static_assert(RS_FLOATS * 4 <= SZ_AC, "epilogue staging does not fit");
+    static_assert(SMEM <= 232448, "shared memory budget");
+    static_assert(Nfq <= 8, "face groups are 8 lanes");
     static constexpr int TMEM_COLS = 256;
     static constexpr int D2_COL = 128;
     static_assert(NG <= 128 && NP2 <= 128, "tensor memory layout");
@@ -84,6 +100,10 @@ struct SplitArgs {
 
 constexpr uint32_t kWaitLimit = 1u << 22;
 
+__device__ __forceinline__ float pick4(const float* x, int i) {
+    return i == 0 ? x[0] : (i == 1 ? x[1] : (i == 2 ? x[2] : x[3]));
+}
+
 template <int N>
 __global__ void __launch_bounds__(256, 1) euler_stage_split_kernel(SplitArgs sa) {
     using D = SplitDims<N>;
@@ -94,14 +114,14 @@ __global__ void __launch_bounds__(256, 1) euler_stage_split_kernel(SplitArgs sa)
     float* sB1 = reinterpret_cast<float*>(smem + D::OFF_B1);
     float* sB2 = reinterpret_cast<float*>(smem + D::OFF_B2);
     float* sA1 = reinterpret_cast<float*>(smem + D::OFF_A1);
-    float* sAC = reinterpret_cast<float*>(smem + D::OFF_AC);
     float* sAF = reinterpret_cast<float*>(smem + D::OFF_AF);
-    float* sX = reinterpret_cast<float*>(smem + D::OFF_X);
     float* sQF = reinterpret_cast<float*>(smem + D::OFF_QF);
-    float* sRS = sAC;  // epilogue staging, used only after GEMM2 completed
+    double* sQ64 = reinterpret_cast<double*>(smem + D::OFF_Q64);
+    float* sQB = reinterpret_cast<float*>(smem + D::OFF_QB);
+    float* sRS = reinterpret_cast<float*>(smem + D::OFF_AC);  // after GEMM2 completed
     uint64_t* bar1 = reinterpret_cast<uint64_t*>(smem + D::OFF_BAR);
-    uint64_t* bar2 = bar1 + 1;
-    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bar1 + 2);
+    uint64_t* bar2 = bar1 + 1;  // [NBUF]
+    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bar1 + 3);
 
     const EulerArgs& a = sa.e;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -121,7 +141,7 @@ __global__ void __launch_bounds__(256, 1) euler_stage_split_kernel(SplitArgs sa)
     }
     if (tid == 0) {
         umma::mbar_init(bar1, 1);
-        umma::mbar_init(bar2, 1);
+        for (int b = 0; b < D::NBUF; b++) umma::mbar_init(bar2 + b, 1);
         umma::fence_mbar_init();
     }
     if (warp == 0) {
@@ -137,24 +157,46 @@ __global__ void __launch_bounds__(256, 1) euler_stage_split_kernel(SplitArgs sa)
     const uint32_t idesc1 = umma::idesc_tf32(128, NG);
     const uint32_t idesc2 = umma::idesc_tf32(128, NP2);
     const uint32_t aB1 = umma::smem_u32(sB1), aB2 = umma::smem_u32(sB2);
-    const uint32_t aA1 = umma::smem_u32(sA1), aAC = umma::smem_u32(sAC), aAF = umma::smem_u32(sAF);
+    const uint32_t aA1 = umma::smem_u32(sA1), aAF = umma::smem_u32(sAF);
+    const uint32_t aAC = umma::smem_u32(smem + D::OFF_AC);
     constexpr uint32_t LO_B1 = NG * KP1 * 4, LO_B2 = NP2 * KP2 * 4, LO_A1 = 128 * KP1 * 4, LO_AC = 128 * KC * 4,
-                       LO_AF = 128 * NF * 4;
-    uint32_t ph1 = 0, ph2 = 0;
+                       LO_AF = 128 * NF * 4, STRIDE_AC = D::AL_AC;
+    uint32_t ph1 = 0;
+    uint32_t ph2[2] = {0, 0};
     bool failed = false;
+
+    // this thread's rows in the element-major TMEM layout r = 4 e + v
+    const int qd = warp & 3, half = warp >> 2;
+    const int my_e = 8 * qd + (lane >> 2), my_v = lane & 3;
 
     for (int tile = blockIdx.x; tile < ntiles && !failed; tile += gridDim.x) {
         const int k0 = tile * E;
         const int ne = min(E, a.K - k0);
-        // ---- (A) stage the tile: FP64 -> FP32 copy + TF32 hi/lo operand
-        const double* qin = a.qin + (size_t)k0 * 4 * Np;
+        // ---- (A) stage the tile: FP64 copy, per-(element, variable) reference
+        //      state (row mean, FP32), FP32 deltas, TF32 hi/lo of the deltas
+        {
+            const double* qin = a.qin + (size_t)k0 * 4 * Np;
+            for (int i = tid; i < ne * 4 * Np; i += blockDim.x) sQ64[i] = qin[i];
+        }
+        __syncthreads();
+        if (tid < D::ROWS) {
+            const int e = tid >> 2, v = tid & 3;
+            float s = 0.f;
+            if (e < ne) {
+                const double* row = sQ64 + e * 4 * Np + v * Np;
+#pragma unroll 4
+                for (int p = 0; p < Np; p++) s += (float)row[p];
+            }
+            sQB[tid] = e < ne ? s * (1.f / Np) : 1.f;
+        }
+        __syncthreads();
         for (int i = tid; i < ne * 4 * Np; i += blockDim.x) {
-            const float x = (float)qin[i];
-            sQF[i] = x;
             const int e = i / (4 * Np), rem = i - e * 4 * Np, v = rem / Np, p = rem - v * Np;
-            const int r = v * 32 + e;
+            const int r = 4 * e + v;
+            const float d = (float)(sQ64[i] - (double)sQB[r]);
+            sQF[i] = d;
             float hi, lo;
-            umma::split_tf32(x, hi, lo);
+            umma::split_tf32(d, hi, lo);
             const uint32_t off = umma::kmajor_offset(r, p, KP1) >> 2;
             sA1[off] = hi;
             sA1[off + LO_A1 / 4] = lo;
@@ -164,7 +206,7 @@ __global__ void __launch_bounds__(256, 1) euler_stage_split_kernel(SplitArgs sa)
         __syncthreads();
         umma::fence_after_sync();
         if (tid == 0) {
-            // GEMM1: D1 = Q (hi,lo) x Vg (hi,lo)^T, 3 passes per K=8 step
+            // GEMM1: D1 = dQ (hi,lo) x Vg (hi,lo)^T, 3 passes per K=8 step
 #pragma unroll
             for (int s = 0; s < KP1 / 8; s++) {
                 const uint64_t ah = umma::smem_desc(aA1 + s * 256, 128, (KP1 / 4) * 128);
@@ -177,141 +219,144 @@ __global__ void __launch_bounds__(256, 1) euler_stage_split_kernel(SplitArgs sa)
             }
             umma::commit(bar1);
         }
-        // ---- (B) face fluxes while GEMM1 runs: one thread per (element, face)
-        if (tid < 3 * E) {
-            const int e = tid / 3, f = tid - 3 * e;
-            if (e < ne) {
-                const int k = k0 + e;
-                double nxd, nyd, fscd;
-                const double* gk = a.geo + (size_t)k * 4;
-                face_normal(f, gk[0], gk[1], gk[2], gk[3], nxd, nyd, fscd);
-                const float nx = (float)nxd, ny = (float)nyd, fsc = (float)fscd;
-                float um[4][Nfp], up[4][Nfp];
-                const float* qe = sQF + e * 4 * Np;
+        // ---- (B) face fluxes while GEMM1 runs: 8-lane groups per (element, face),
+        //      lane i = face node i (gather) and face Gauss point i (flux)
+        {
+            const int i = lane & 7;
+#pragma unroll 1
+            for (int j = 0; j < 3; j++) {
+                const int G = (tid >> 3) + 32 * j;
+                const int e = G / 3, f = G - 3 * e;
+                const bool valid = e < ne;
+                const int k = k0 + (valid ? e : 0);
+                float own[4] = {0.f, 0.f, 0.f, 0.f}, nbr[4] = {0.f, 0.f, 0.f, 0.f};
+                float qbv[4];
 #pragma unroll
-                for (int j = 0; j < Nfp; j++) {
-                    const int pos = (f * N + j) % NB;
+                for (int v = 0; v < 4; v++) qbv[v] = sQB[4 * (valid ? e : 0) + v];
+                if (valid && i < Nfp) {
+                    const int pos = (f * N + i) % NB;
 #pragma unroll
-                    for (int v = 0; v < 4; v++) um[v][j] = qe[v * Np + pos];
-                }
-                const int c = __ldg(a.conn + (size_t)k * 3 + f);
-                if (c >= 0) {
-                    const int nb = c >> 3, fn = c & 3, rot = (c >> 2) & 1;
-                    const double* qn = a.qin + (size_t)nb * 4 * Np;
+                    for (int v = 0; v < 4; v++) own[v] = sQF[e * 4 * Np + v * Np + pos];
+                    const int c = __ldg(a.conn + (size_t)k * 3 + f);
+                    if (c >= 0) {
+                        const int nb = c >> 3, fn = c & 3, rot = (c >> 2) & 1;
+                        const int jj = rot ? (N - i) : i;
+                        const int npos = (fn * N + jj) % NB;
+                        const double* qn = a.qin + (size_t)nb * 4 * Np + npos;
 #pragma unroll
-                    for (int j = 0; j < Nfp; j++) {
-                        const int jj = rot ? (N - j) : j;
-                        const int pos = (fn * N + jj) % NB;
+                        for (int v = 0; v < 4; v++) nbr[v] = (float)(__ldg(qn + v * Np) - (double)qbv[v]);
+                    } else {
+                        const double* bt = a.btrace + (size_t)(-1 - c) * 4 * Nfp + i;
 #pragma unroll
-                        for (int v = 0; v < 4; v++) up[v][j] = (float)__ldg(qn + v * Np + pos);
+                        for (int v = 0; v < 4; v++) nbr[v] = (float)(__ldg(bt + v * Nfp) - (double)qbv[v]);
                     }
-                } else {
-                    const double* bt = a.btrace + (size_t)(-1 - c) * 4 * Nfp;
-#pragma unroll
-                    for (int j = 0; j < Nfp; j++)
-#pragma unroll
-                        for (int v = 0; v < 4; v++) up[v][j] = (float)__ldg(bt + v * Nfp + j);
                 }
-                float qm[Nfq][4], qp[Nfq][4];
+                // interpolate both traces to Gauss point i (shuffles within the 8-lane group)
+                float dm[4] = {0.f, 0.f, 0.f, 0.f}, dp[4] = {0.f, 0.f, 0.f, 0.f};
+                const int gi = i < Nfq ? i : 0;
 #pragma unroll
-                for (int i = 0; i < Nfq; i++)
+                for (int jn = 0; jn < Nfp; jn++) {
+                    const float w = (float)__ldg(a.ops.If + gi * Nfp + jn);
 #pragma unroll
                     for (int v = 0; v < 4; v++) {
-                        float s1 = 0.f, s2 = 0.f;
-#pragma unroll
-                        for (int j = 0; j < Nfp; j++) {
-                            const float w = (float)__ldg(a.ops.If + i * Nfp + j);
-                            s1 = fmaf(w, um[v][j], s1);
-                            s2 = fmaf(w, up[v][j], s2);
-                        }
-                        qm[i][v] = s1;
-                        qp[i][v] = s2;
-                    }
-                float lam = 0.f;
-                if (a.flux != 1) {
-#pragma unroll
-                    for (int i = 0; i < Nfq; i++) {
-                        lam = fmaxf(lam, wave_speed(gamma, nx, ny, qm[i]));
-                        lam = fmaxf(lam, wave_speed(gamma, nx, ny, qp[i]));
+                        dm[v] = fmaf(w, __shfl_sync(0xffffffffu, own[v], jn, 8), dm[v]);
+                        dp[v] = fmaf(w, __shfl_sync(0xffffffffu, nbr[v], jn, 8), dp[v]);
                     }
                 }
+                const double* gk = a.geo + (size_t)k * 4;
+                float nx, ny, fsc;
+                face_normal_f(f, (float)gk[0], (float)gk[1], (float)gk[2], (float)gk[3], nx, ny, fsc);
+                const RefState b = make_ref(gamma, qbv);
+                const DeltaPrim pm = delta_prim(gamma, b, dm), pp = delta_prim(gamma, b, dp);
+                float F[4];
+                if (a.flux == 1) {
+                    roe_flux_delta(gamma, nx, ny, b, dm, pm, dp, pp, F);
+                } else {
+                    float lam = (i < Nfq) ? fmaxf(wave_speed_delta(gamma, nx, ny, b, pm),
+                                                  wave_speed_delta(gamma, nx, ny, b, pp))
+                                          : 0.f;
 #pragma unroll
-                for (int i = 0; i < Nfq; i++) {
-                    float F[4];
-                    if (a.flux == 1) roe_flux(gamma, nx, ny, qm[i], qp[i], F);
-                    else lf_flux(gamma, nx, ny, lam, qm[i], qp[i], F);
+                    for (int o = 1; o < 8; o <<= 1) lam = fmaxf(lam, __shfl_xor_sync(0xffffffffu, lam, o, 8));
+                    lf_flux_delta(nx, ny, lam, b, dm, pm, dp, pp, F);
+                }
+                if (valid && i < Nfq) {
 #pragma unroll
                     for (int v = 0; v < 4; v++) {
                         float hi, lo;
                         umma::split_tf32(-fsc * F[v], hi, lo);
-                        const uint32_t off = umma::kmajor_offset(v * 32 + e, f * Nfq + i, NF) >> 2;
+                        const uint32_t off = umma::kmajor_offset(4 * e + v, f * Nfq + i, NF) >> 2;
                         sAF[off] = hi;
                         sAF[off + LO_AF / 4] = lo;
                     }
                 }
             }
         }
+        // per-thread element data for the volume flux: reference state and metrics
+        float qbe[4];
+#pragma unroll
+        for (int v = 0; v < 4; v++) qbe[v] = sQB[4 * my_e + v];
+        const RefState bref = make_ref(gamma, qbe);
+        float rx = 0.f, sx = 0.f, ry = 0.f, sy = 0.f;
+        if (my_e < ne) {
+            const double* gk = a.geo + (size_t)(k0 + my_e) * 4;
+            rx = (float)gk[0]; sx = (float)gk[1]; ry = (float)gk[2]; sy = (float)gk[3];
+        }
         // ---- (C) wait for GEMM1, then the volume flux per chunk of cubature points
         bool ok = umma::mbar_wait(bar1, ph1, kWaitLimit);
         ph1 ^= 1;
         if (__syncthreads_or(!ok)) { failed = true; break; }
         umma::fence_after_sync();
-        // metrics of this thread's flux points (same element for both points: e = lane)
-        float rx = 0.f, sx = 0.f, ry = 0.f, sy = 0.f;
-        if (lane < ne) {
-            const double* gk = a.geo + (size_t)(k0 + lane) * 4;
-            rx = (float)gk[0]; sx = (float)gk[1]; ry = (float)gk[2]; sy = (float)gk[3];
-        }
         for (int ch = 0; ch < D::NCH; ch++) {
-            // tensor memory -> exchange buffer: warp w reads lanes of quarter (w & 3) = variable v
-            {
-                const int v = warp & 3, half = warp >> 2;
-                float val[8];
-                umma::tmem_ld8(tD1 + ((uint32_t)(32 * v) << 16) + ch * CH + half * 8, val);
-                umma::tmem_ld_wait();
-#pragma unroll
-                for (int j = 0; j < 8; j++) sX[(v * CH + half * 8 + j) * E + lane] = val[j];
-            }
-            __syncthreads();
-            // FP32 flux for 2 points per thread: (g = warp*2 + j, e = lane)
+            const int buf = (D::NBUF == 2) ? (ch & 1) : 0;
+            float* sAC = reinterpret_cast<float*>(smem + D::OFF_AC + buf * STRIDE_AC);
+            // this thread's row (e, v) at 8 cubature points of the chunk
+            float x[8];
+            umma::tmem_ld8(tD1 + ((uint32_t)(32 * qd) << 16) + ch * CH + half * 8, x);
+            umma::tmem_ld_wait();
             float fr[2][4], fs[2][4];
 #pragma unroll
-            for (int j = 0; j < 2; j++) {
-                const int gl = warp * 2 + j;
-                const int g = ch * CH + gl;
-                if (g < Ng && lane < ne) {
-                    float q[4], fx[4], fy[4];
+            for (int s2 = 0; s2 < 2; s2++) {
+                // gather the 4 variables at point (my_v + 4 s2) of the 8 from the element's 4 lanes
+                float dq[4];
 #pragma unroll
-                    for (int v = 0; v < 4; v++) q[v] = sX[(v * CH + gl) * E + lane];
-                    euler_phys_flux(gamma, q, fx, fy);
+                for (int s = 0; s < 4; s++) {
+                    const float send = pick4(x + 4 * s2, (my_v + s) & 3);
+                    const float got = __shfl_sync(0xffffffffu, send, (lane & ~3) | ((my_v - s) & 3));
+                    dq[(my_v - s) & 3] = got;
+                }
+                const int g = ch * CH + half * 8 + my_v + 4 * s2;
+                if (g < Ng && my_e < ne) {
+                    const DeltaPrim d = delta_prim(gamma, bref, dq);
+                    float fx[4], fy[4];
+                    flux_delta(bref, dq, d, fx, fy);
 #pragma unroll
                     for (int v = 0; v < 4; v++) {
-                        fr[j][v] = rx * fx[v] + ry * fy[v];
-                        fs[j][v] = sx * fx[v] + sy * fy[v];
+                        fr[s2][v] = rx * fx[v] + ry * fy[v];
+                        fs[s2][v] = sx * fx[v] + sy * fy[v];
                     }
                 } else {
 #pragma unroll
-                    for (int v = 0; v < 4; v++) fr[j][v] = fs[j][v] = 0.f;
+                    for (int v = 0; v < 4; v++) fr[s2][v] = fs[s2][v] = 0.f;
                 }
             }
-            // the previous chunk's MMAs must have consumed the chunk buffer
-            if (ch > 0) {
-                ok = umma::mbar_wait(bar2, ph2, kWaitLimit);
-                ph2 ^= 1;
+            // the MMAs that last read this buffer must be complete
+            if (ch >= D::NBUF) {
+                ok = umma::mbar_wait(bar2 + buf, ph2[buf], kWaitLimit);
+                ph2[buf] ^= 1;
                 if (__syncthreads_or(!ok)) { failed = true; break; }
             }
 #pragma unroll
-            for (int j = 0; j < 2; j++) {
-                const int gl = warp * 2 + j;
+            for (int s2 = 0; s2 < 2; s2++) {
+                const int gl = half * 8 + my_v + 4 * s2;
 #pragma unroll
                 for (int v = 0; v < 4; v++) {
-                    const int r = v * 32 + lane;
+                    const int r = 4 * my_e + v;
                     float hi, lo;
-                    umma::split_tf32(fr[j][v], hi, lo);
+                    umma::split_tf32(fr[s2][v], hi, lo);
                     uint32_t off = umma::kmajor_offset(r, gl, KC) >> 2;
                     sAC[off] = hi;
                     sAC[off + LO_AC / 4] = lo;
-                    umma::split_tf32(fs[j][v], hi, lo);
+                    umma::split_tf32(fs[s2][v], hi, lo);
                     off = umma::kmajor_offset(r, CH + gl, KC) >> 2;
                     sAC[off] = hi;
                     sAC[off + LO_AC / 4] = lo;
@@ -323,12 +368,13 @@ __global__ void __launch_bounds__(256, 1) euler_stage_split_kernel(SplitArgs sa)
             umma::fence_after_sync();
             if (tid == 0) {
                 constexpr uint32_t sboA = (KC / 4) * 128, sboB = (KP2 / 4) * 128;
+                const uint32_t aC = aAC + buf * STRIDE_AC;
 #pragma unroll
                 for (int s = 0; s < KC / 8; s++) {
                     // chunk K step s: Fr part (s < 2) at B2 k = ch*CH + 8s, Fs part at NG + ch*CH + 8(s-2)
                     const int kb = (s < CH / 8) ? (ch * CH + 8 * s) : (NG + ch * CH + 8 * (s - CH / 8));
-                    const uint64_t ah = umma::smem_desc(aAC + s * 256, 128, sboA);
-                    const uint64_t al = umma::smem_desc(aAC + LO_AC + s * 256, 128, sboA);
+                    const uint64_t ah = umma::smem_desc(aC + s * 256, 128, sboA);
+                    const uint64_t al = umma::smem_desc(aC + LO_AC + s * 256, 128, sboA);
                     const uint64_t bh = umma::smem_desc(aB2 + kb * 32, 128, sboB);
                     const uint64_t bl = umma::smem_desc(aB2 + LO_B2 + kb * 32, 128, sboB);
                     const uint32_t acc = (ch > 0 || s > 0) ? 1u : 0u;
@@ -350,27 +396,34 @@ __global__ void __launch_bounds__(256, 1) euler_stage_split_kernel(SplitArgs sa)
                         umma::mma_tf32(tD2, ah, bl, idesc2, 1);
                     }
                 }
-                umma::commit(bar2);
+                umma::commit(bar2 + buf);
             }
         }
         if (failed) break;
-        ok = umma::mbar_wait(bar2, ph2, kWaitLimit);
-        ph2 ^= 1;
-        if (__syncthreads_or(!ok)) { failed = true; break; }
+        // outstanding commits: the last NBUF chunks (one per buffer)
+#pragma unroll
+        for (int b = 0; b < D::NBUF; b++) {
+            const int chb = D::NCH - D::NBUF + b;
+            if (chb < 0) continue;
+            const int buf = (D::NBUF == 2) ? (chb & 1) : 0;
+            ok = umma::mbar_wait(bar2 + buf, ph2[buf], kWaitLimit);
+            ph2[buf] ^= 1;
+            if (__syncthreads_or(!ok)) { failed = true; break; }
+        }
+        if (failed) break;
         umma::fence_after_sync();
         // ---- (D) epilogue: R (tensor memory) -> staging -> coalesced stage update
         {
-            const int v = warp & 3, half = warp >> 2;
 #pragma unroll
             for (int c0 = 0; c0 < NP2 / 2; c0 += 8) {
                 const int col = half * (NP2 / 2) + c0;
                 float val[8];
-                umma::tmem_ld8(tD2 + ((uint32_t)(32 * v) << 16) + col, val);
+                umma::tmem_ld8(tD2 + ((uint32_t)(32 * qd) << 16) + col, val);
                 umma::tmem_ld_wait();
 #pragma unroll
                 for (int j = 0; j < 8; j++) {
                     const int p = col + j;
-                    if (p < Np && lane < ne) sRS[(lane * 4 + v) * Np + p] = val[j];
+                    if (p < Np && my_e < ne) sRS[(4 * my_e + my_v) * Np + p] = val[j];
                 }
             }
         }
@@ -382,23 +435,23 @@ __global__ void __launch_bounds__(256, 1) euler_stage_split_kernel(SplitArgs sa)
             const float rka = (float)a.rka, dtf = (float)a.dt, rkb = (float)a.rkb;
             for (int i = tid; i < ne * 4 * Np; i += blockDim.x) {
                 const float R = sRS[i];
+                const double q0 = sQ64[i];
                 const size_t idx = base + i;
                 switch (a.mode) {
                     case MODE_RHS: a.rhs[idx] = (double)R; break;
                     case MODE_LSERK: {
                         const float r = first ? dtf * R : fmaf(rka, sa.res32[idx], dtf * R);
                         sa.res32_out[idx] = r;
-                        a.qout[idx] = a.qin[idx] + (double)(rkb * r);
+                        a.qout[idx] = q0 + (double)(rkb * r);
                     } break;
-                    case MODE_EULER: a.qout[idx] = a.qin[idx] + (double)(dtf * R); break;
-                    default: a.qout[idx] = 0.5 * a.qold[idx] + 0.5 * (a.qin[idx] + (double)(dtf * R)); break;
+                    case MODE_EULER: a.qout[idx] = q0 + (double)(dtf * R); break;
+                    default: a.qout[idx] = 0.5 * a.qold[idx] + 0.5 * (q0 + (double)(dtf * R)); break;
                 }
             }
         }
         __syncthreads();  // staging buffers are rewritten by the next tile
     }
     if (failed && tid == 0) atomicExch(sa.status, 1);
-    // drain: make sure no MMA is still writing tensor memory before freeing it
     umma::fence_before_sync();
     __syncthreads();
     if (warp == 0) umma::tmem_dealloc(tmem, D::TMEM_COLS);

@@ -139,6 +139,31 @@ int dg_ssprk2_step(dg_ctx* ctx, double dt, int nsteps, int flux, int precision);
  * (the reference uses a fixed dt, controlDict). */
 int dg_cfl_dt(dg_ctx* ctx, double cfl, double* dt);
 
+/* Symmetric interior-penalty Laplacian of the pressure equation on the
+ * context's mesh, penalty tau = tau_coef (N+1)^2 max(sJ/J) per face
+ * (tau_coef = 20 is the reference's value,
+ * DG/laplacianSchemes/defaultLaplacianScheme/defaultLaplacianScheme.C:114);
+ * boundary faces are homogeneous Dirichlet (fixesValue, :157-209).  Builds
+ * the reference stiffness parts and the block-Jacobi inverse on the device.
+ * Replaces the per-element assembly of laplacianFunc (:63-288) and
+ * dgMatrix::assembleMatrix (dgMatrices/dgMatrix/dgMatrix.C:383-438). */
+int dg_ipdg_setup(dg_ctx* ctx, double tau_coef);
+
+/* y = S x with S = -A (SPD sign of the reference operator A), matrix-free,
+ * FP64; x, y host arrays of K*Np doubles in the reference node order. */
+int dg_ipdg_apply(dg_ctx* ctx, const double* x_host, double* y_host);
+
+/* Solves S x = b to ||b - S x|| <= rtol ||b|| with preconditioned CG
+ * (replaces dgMatrix::solve -> KSPSolve, dgMatrices/dgMatrix/dgMatrix.C:162-283,
+ * dgMatrixSolve.C:91-213).  x_host holds the initial guess and receives the
+ * solution.  pc: DG_PC_BLOCK_JACOBI or DG_PC_LEARNED (after dg_lpc_*).
+ * precision DG_PREC_FP64: FP64 operator in every iteration; DG_PREC_SPLIT:
+ * mixed-precision refinement (FP32-arithmetic operator inside CG, FP64 outer
+ * residual, FP64 vectors and dot products).  The returned rel_residual is
+ * the true FP64 residual.  DG_ERR_NOT_CONVERGED when maxit is reached. */
+int dg_pcg_solve(dg_ctx* ctx, const double* b_host, double* x_host, double rtol, int maxit, int pc, int precision,
+                 dg_solve_stats* stats);
+
 /* Host-only (no GPU needed): the reference-element operators this library
  * builds for order N from a cubature rule, in the reference node order.
  * Arrays are caller-allocated: r, s [Np]; Dr, Ds, Mref [Np*Np] (row-major);

@@ -287,6 +287,7 @@ __device__ __forceinline__ void block_sum2(double a, double b, double* oa, doubl
         if (oa) *oa = sa;
         if (ob) *ob = sb;
     }
+    __syncthreads();  // ra/rb are reused by the next call
 }
 
 // element-aligned thread mapping: CTA = EB elements x Np rows (EB*Np <= blockDim)
@@ -299,6 +300,19 @@ __device__ __forceinline__ double bj_apply_row(const float* __restrict__ P, cons
     return (double)s;
 }
 
+__device__ __forceinline__ double bj_apply_row64(const double* __restrict__ P, const double* __restrict__ r, int Np,
+                                                 int k, int i) {
+    const double* row = P + ((size_t)k * Np + i) * Np;
+    const double* rk = r + (size_t)k * Np;
+    double s = 0.0;
+    for (int j = 0; j < Np; j++) s += row[j] * rk[j];
+    return s;
+}
+
+__device__ __forceinline__ double bj_apply(const PcgVecs& v, int Np, int k, int i) {
+    return v.P64 ? bj_apply_row64(v.P64, v.r, Np, k, i) : bj_apply_row(v.P32, v.r, Np, k, i);
+}
+
 // z = P r, p = z, part_rz[1] = r.z, part_rr = r.r   (x, r given)
 __global__ void pcg_init_kernel(PcgVecs v, int K, int Np) {
     const int EB = blockDim.x / Np;
@@ -309,7 +323,7 @@ __global__ void pcg_init_kernel(PcgVecs v, int K, int Np) {
         const int k = grp * EB + e;
         if (e < EB && k < K) {
             const size_t idx = (size_t)k * Np + i;
-            const double z = bj_apply_row(v.P32, v.r, Np, k, i);
+            const double z = bj_apply(v, Np, k, i);
             v.z[idx] = z;
             v.p[idx] = z;
             rz += v.r[idx] * z;
@@ -319,7 +333,8 @@ __global__ void pcg_init_kernel(PcgVecs v, int K, int Np) {
     block_sum2(rz, rr, v.part_rz + v.G + blockIdx.x, v.part_rr + blockIdx.x);
 }
 
-// alpha = rz / pAp; x += alpha p; r -= alpha Ap; z = P r; partials of r.z and r.r
+// alpha = rz / pAp; x += alpha p; r -= alpha Ap; z = P r; partials of r.z,
+// r.r and r.z_old (flexible / Polak-Ribiere beta)
 __global__ void pcg_update_kernel(PcgVecs v, int K, int Np, int parity) {
     if (v.S->done) return;
     __shared__ double s_alpha;
@@ -332,7 +347,7 @@ __global__ void pcg_update_kernel(PcgVecs v, int K, int Np, int parity) {
     const double alpha = s_alpha;
     const int EB = blockDim.x / Np;
     const int e = threadIdx.x / Np, i = threadIdx.x - e * Np;
-    double rz = 0, rr = 0;
+    double rz = 0, rr = 0, rzo = 0;
     const int ngroups = (K + EB - 1) / EB;
     for (int grp = blockIdx.x; grp < ngroups; grp += gridDim.x) {
         const int k = grp * EB + e;
@@ -344,14 +359,18 @@ __global__ void pcg_update_kernel(PcgVecs v, int K, int Np, int parity) {
         }
         __syncthreads();  // the element's r rows are written by this CTA
         if (act) {
-            const double z = bj_apply_row(v.P32, v.r, Np, k, i);
+            const double zo = v.z[idx];
+            const double z = bj_apply(v, Np, k, i);
             v.z[idx] = z;
-            rz += v.r[idx] * z;
-            rr += v.r[idx] * v.r[idx];
+            const double ri = v.r[idx];
+            rz += ri * z;
+            rr += ri * ri;
+            rzo += ri * zo;
         }
         __syncthreads();
     }
     block_sum2(rz, rr, v.part_rz + parity * v.G + blockIdx.x, v.part_rr + blockIdx.x);
+    block_sum2(rzo, 0.0, v.part_rzo + blockIdx.x, nullptr);
 }
 
 // beta = rz_new / rz_old; p = z + beta p; convergence test on r.r
@@ -362,9 +381,10 @@ __global__ void pcg_pupdate_kernel(PcgVecs v, size_t n, int parity) {
     if (threadIdx.x < 32) {
         const double rz_new = warp_sum(v.part_rz + parity * v.G, v.G);
         const double rz_old = warp_sum(v.part_rz + (parity ^ 1) * v.G, v.G);
+        const double rzo = warp_sum(v.part_rzo, v.G);
         const double rr = warp_sum(v.part_rr, v.G);
         if (threadIdx.x == 0) {
-            s_beta = rz_new / rz_old;
+            s_beta = (rz_new - rzo) / rz_old;
             int stop = 0;
             if (!(rr == rr) || !(rz_new == rz_new) || rz_old == 0.0) stop = 2;
             else if (rr <= v.S->tol2) stop = 1;

@@ -32,7 +32,9 @@ struct PcgVecs {
     double *part_pap;            // [G]
     double *part_rz;             // [2][G]
     double *part_rr;             // [G]
+    double *part_rzo;            // [G] r_new . z_old (flexible beta)
     const float* P32;            // block-Jacobi inverse blocks (FP32), K x Np x Np
+    const double* P64;           // FP64 blocks; used instead of P32 when set
     PcgScalars* S;
     int G;                       // grid of the reduction kernels
 };

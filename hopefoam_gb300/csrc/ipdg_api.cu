@@ -180,7 +180,7 @@ int dg_ipdg_setup(dg_ctx* c, double tau_coef) {
     rc |= ialloc(c, s, &s->d_z, n);
     rc |= ialloc(c, s, &s->d_p, n);
     rc |= ialloc(c, s, &s->d_Ap, n);
-    rc |= ialloc(c, s, &s->d_part, (size_t)4 * s->G);
+    rc |= ialloc(c, s, &s->d_part, (size_t)5 * s->G);
     rc |= ialloc(c, s, &s->d_S, 1);
     rc |= ialloc(c, s, &s->d_scal, 4);
     rc |= ialloc(c, s, &s->d_status, 1);
@@ -255,7 +255,9 @@ int dg_pcg_solve(dg_ctx* c, const double* b_host, double* x_host, double rtol, i
     v.part_pap = s->d_part;
     v.part_rz = s->d_part + s->G;  // [2][G]
     v.part_rr = s->d_part + 3 * s->G;
+    v.part_rzo = s->d_part + 4 * s->G;
     v.P32 = s->d_blocks32;
+    v.P64 = nullptr;
     v.S = s->d_S;
     v.G = s->G;
     int total_it = 0, stop = 0;
@@ -268,6 +270,7 @@ int dg_pcg_solve(dg_ctx* c, const double* b_host, double* x_host, double rtol, i
         if (rc) return rc;
         IP_CUDA(c, launch_xmy(s->d_r, s->d_b, s->d_Ap, n, c->stream));
         v.x = s->d_x;
+        v.P64 = s->d_blocks;  // FP64 preconditioner: an inexact one stalls CG at high condition numbers
         rc = run_cg(c, v, false, rtol * rtol * bb, maxit, &total_it, &stop);
         if (rc) return rc;
     } else {

@@ -147,10 +147,13 @@ def box_square(nx, ny, Lx, Ly, x0=0.0, y0=0.0, name=""):
     return Mesh(EToV, VXY, EToE, EToF, ROT, BC, name or "box_%dx%dx2" % (nx, ny))
 
 
-def delaunay_square(n_interior, L=2 * np.pi, n_edge=None, seed=0, name=""):
-    """Unstructured Delaunay triangulation of [0,L]^2 from seeded uniform
-    interior points plus evenly spaced boundary points; boundary faces are
-    Dirichlet.  About 2*n_interior triangles."""
+def delaunay_square(n_interior, L=2 * np.pi, n_edge=None, seed=0, jitter=0.35, uniform=False, name=""):
+    """Unstructured Delaunay triangulation of [0,L]^2 from a seeded point set
+    plus evenly spaced boundary points; boundary faces are Dirichlet.  About
+    2*n_interior triangles.  The interior points are a jittered lattice
+    (each point moved by U(-jitter*h, jitter*h) per coordinate), which keeps
+    the triangles well shaped; uniform=True draws them i.i.d. uniform instead
+    (slivers, much worse conditioning)."""
     from scipy.spatial import Delaunay
 
     rng = np.random.default_rng(seed)
@@ -164,7 +167,15 @@ def delaunay_square(n_interior, L=2 * np.pi, n_edge=None, seed=0, name=""):
         np.stack([np.zeros_like(t), L - t], 1),
     ])
     margin = 0.25 * L / n_edge
-    pts = rng.uniform(margin, L - margin, size=(n_interior, 2))
+    if uniform:
+        pts = rng.uniform(margin, L - margin, size=(n_interior, 2))
+    else:
+        m = max(2, int(round(np.sqrt(n_interior))))
+        h = L / (m + 1)
+        g = (np.arange(m) + 1) * h
+        X, Y = np.meshgrid(g, g, indexing="ij")
+        pts = np.stack([X.reshape(-1), Y.reshape(-1)], 1)
+        pts = pts + rng.uniform(-jitter * h, jitter * h, size=pts.shape)
     P = np.concatenate([bnd, pts])
     tri = Delaunay(P)
     EToV = tri.simplices.astype(np.int32)

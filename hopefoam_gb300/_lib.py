@@ -59,7 +59,9 @@ SIGNATURES = {
     "dg_ipdg_apply": (ctypes.c_int, [_vp, _dp, _dp]),
     "dg_pcg_solve": (ctypes.c_int, [_vp, _dp, _dp, ctypes.c_double, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                     ctypes.POINTER(SolveStats)]),
+    "dg_euler_rhs_noalloc": (ctypes.c_int, [_vp, _vp, _vp, ctypes.c_int]),
 }
+DG_NOALLOC_MAX_VALUES = 524288
 
 _lib = None
 

@@ -164,6 +164,24 @@ int dg_ipdg_apply(dg_ctx* ctx, const double* x_host, double* y_host);
 int dg_pcg_solve(dg_ctx* ctx, const double* b_host, double* x_host, double rtol, int maxit, int pc, int precision,
                  dg_solve_stats* stats);
 
+/* Allocation-free right-hand side.  No counterpart in the reference: it is an
+ * addition for callers that must not allocate device memory while they run
+ * (inside a CUDA stream capture, under an application-owned memory pool, or
+ * in a loop with a real-time budget).  Same result as dg_euler_rhs with
+ * DG_PREC_FP64, but state and output are device arrays in the reference
+ * layout (q_dev, rhs_dev: 4*K*Np doubles each, on the context's device, which
+ * must be current) and the call makes no allocation: its scratch is a fixed
+ * array in device global memory, 2 x DG_NOALLOC_MAX_VALUES doubles (8 MiB),
+ * kept by every GPU that loads the library until the process exits.  Sizes
+ * with 4*K*Np > DG_NOALLOC_MAX_VALUES are rejected with DG_ERR_ARG.  The
+ * first call on a device looks up the scratch address; make that first call
+ * before any stream capture starts.  Work is queued on the context's stream
+ * and the call returns without synchronising.  All calls share the scratch
+ * array, which keeps the last call's contents; calls whose GPU work overlaps
+ * in time (other streams, other contexts on the same device) race on it. */
+#define DG_NOALLOC_MAX_VALUES 524288
+int dg_euler_rhs_noalloc(dg_ctx* ctx, const double* q_dev, double* rhs_dev, int flux);
+
 /* Host-only (no GPU needed): the reference-element operators this library
  * builds for order N from a cubature rule, in the reference node order.
  * Arrays are caller-allocated: r, s [Np]; Dr, Ds, Mref [Np*Np] (row-major);

@@ -23,7 +23,7 @@
 // low-storage RK register is FP32 (it carries dt*R, whose own precision is
 // FP32); q += b*res is the only FP64 arithmetic per value in the update.
 //
-// Structure: persistent CTAs (one per SM, 256 threads), 32 elements per tile.
+// Structure: persistent CTAs (one per SM, 512 threads), 32 elements per tile.
 // Per tile: stage q (FP64 tile in shared memory, reference state, FP32 deltas,
 // TF32 hi/lo in the canonical no-swizzle K-major layout, see umma.cuh) ->
 // GEMM1 (issued by one thread, completion on an mbarrier) -> face fluxes in
@@ -49,7 +49,7 @@ namespace dgk {
 template <int N>
 struct SplitDims {
     static constexpr int Np = Dims<N>::Np, Ng = Dims<N>::Ng, Nfp = Dims<N>::Nfp, Nfq = Dims<N>::Nfq;
-    static constexpr int E = 32, ROWS = 128, THREADS = 256;
+    static constexpr int E = 32, ROWS = 128, THREADS = 512;
     static constexpr int KP1 = (Np + 7) / 8 * 8;      // GEMM1 K (padded nodes)
     static constexpr int NG = (Ng + 15) / 16 * 16;    // GEMM1 N (padded cubature points)
     static constexpr int NF = (3 * Nfq + 7) / 8 * 8;  // face-flux K
@@ -105,7 +105,7 @@ __device__ __forceinline__ float pick4(const float* x, int i) {
 }
 
 template <int N>
-__global__ void __launch_bounds__(256, 1) euler_stage_split_kernel(SplitArgs sa) {
+__global__ void __launch_bounds__(512, 1) euler_stage_split_kernel(SplitArgs sa) {
     using D = SplitDims<N>;
     constexpr int Np = D::Np, Ng = D::Ng, Nfp = D::Nfp, Nfq = D::Nfq, E = D::E;
     constexpr int KP1 = D::KP1, NG = D::NG, NF = D::NF, NP2 = D::NP2, KP2 = D::KP2, CH = D::CH, KC = D::KC;
@@ -165,8 +165,9 @@ __global__ void __launch_bounds__(256, 1) euler_stage_split_kernel(SplitArgs sa)
     uint32_t ph2[2] = {0, 0};
     bool failed = false;
 
-    // this thread's rows in the element-major TMEM layout r = 4 e + v
-    const int qd = warp & 3, half = warp >> 2;
+    // this thread's rows in the element-major TMEM layout r = 4 e + v; the
+    // four warps sharing a lane quarter split the columns (sub = 0..3)
+    const int qd = warp & 3, sub = warp >> 2;
     const int my_e = 8 * qd + (lane >> 2), my_v = lane & 3;
 
     for (int tile = blockIdx.x; tile < ntiles && !failed; tile += gridDim.x) {
@@ -223,9 +224,10 @@ __global__ void __launch_bounds__(256, 1) euler_stage_split_kernel(SplitArgs sa)
         //      lane i = face node i (gather) and face Gauss point i (flux)
         {
             const int i = lane & 7;
+            // 96 groups of 8 lanes over 512 threads: warps 0-7 take two groups, 8-15 one
+            // (the bound is warp-uniform, so the shuffles below see full warps)
 #pragma unroll 1
-            for (int j = 0; j < 3; j++) {
-                const int G = (tid >> 3) + 32 * j;
+            for (int G = tid >> 3; G < 3 * E; G += D::THREADS / 8) {
                 const int e = G / 3, f = G - 3 * e;
                 const bool valid = e < ne;
                 const int k = k0 + (valid ? e : 0);
@@ -309,34 +311,33 @@ __global__ void __launch_bounds__(256, 1) euler_stage_split_kernel(SplitArgs sa)
         for (int ch = 0; ch < D::NCH; ch++) {
             const int buf = (D::NBUF == 2) ? (ch & 1) : 0;
             float* sAC = reinterpret_cast<float*>(smem + D::OFF_AC + buf * STRIDE_AC);
-            // this thread's row (e, v) at 8 cubature points of the chunk
-            float x[8];
-            umma::tmem_ld8(tD1 + ((uint32_t)(32 * qd) << 16) + ch * CH + half * 8, x);
+            // this thread's row (e, v) at 4 cubature points of the chunk
+            float x[4];
+            umma::tmem_ld4(tD1 + ((uint32_t)(32 * qd) << 16) + ch * CH + sub * 4, x);
             umma::tmem_ld_wait();
-            float fr[2][4], fs[2][4];
-#pragma unroll
-            for (int s2 = 0; s2 < 2; s2++) {
-                // gather the 4 variables at point (my_v + 4 s2) of the 8 from the element's 4 lanes
+            float fr[1][4], fs[1][4];
+            {
+                // gather the 4 variables at point (sub*4 + my_v) from the element's 4 lanes
                 float dq[4];
 #pragma unroll
                 for (int s = 0; s < 4; s++) {
-                    const float send = pick4(x + 4 * s2, (my_v + s) & 3);
+                    const float send = pick4(x, (my_v + s) & 3);
                     const float got = __shfl_sync(0xffffffffu, send, (lane & ~3) | ((my_v - s) & 3));
                     dq[(my_v - s) & 3] = got;
                 }
-                const int g = ch * CH + half * 8 + my_v + 4 * s2;
+                const int g = ch * CH + sub * 4 + my_v;
                 if (g < Ng && my_e < ne) {
                     const DeltaPrim d = delta_prim(gamma, bref, dq);
                     float fx[4], fy[4];
                     flux_delta(bref, dq, d, fx, fy);
 #pragma unroll
                     for (int v = 0; v < 4; v++) {
-                        fr[s2][v] = rx * fx[v] + ry * fy[v];
-                        fs[s2][v] = sx * fx[v] + sy * fy[v];
+                        fr[0][v] = rx * fx[v] + ry * fy[v];
+                        fs[0][v] = sx * fx[v] + sy * fy[v];
                     }
                 } else {
 #pragma unroll
-                    for (int v = 0; v < 4; v++) fr[s2][v] = fs[s2][v] = 0.f;
+                    for (int v = 0; v < 4; v++) fr[0][v] = fs[0][v] = 0.f;
                 }
             }
             // the MMAs that last read this buffer must be complete
@@ -345,18 +346,17 @@ __global__ void __launch_bounds__(256, 1) euler_stage_split_kernel(SplitArgs sa)
                 ph2[buf] ^= 1;
                 if (__syncthreads_or(!ok)) { failed = true; break; }
             }
-#pragma unroll
-            for (int s2 = 0; s2 < 2; s2++) {
-                const int gl = half * 8 + my_v + 4 * s2;
+            {
+                const int gl = sub * 4 + my_v;
 #pragma unroll
                 for (int v = 0; v < 4; v++) {
                     const int r = 4 * my_e + v;
                     float hi, lo;
-                    umma::split_tf32(fr[s2][v], hi, lo);
+                    umma::split_tf32(fr[0][v], hi, lo);
                     uint32_t off = umma::kmajor_offset(r, gl, KC) >> 2;
                     sAC[off] = hi;
                     sAC[off + LO_AC / 4] = lo;
-                    umma::split_tf32(fs[s2][v], hi, lo);
+                    umma::split_tf32(fs[0][v], hi, lo);
                     off = umma::kmajor_offset(r, CH + gl, KC) >> 2;
                     sAC[off] = hi;
                     sAC[off + LO_AC / 4] = lo;
@@ -415,8 +415,7 @@ __global__ void __launch_bounds__(256, 1) euler_stage_split_kernel(SplitArgs sa)
         // ---- (D) epilogue: R (tensor memory) -> staging -> coalesced stage update
         {
 #pragma unroll
-            for (int c0 = 0; c0 < NP2 / 2; c0 += 8) {
-                const int col = half * (NP2 / 2) + c0;
+            for (int col = sub * 8; col < NP2; col += 32) {
                 float val[8];
                 umma::tmem_ld8(tD2 + ((uint32_t)(32 * qd) << 16) + col, val);
                 umma::tmem_ld_wait();

@@ -177,6 +177,7 @@ def main():
     ap.add_argument("--nx", type=int, default=256)
     ap.add_argument("--order", type=int, default=5)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-poisson", action="store_true")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
@@ -291,11 +292,60 @@ def main():
         v, el = cpu_baseline(mesh, order, q0, dt, threads)
         line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
                                 "sample": "one LSERK4 step (5 stages) over all %d elements, %.1f s" % (mesh.K, el)}
+    ctx.close()
+    if rank == 0 and not args.no_poisson:
+        try:
+            line["poisson"] = poisson_bench(with_cpu=not args.no_cpu_baseline)
+        except Exception as exc:  # reported, never hides the Euler line
+            line["poisson"] = {"error": str(exc)}
     if rank == 0:
         print(json.dumps(line))
-    ctx.close()
     if world > 1:
         torch.distributed.destroy_process_group()
+
+
+def poisson_bench(with_cpu, n_interior=50000, order=4, tau_coef=1.0, rtol=1e-10):
+    """Pressure-Poisson workload: SIPG (tau = (N+1)^2 / h, i.e. tau_coef 1 with
+    h = J/sJ) on a seeded ~100k-triangle Delaunay mesh of [0, 2pi]^2, N = 4,
+    Dirichlet boundary, Taylor-Green + random Fourier RHS; wall ms of the
+    block-Jacobi PCG to 1e-10 (true FP64 residual), mixed-precision and
+    plain-FP64 arithmetic, and the learned preconditioner when one is loaded."""
+    from hopefoam_gb300 import _lib as L
+    from hopefoam_gb300.mesh import delaunay_square
+    from hopefoam_gb300.poisson import PressureSolver, poisson_rhs
+
+    mesh = delaunay_square(n_interior, seed=0)
+    ps = PressureSolver(mesh, order, tau_coef=tau_coef)
+    b, _ = poisson_rhs(mesh, order, seed=1)
+    out = {"workload": "SIPG N=%d, Delaunay [0,2pi]^2 K=%d, tau=(N+1)^2/h, Dirichlet, TG+Fourier(k<=16) rhs"
+                       % (order, mesh.K), "rtol": rtol}
+    ps.solve(b, rtol=1e-4, precision=L.DG_PREC_SPLIT, raise_on_fail=False)  # warm-up
+    x, st = ps.solve(b, rtol=rtol, precision=L.DG_PREC_SPLIT, raise_on_fail=False)
+    out["bj_mixed"] = {"ms": st["ms"], "iterations": st["iterations"], "rel_residual": st["rel_residual"]}
+    x, st64 = ps.solve(b, rtol=rtol, precision=L.DG_PREC_FP64, maxit=4000, raise_on_fail=False)
+    out["bj_fp64"] = {"ms": st64["ms"], "iterations": st64["iterations"], "rel_residual": st64["rel_residual"],
+                      "note": "capped at 4000 iterations" if st64["status"] != L.DG_OK else ""}
+    # algorithmic bytes per iteration (FP64 vectors x 11 passes, FP32 block inverse)
+    Np = ps.Np
+    bytes_it = mesh.K * (8 * Np * 11 + 4 * Np * Np + 136)
+    if st["iterations"]:
+        per_it = st["ms"] * 1e-3 / st["iterations"]
+        out["bj_mixed"]["GBps_per_iteration"] = bytes_it / per_it / 1e9
+    if with_cpu:
+        from hopefoam_gb300.mesh import load_cubature
+        from oracle import oracle
+
+        orc = oracle.Oracle(mesh, order, load_cubature(3 * (order + 1)))
+        diag, off, _ = orc.ipdg_blocks(tau_coef=tau_coef)
+        t = time.perf_counter()
+        _, it, _ = orc.pcg_bj(diag, off, b, rtol=1e-30, maxit=20)
+        per = (time.perf_counter() - t) / max(it, 1)
+        out["cpu_baseline"] = {"ms": per * 1e3 * st64["iterations"] if st64["iterations"] else None,
+                               "kind": "port", "cores": oracle.max_threads(),
+                               "sample": "20 oracle block-Jacobi CG iterations on the same system, scaled to the FP64 "
+                                         "iteration count"}
+    ps.ctx.close()
+    return out
 
 
 def _split_ready(ctx):

@@ -25,8 +25,8 @@ __device__ __forceinline__ void euler_phys_flux(T gamma, const T q[4], T fx[4], 
 // metrics (face 0: s = -1, face 1: r + s = 0, face 2: r = -1); equals the
 // reference's faceNx / fscale (gaussTriangleIntegration.C:153-192,
 // triangleBaseFunction.C:393-419) for straight edges.
-__device__ __forceinline__ void face_normal(int f, double rx, double sx, double ry, double sy, double& nx, double& ny,
-                                            double& fsc) {
+__host__ __device__ __forceinline__ void face_normal(int f, double rx, double sx, double ry, double sy, double& nx,
+                                                     double& ny, double& fsc) {
     double gx, gy;
     if (f == 0) { gx = -sx; gy = -sy; }
     else if (f == 1) { gx = rx + sx; gy = ry + sy; }

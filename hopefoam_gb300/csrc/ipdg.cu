@@ -25,6 +25,7 @@
 // iterations of the mixed-precision solve).  Vectors, dot products and the
 // CG recurrences are FP64 (dot products reduced deterministically: per-block
 // partial sums, then a fixed-order reduction).
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -34,137 +35,232 @@
 #include "dg_ctx.hpp"
 #include "euler_flux.cuh"
 #include "ipdg.hpp"
+#include "lpc.hpp"
+#include "pcg_reduce.cuh"
 
 namespace dgk {
 
 template <int N>
 struct IpDims {
     static constexpr int Np = Dims<N>::Np, Nfp = Dims<N>::Nfp, Nfq = Dims<N>::Nfq;
-    static constexpr int E = (N <= 3) ? 16 : 8;  // elements per CTA
-    static constexpr int THREADS = 128;
+    static constexpr int THREADS = 256;
+    static constexpr int W = (Np > 3 * Nfq) ? Np : 3 * Nfq;  // threads one element needs in either phase
+    static constexpr int E = THREADS / W;                    // elements per tile
 };
 
-// per-(element, face, Gauss point) coefficients of the face terms
-//   c1 = wJ (tau/2 [u] - sigma)   (multiplies phi_i)
-//   c2 = -wJ [u] / 2              (multiplies dphi_i/dn)
-// Grid-stride over tiles of E elements so that the optional dot-product
-// partial (u . y per CTA, into part[blockIdx.x]) has one entry per CTA.
+template <typename T>
+__device__ __forceinline__ const IpdgOps<T>& ops_of(const IpdgArgs& a);
+template <>
+__device__ __forceinline__ const IpdgOps<double>& ops_of<double>(const IpdgArgs& a) { return a.o64; }
+template <>
+__device__ __forceinline__ const IpdgOps<float>& ops_of<float>(const IpdgArgs& a) { return a.o32; }
+
+// Per tile of E elements:
+//  (1) staging: the input of the element and of its three face neighbours
+//      enters shared memory as offsets from one value per element (its
+//      first ring node), formed in FP64 and then rounded to T; the offset
+//      between the two elements' values across each face is kept too (FP64
+//      difference, rounded to T).  Gradients annihilate constants, so the
+//      operator sees only these differences: for a smooth field they are
+//      O(h) smaller than the field, and in FP32 arithmetic the apply's error
+//      shrinks by that factor (the full field would carry eps32 |u| into
+//      every jump and derivative and cost CG its convergence at large
+//      condition numbers).  In the PCG the input is the new search direction
+//      p = z + beta p_old, formed here in FP64 (and written out for the
+//      element's own rows) so that no separate update pass is needed;
+//  (2) one thread per (element, face, Gauss point): traces and normal
+//      derivatives of both sides, then
+//        c1 = wJ (tau/2 [u] - sigma)         multiplies phi_i
+//        c2 = -wJ [u] / 2, times n.grad r / n.grad s of the element
+//                                            multiply dphi_i/dr, dphi_i/ds;
+//  (3) one thread per (element, node): volume term and the face terms.
+// Operator tables are read with the thread index running along the
+// contiguous dimension (the stiffness parts are symmetric, the face
+// derivative tables exist in both layouts), so every warp load is coalesced.
+// Persistent CTAs (a few per SM) stride over the tiles; in the PCG each CTA's
+// share of p.Ap enters one deterministic grid-wide sum whose last CTA also
+// forms alpha (one arrival per CTA, not per tile).
+struct ApplyPcg {
+    const double* p_old;  // previous search direction (read when beta != 0)
+    double* p_new;        // this direction, written for each element's rows
+    PcgScalars* S;        // beta in, pap / alpha out; null outside the PCG
+    double* part;
+    // FP32 offset mirrors (element value minus the element's first-node
+    // value) of z and of the search directions; used by the FP32 apply in the
+    // PCG so that staging needs no FP64 arithmetic per node
+    const float* dz;
+    const float* dp_old;
+    float* dp_new;
+};
+
 template <int N, typename T>
-__global__ void __launch_bounds__(128) ipdg_apply_kernel(IpdgArgs a, const double* __restrict__ u,
-                                                         double* __restrict__ y, double* __restrict__ part,
-                                                         const int* __restrict__ done) {
+__global__ void __launch_bounds__(256, 4) ipdg_apply_kernel(IpdgArgs a, const double* __restrict__ u,
+                                                         double* __restrict__ y, ApplyPcg pc) {
     using D = IpDims<N>;
-    constexpr int Np = D::Np, Nfp = D::Nfp, Nfq = D::Nfq, E = D::E, NB = 3 * N;
-    __shared__ T us[E][Np];
-    __shared__ T c1[E][3][Nfq];
-    __shared__ T c2[E][3][Nfq];
-    __shared__ T ar[E][3], as_[E][3];
-    __shared__ double red[D::THREADS / 32];
-    if (done && *done) return;
+    constexpr int Np = D::Np, Nfp = D::Nfp, Nfq = D::Nfq, E = D::E, NB = 3 * N, NF = 3 * Nfq;
+    const IpdgOps<T>& o = ops_of<T>(a);
+    __shared__ T us[E][Np];         // own offsets u - u_k0
+    __shared__ T un[E][3][Np];      // neighbour offsets u_nb - u_nb0
+    __shared__ T dc[E][3];          // u_k0 - u_nb0 (0 on boundary faces)
+    __shared__ T ub0[E];            // u_k0 rounded (Dirichlet jumps)
+    __shared__ double pd[E][Np];    // own input in FP64 (offsets, p.Ap)
+    __shared__ double stg[E][3][Np];  // neighbour input in FP64 (when not staged from the mirrors)
+    __shared__ int nbr[E][3];       // packed neighbour (conn)
+    __shared__ T c1[E][NF];
+    __shared__ T c2r[E][NF];
+    __shared__ T c2s[E][NF];
+    double beta = 0.0;
+    if (pc.S) {
+        if (pc.S->done) return;
+        beta = pc.S->beta;
+    }
+    const double* __restrict__ p_old = pc.p_old;
+    const bool mirrors = sizeof(T) == 4 && pc.dz != nullptr;
+    const bool has_beta = beta != 0.0;  // uniform: one FP64 compare per thread
+    const float betaf = (float)beta;
     const int ntiles = (a.K + E - 1) / E;
     double dot = 0;
     for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-        const int k0 = tile * E;
-        const int ne = min(E, a.K - k0);
-        for (int i = threadIdx.x; i < ne * Np; i += blockDim.x) us[i / Np][i % Np] = (T)u[(size_t)k0 * Np + i];
-        __syncthreads();
-        // face terms
-        for (int it = threadIdx.x; it < ne * 3 * Nfq; it += blockDim.x) {
-            const int e = it / (3 * Nfq), rem = it - e * 3 * Nfq, f = rem / Nfq, g = rem - f * Nfq;
-            const int k = k0 + e;
-            const double* gk = a.geo + (size_t)k * 4;
-            double nxd, nyd, fscd;
-            face_normal(f, gk[0], gk[1], gk[2], gk[3], nxd, nyd, fscd);
-            const T nx = (T)nxd, ny = (T)nyd;
-            const T arr = nx * (T)gk[0] + ny * (T)gk[2];  // n . grad r
-            const T ass = nx * (T)gk[1] + ny * (T)gk[3];  // n . grad s
-            if (g == 0) { ar[e][f] = arr; as_[e][f] = ass; }
-            T um = 0, dm = 0;
-#pragma unroll
-            for (int j = 0; j < Nfp; j++) um += (T)a.If[g * Nfp + j] * us[e][(f * N + j) % NB];
-            const double* drf = a.Drf + (size_t)(f * Nfq + g) * Np;
-            const double* dsf = a.Dsf + (size_t)(f * Nfq + g) * Np;
-#pragma unroll
-            for (int p = 0; p < Np; p++) dm += (arr * (T)drf[p] + ass * (T)dsf[p]) * us[e][p];
-            T up, dp;
-            double tau;
-            const int c = a.conn[(size_t)k * 3 + f];
-            if (c >= 0) {
-                const int nb = c >> 3, fn = c & 3, rot = (c >> 2) & 1;
-                const double* gn = a.geo + (size_t)nb * 4;
-                double nx2, ny2, fsc2;
-                face_normal(fn, gn[0], gn[1], gn[2], gn[3], nx2, ny2, fsc2);
-                tau = a.tau_coef * (N + 1) * (N + 1) * fmax(fscd, fsc2);
-                const double* un = u + (size_t)nb * Np;
-                up = 0;
-#pragma unroll
-                for (int j = 0; j < Nfp; j++) {
-                    const int jj = rot ? (N - j) : j;
-                    up += (T)a.If[g * Nfp + j] * (T)un[(fn * N + jj) % NB];
-                }
-                const int g2 = rot ? (Nfq - 1 - g) : g;
-                const T ar2 = nx * (T)gn[0] + ny * (T)gn[2], as2 = nx * (T)gn[1] + ny * (T)gn[3];
-                const double* drn = a.Drf + (size_t)(fn * Nfq + g2) * Np;
-                const double* dsn = a.Dsf + (size_t)(fn * Nfq + g2) * Np;
-                dp = 0;
-#pragma unroll
-                for (int p = 0; p < Np; p++) dp += (ar2 * (T)drn[p] + as2 * (T)dsn[p]) * (T)un[p];
-            } else {
-                tau = a.tau_coef * (N + 1) * (N + 1) * fscd;
-                up = -um;
-                dp = dm;
-            }
-            const T wJ = (T)(fscd * a.J[k] * a.fw[g]);
-            const T jump = um - up;
-            const T sigma = (T)0.5 * (dm + dp);
-            c1[e][f][g] = wJ * ((T)(0.5 * tau) * jump - sigma);
-            c2[e][f][g] = -(T)0.5 * wJ * jump;
+    const int k0 = tile * E;
+    const int ne = min(E, a.K - k0);
+    // (1) staging.  FP64 work is kept out of divergent branches: a warp
+    // instruction occupies the FP64 pipe for its full width whatever its
+    // active lanes.  (a) own rows, (b) neighbour rows, (c) per element face.
+    for (int t = threadIdx.x; t < ne * Np; t += blockDim.x) {
+        const int e = t / Np, p = t - e * Np;
+        const size_t i = (size_t)k0 * Np + t;
+        const double vp = has_beta ? fma(beta, p_old[i], u[i]) : u[i];
+        pd[e][p] = vp;
+        if (pc.p_new) pc.p_new[i] = vp;
+        if (mirrors) {
+            float d = pc.dz[i];
+            if (has_beta) d = fmaf(betaf, pc.dp_old[i], d);
+            us[e][p] = (T)d;
+            pc.dp_new[i] = d;
         }
-        __syncthreads();
-        // element rows
-        for (int it = threadIdx.x; it < ne * Np; it += blockDim.x) {
-            const int e = it / Np, i = it - e * Np;
-            const int k = k0 + e;
-            const double* gk = a.geo + (size_t)k * 4;
-            const T rx = (T)gk[0], sx = (T)gk[1], ry = (T)gk[2], sy = (T)gk[3];
-            const T crr = rx * rx + ry * ry, crs = rx * sx + ry * sy, css = sx * sx + sy * sy;
-            const double* srr = a.Srr + (size_t)i * Np;
-            const double* srs = a.Srs2 + (size_t)i * Np;
-            const double* sss = a.Sss + (size_t)i * Np;
-            T v = 0;
+    }
+    for (int t = threadIdx.x; t < ne * 3 * Np; t += blockDim.x) {
+        const int e = t / (3 * Np), rem = t - e * 3 * Np, f = rem / Np, p = rem - f * Np;
+        const int c = a.conn[(size_t)(k0 + e) * 3 + f];
+        if (p == 0) nbr[e][f] = c;
+        if (c < 0) continue;
+        const size_t i = (size_t)(c >> 3) * Np + p;
+        if (mirrors) {
+            float d = pc.dz[i];
+            if (has_beta) d = fmaf(betaf, pc.dp_old[i], d);
+            un[e][f][p] = (T)d;
+        } else {
+            stg[e][f][p] = has_beta ? fma(beta, p_old[i], u[i]) : u[i];
+        }
+    }
+    __syncthreads();
+    if (!mirrors) {
+        for (int t = threadIdx.x; t < ne * Np; t += blockDim.x) {
+            const int e = t / Np, p = t - e * Np;
+            us[e][p] = (T)(pd[e][p] - pd[e][0]);
+        }
+        for (int t = threadIdx.x; t < ne * 3 * Np; t += blockDim.x) {
+            const int e = t / (3 * Np), rem = t - e * 3 * Np, f = rem / Np, p = rem - f * Np;
+            if (nbr[e][f] >= 0) un[e][f][p] = (T)(stg[e][f][p] - stg[e][f][0]);
+        }
+    }
+    if (threadIdx.x < ne * 3) {
+        const int e = threadIdx.x / 3, f = threadIdx.x - e * 3;
+        const int c = nbr[e][f];
+        double d = 0.0;
+        if (c >= 0) {
+            const size_t i0 = (size_t)(c >> 3) * Np;
+            d = pd[e][0] - (has_beta ? fma(beta, p_old[i0], u[i0]) : u[i0]);
+        }
+        dc[e][f] = (T)d;
+        if (f == 0) ub0[e] = (T)pd[e][0];
+    }
+    __syncthreads();
+    // (2) face terms
+    if (threadIdx.x < ne * NF) {
+        const int e = threadIdx.x / NF, fg = threadIdx.x - e * NF, f = fg / Nfq, g = fg - f * Nfq;
+        const int k = k0 + e;
+        const T* fc = o.fc + ((size_t)k * 3 + f) * kFaceCoef;
+        const T arr = fc[0], ass = fc[1];  // n . grad r, n . grad s
+        T ur = 0, usd = 0, um = 0;
 #pragma unroll
-            for (int p = 0; p < Np; p++) v += (crr * (T)srr[p] + crs * (T)srs[p] + css * (T)sss[p]) * us[e][p];
-            v *= (T)a.J[k];
+        for (int p = 0; p < Np; p++) {
+            ur += o.DrfT[p * NF + fg] * us[e][p];
+            usd += o.DsfT[p * NF + fg] * us[e][p];
+        }
+#pragma unroll
+        for (int j = 0; j < Nfp; j++) um += o.If[g * Nfp + j] * us[e][(f * N + j) % NB];
+        const T dm = arr * ur + ass * usd;
+        T jump, dp;
+        const int c = nbr[e][f];
+        if (c >= 0) {
+            const int fn = c & 3, rot = (c >> 2) & 1;
+            const int g2 = rot ? (Nfq - 1 - g) : g;
+            const int fg2 = fn * Nfq + g2;
+            T vr = 0, vs = 0, up = 0;
+#pragma unroll
+            for (int p = 0; p < Np; p++) {
+                vr += o.DrfT[p * NF + fg2] * un[e][f][p];
+                vs += o.DsfT[p * NF + fg2] * un[e][f][p];
+            }
+#pragma unroll
+            for (int j = 0; j < Nfp; j++) {
+                const int jj = rot ? (N - j) : j;
+                up += o.If[g * Nfp + j] * un[e][f][(fn * N + jj) % NB];
+            }
+            dp = fc[2] * vr + fc[3] * vs;  // own normal . grad r, s of the neighbour
+            jump = (um - up) + dc[e][f];
+        } else {
+            // Dirichlet face: u+ = -u-, so [u] = 2 u- (offset included)
+            jump = (T)2 * (um + ub0[e]);
+            dp = dm;
+        }
+        const T wJ = fc[5] * o.fw[g];
+        const T sigma = (T)0.5 * (dm + dp);
+        const T cc2 = -(T)0.5 * wJ * jump;
+        c1[e][fg] = wJ * (fc[4] * jump - sigma);
+        c2r[e][fg] = cc2 * arr;
+        c2s[e][fg] = cc2 * ass;
+    }
+    __syncthreads();
+    // (3) element rows
+    if (threadIdx.x < ne * Np) {
+        const int e = threadIdx.x / Np, i = threadIdx.x - e * Np;
+        const int k = k0 + e;
+        T A = 0, B = 0, C = 0;
+#pragma unroll
+        for (int p = 0; p < Np; p++) {
+            const T up = us[e][p];
+            A += o.Srr[p * Np + i] * up;
+            B += o.Srs2[p * Np + i] * up;
+            C += o.Sss[p * Np + i] * up;
+        }
+        T v = o.vc[(size_t)k * 3] * A + o.vc[(size_t)k * 3 + 1] * B + o.vc[(size_t)k * 3 + 2] * C;
+#pragma unroll
+        for (int fg = 0; fg < NF; fg++) v += c2r[e][fg] * o.Drf[fg * Np + i] + c2s[e][fg] * o.Dsf[fg * Np + i];
+        if (i < NB) {
 #pragma unroll
             for (int f = 0; f < 3; f++) {
-                int jf = -1;  // phi_i on face f: ring positions f*N .. f*N+N (mod 3N)
-                if (i < NB) {
-                    const int d = (i - f * N + NB) % NB;
-                    if (d <= N) jf = d;
-                }
+                const int d = (i - f * N + NB) % NB;  // phi_i on face f: ring positions f*N .. f*N+N (mod 3N)
+                if (d <= N) {
 #pragma unroll
-                for (int g = 0; g < Nfq; g++) {
-                    const T dn = ar[e][f] * (T)a.Drf[(size_t)(f * Nfq + g) * Np + i] +
-                                 as_[e][f] * (T)a.Dsf[(size_t)(f * Nfq + g) * Np + i];
-                    T t = c2[e][f][g] * dn;
-                    if (jf >= 0) t += c1[e][f][g] * (T)a.If[g * Nfp + jf];
-                    v += t;
+                    for (int g = 0; g < Nfq; g++) v += c1[e][f * Nfq + g] * o.If[g * Nfp + d];
                 }
             }
-            const double out = (double)v;
-            y[(size_t)k * Np + i] = out;
-            dot += out * u[(size_t)k * Np + i];
         }
-        __syncthreads();
+        const double out = (double)v;
+        y[(size_t)k * Np + i] = out;
+        dot += out * pd[e][i];
     }
-    if (part) {
-        for (int o = 16; o > 0; o >>= 1) dot += __shfl_xor_sync(0xffffffffu, dot, o);
-        if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = dot;
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            double s = 0;
-            for (int w = 0; w < D::THREADS / 32; w++) s += red[w];
-            part[blockIdx.x] = s;
+    __syncthreads();  // shared tile buffers are refilled by the next tile
+    }
+    if (pc.S) {
+        double val[1] = {dot}, tot[1];
+        if (grid_sum<1>(val, pc.part, gridDim.x, &pc.S->counter, tot) && threadIdx.x == 0) {
+            const double pap = tot[0];
+            pc.S->pap = pap;
+            pc.S->alpha = pc.S->rz / pap;
+            if (!(pap > 0.0) || !(pc.S->alpha == pc.S->alpha)) pc.S->done = 2;
         }
     }
 }
@@ -174,30 +270,18 @@ template <int N>
 __global__ void ipdg_diag_kernel(IpdgArgs a, double* __restrict__ blocks) {
     using D = IpDims<N>;
     constexpr int Np = D::Np, Nfp = D::Nfp, Nfq = D::Nfq, NB = 3 * N;
+    const IpdgOps<double>& o = a.o64;
     const int k = blockIdx.x;
     const int j = threadIdx.x;  // column
     if (k >= a.K || j >= Np) return;
-    const double* gk = a.geo + (size_t)k * 4;
-    const double rx = gk[0], sx = gk[1], ry = gk[2], sy = gk[3];
-    const double crr = rx * rx + ry * ry, crs = rx * sx + ry * sy, css = sx * sx + sy * sy;
+    const double vrr = o.vc[(size_t)k * 3], vrs = o.vc[(size_t)k * 3 + 1], vss = o.vc[(size_t)k * 3 + 2];
     double col[Np];
     for (int i = 0; i < Np; i++)
-        col[i] = a.J[k] * (crr * a.Srr[i * Np + j] + crs * a.Srs2[i * Np + j] + css * a.Sss[i * Np + j]);
+        col[i] = vrr * o.Srr[i * Np + j] + vrs * o.Srs2[i * Np + j] + vss * o.Sss[i * Np + j];
     for (int f = 0; f < 3; f++) {
-        double nx, ny, fsc;
-        face_normal(f, rx, sx, ry, sy, nx, ny, fsc);
-        const double arr = nx * rx + ny * ry, ass = nx * sx + ny * sy;
+        const double* fc = o.fc + ((size_t)k * 3 + f) * kFaceCoef;
+        const double arr = fc[0], ass = fc[1];
         const int c = a.conn[(size_t)k * 3 + f];
-        double tau;
-        if (c >= 0) {
-            const int nb = c >> 3, fn = c & 3;
-            const double* gn = a.geo + (size_t)nb * 4;
-            double nx2, ny2, fsc2;
-            face_normal(fn, gn[0], gn[1], gn[2], gn[3], nx2, ny2, fsc2);
-            tau = a.tau_coef * (N + 1) * (N + 1) * fmax(fsc, fsc2);
-        } else {
-            tau = a.tau_coef * (N + 1) * (N + 1) * fsc;
-        }
         // u = e_j: own trace / normal derivative at each Gauss point
         int jf = -1;
         if (j < NB) {
@@ -205,18 +289,18 @@ __global__ void ipdg_diag_kernel(IpdgArgs a, double* __restrict__ blocks) {
             if (d <= N) jf = d;
         }
         for (int g = 0; g < Nfq; g++) {
-            const double um = jf >= 0 ? a.If[g * Nfp + jf] : 0.0;
-            const double dm = arr * a.Drf[(size_t)(f * Nfq + g) * Np + j] + ass * a.Dsf[(size_t)(f * Nfq + g) * Np + j];
+            const double um = jf >= 0 ? o.If[g * Nfp + jf] : 0.0;
+            const double dm = arr * o.Drf[(f * Nfq + g) * Np + j] + ass * o.Dsf[(f * Nfq + g) * Np + j];
             const double up = (c >= 0) ? 0.0 : -um;
             const double dp = (c >= 0) ? 0.0 : dm;
-            const double wJ = fsc * a.J[k] * a.fw[g];
+            const double wJ = fc[5] * o.fw[g];
             const double jump = um - up, sigma = 0.5 * (dm + dp);
-            const double cc1 = wJ * (0.5 * tau * jump - sigma), cc2 = -0.5 * wJ * jump;
+            const double cc1 = wJ * (fc[4] * jump - sigma), cc2 = -0.5 * wJ * jump;
             for (int i = 0; i < Np; i++) {
-                double t = cc2 * (arr * a.Drf[(size_t)(f * Nfq + g) * Np + i] + ass * a.Dsf[(size_t)(f * Nfq + g) * Np + i]);
+                double t = cc2 * (arr * o.Drf[(f * Nfq + g) * Np + i] + ass * o.Dsf[(f * Nfq + g) * Np + i]);
                 if (i < NB) {
                     const int d = (i - f * N + NB) % NB;
-                    if (d <= N) t += cc1 * a.If[g * Nfp + d];
+                    if (d <= N) t += cc1 * o.If[g * Nfp + d];
                 }
                 col[i] += t;
             }
@@ -255,163 +339,215 @@ __global__ void invert_blocks_kernel(double* __restrict__ blocks, float* __restr
             for (int j = 0; j < Np; j++) { M[i * Np + j] -= f * M[c * Np + j]; X[i * Np + j] -= f * X[c * Np + j]; }
         }
     }
-    for (int i = 0; i < Np * Np; i++) { A[i] = X[i]; blocks32[(size_t)k * Np * Np + i] = (float)X[i]; }
+    for (int i = 0; i < Np * Np; i++) {
+        A[i] = X[i];
+        if (blocks32) blocks32[(size_t)k * Np * Np + i] = (float)X[i];
+    }
 }
 
 // ---------------------------------------------------------------------------
-// PCG.  Scalars live on the device; every kernel returns immediately once the
-// solve has stopped (S->done), so launches can be issued ahead of the host's
-// convergence check.  Dot products: per-CTA partials over a fixed grid G, then
-// a fixed-order warp reduction by each consumer (deterministic).  The partial
-// r.z is double-buffered by iteration parity so consumers of the old and the
-// new value never race.
+// PCG.  Scalars live on the device (PcgScalars); every kernel returns at once
+// when the solve has stopped (S->done), so launches are issued ahead of the
+// host's convergence check.  Dot products are deterministic grid-wide sums
+// (pcg_reduce.cuh); the last CTA of each sum forms the scalars that the next
+// kernel needs (alpha after the apply, beta and the stop test after the
+// update), so an iteration is two launches: apply (with p = z + beta p_old
+// fused in) and update.
 
-__device__ __forceinline__ double warp_sum(const double* __restrict__ part, int n) {
-    double s = 0;
-    for (int i = threadIdx.x & 31; i < n; i += 32) s += part[i];
-    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-    return s;
-}
-
-__device__ __forceinline__ void block_sum2(double a, double b, double* oa, double* ob) {
-    __shared__ double ra[32], rb[32];
-    for (int o = 16; o > 0; o >>= 1) {
-        a += __shfl_xor_sync(0xffffffffu, a, o);
-        b += __shfl_xor_sync(0xffffffffu, b, o);
-    }
-    if ((threadIdx.x & 31) == 0) { ra[threadIdx.x >> 5] = a; rb[threadIdx.x >> 5] = b; }
+// standalone partial sums (host-side dot products): per-CTA partials over a
+// fixed grid, reduced in fixed order by reduce_to_kernel
+__device__ __forceinline__ void block_sum1(double a, double* oa) {
+    __shared__ double ra[32];
+    for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
+    if ((threadIdx.x & 31) == 0) ra[threadIdx.x >> 5] = a;
     __syncthreads();
     if (threadIdx.x == 0) {
-        double sa = 0, sb = 0;
-        for (int w = 0; w < (int)((blockDim.x + 31) >> 5); w++) { sa += ra[w]; sb += rb[w]; }
-        if (oa) *oa = sa;
-        if (ob) *ob = sb;
+        double sa = 0;
+        for (int w = 0; w < (int)((blockDim.x + 31) >> 5); w++) sa += ra[w];
+        *oa = sa;
     }
-    __syncthreads();  // ra/rb are reused by the next call
 }
 
-// element-aligned thread mapping: CTA = EB elements x Np rows (EB*Np <= blockDim)
-__device__ __forceinline__ double bj_apply_row(const float* __restrict__ P, const double* __restrict__ r, int Np,
-                                               int k, int i) {
-    const float* row = P + ((size_t)k * Np + i) * Np;
-    const double* rk = r + (size_t)k * Np;
-    float s = 0.f;
-    for (int j = 0; j < Np; j++) s = fmaf(row[j], (float)rk[j], s);
+// Element-aligned kernels: a group of EB = 256 / Np whole elements, one
+// thread per (element, row), Np a compile-time constant so that the block
+// products unroll (Np independent loads in flight per thread).  Persistent
+// CTAs (a few per SM) stride over the groups, so each grid-wide sum has one
+// arrival per CTA.  The inverse diagonal blocks are stored grouped: for group
+// g and column j the EB x Np entries (element, row) are contiguous,
+//   Pg[((g Np + j) EB + e) Np + i] = P_{g EB + e}[i][j],
+// so the CTA's loads for one column form a single contiguous read.
+template <int NP>
+struct RowDims {
+    static constexpr int EB = 256 / NP;
+    static constexpr int THREADS = (EB * NP + 31) / 32 * 32;  // extra lanes idle but join the reductions
+};
+
+__device__ __forceinline__ float fma_t(float a, float b, float c) { return fmaf(a, b, c); }
+__device__ __forceinline__ double fma_t(double a, double b, double c) { return fma(a, b, c); }
+
+template <int NP, typename PT, typename RT>
+__device__ __forceinline__ double bj_rowg(const PT* __restrict__ P, const RT* rs, int grp) {
+    constexpr int EBNP = RowDims<NP>::EB * NP;
+    const PT* col = P + (size_t)grp * NP * EBNP + threadIdx.x;
+    PT s = 0;
+#pragma unroll
+    for (int j = 0; j < NP; j++) s = fma_t(col[j * EBNP], (PT)rs[j], s);
     return (double)s;
 }
 
-__device__ __forceinline__ double bj_apply_row64(const double* __restrict__ P, const double* __restrict__ r, int Np,
-                                                 int k, int i) {
-    const double* row = P + ((size_t)k * Np + i) * Np;
-    const double* rk = r + (size_t)k * Np;
-    double s = 0.0;
-    for (int j = 0; j < Np; j++) s += row[j] * rk[j];
-    return s;
-}
-
-__device__ __forceinline__ double bj_apply(const PcgVecs& v, int Np, int k, int i) {
-    return v.P64 ? bj_apply_row64(v.P64, v.r, Np, k, i) : bj_apply_row(v.P32, v.r, Np, k, i);
-}
-
-// z = P r, p = z, part_rz[1] = r.z, part_rr = r.r   (x, r given)
-__global__ void pcg_init_kernel(PcgVecs v, int K, int Np) {
-    const int EB = blockDim.x / Np;
-    const int e = threadIdx.x / Np, i = threadIdx.x - e * Np;
-    double rz = 0, rr = 0;
+// mode 0 (init):    z = P r; S->rz = r.z, S->rr = r.r, beta = 0 (first p = z)
+// mode 1 (refresh): the same, beta kept (residual replacement)
+// Learned mode (v.zb): zb = P r and S->rr only; the learned kernel forms z, r.z.
+template <int NP>
+__global__ void __launch_bounds__(RowDims<NP>::THREADS) pcg_init_kernel(PcgVecs v, int K, int mode) {
+    constexpr int EB = RowDims<NP>::EB;
+    __shared__ double rs[EB][NP];
+    __shared__ float rs32[EB][NP];
+    __shared__ double zs0[EB];
+    const int e = threadIdx.x / NP, i = threadIdx.x - e * NP;
     const int ngroups = (K + EB - 1) / EB;
+    double rz = 0, rr = 0;
     for (int grp = blockIdx.x; grp < ngroups; grp += gridDim.x) {
         const int k = grp * EB + e;
-        if (e < EB && k < K) {
-            const size_t idx = (size_t)k * Np + i;
-            const double z = bj_apply(v, Np, k, i);
-            v.z[idx] = z;
-            v.p[idx] = z;
-            rz += v.r[idx] * z;
-            rr += v.r[idx] * v.r[idx];
+        const bool act = e < EB && k < K;
+        const size_t idx = (size_t)k * NP + i;
+        double ri = 0, z = 0;
+        if (act) {
+            ri = v.r[idx];
+            rs[e][i] = ri;
+            rs32[e][i] = (float)ri;
+        }
+        __syncthreads();
+        if (act) {
+            z = v.P64 ? bj_rowg<NP>(v.P64, rs[e], grp) : bj_rowg<NP>(v.P32, rs32[e], grp);
+            if (v.zb) v.zb[idx] = z;
+            else {
+                v.z[idx] = z;
+                rz += ri * z;
+                if (i == 0) zs0[e] = z;
+            }
+            rr += ri * ri;
+        }
+        if (v.dz && !v.zb) {
+            __syncthreads();
+            if (act) v.dz[idx] = (float)(z - zs0[e]);
+        }
+        __syncthreads();
+    }
+    double val[2] = {rz, rr}, tot[2];
+    if (grid_sum<2>(val, v.part, gridDim.x, &v.S->counter, tot) && threadIdx.x == 0) {
+        v.S->rr = tot[1];
+        if (!v.zb) v.S->rz = tot[0];
+        if (mode == 0) {
+            v.S->beta = 0.0;
+            if (tot[1] <= v.S->tol2) v.S->done = 1;
         }
     }
-    block_sum2(rz, rr, v.part_rz + v.G + blockIdx.x, v.part_rr + blockIdx.x);
 }
 
-// alpha = rz / pAp; x += alpha p; r -= alpha Ap; z = P r; partials of r.z,
-// r.r and r.z_old (flexible / Polak-Ribiere beta)
-__global__ void pcg_update_kernel(PcgVecs v, int K, int Np, int parity) {
-    if (v.S->done) return;
-    __shared__ double s_alpha;
-    if (threadIdx.x < 32) {
-        const double rz = warp_sum(v.part_rz + (parity ^ 1) * v.G, v.G);
-        const double pap = warp_sum(v.part_pap, v.G);
-        if (threadIdx.x == 0) s_alpha = rz / pap;
-    }
-    __syncthreads();
-    const double alpha = s_alpha;
-    const int EB = blockDim.x / Np;
-    const int e = threadIdx.x / Np, i = threadIdx.x - e * Np;
-    double rz = 0, rr = 0, rzo = 0;
+// z = P r over all elements (FP32 blocks)
+template <int NP>
+__global__ void __launch_bounds__(RowDims<NP>::THREADS) bj_kernel(const float* __restrict__ P32,
+                                                                  const double* __restrict__ r,
+                                                                  double* __restrict__ z, int K) {
+    constexpr int EB = RowDims<NP>::EB;
+    __shared__ float rs32[EB][NP];
+    const int e = threadIdx.x / NP, i = threadIdx.x - e * NP;
     const int ngroups = (K + EB - 1) / EB;
     for (int grp = blockIdx.x; grp < ngroups; grp += gridDim.x) {
         const int k = grp * EB + e;
         const bool act = e < EB && k < K;
-        const size_t idx = (size_t)k * Np + i;
+        if (act) rs32[e][i] = (float)r[(size_t)k * NP + i];
+        __syncthreads();
+        if (act) z[(size_t)k * NP + i] = bj_rowg<NP>(P32, rs32[e], grp);
+        __syncthreads();
+    }
+}
+
+// x += alpha p; r -= alpha Ap; z = P r; then beta (flexible, with r.z_old)
+// and the stop test (learned mode: zb = P r and r.r only)
+template <int NP>
+__global__ void __launch_bounds__(RowDims<NP>::THREADS) pcg_update_kernel(PcgVecs v, int K, int parity) {
+    constexpr int EB = RowDims<NP>::EB;
+    if (v.S->done) return;
+    __shared__ double rs[EB][NP];
+    __shared__ float rs32[EB][NP];
+    __shared__ double zs0[EB];
+    const double alpha = v.S->alpha;
+    const double* __restrict__ p = v.p[parity ^ 1];
+    const int e = threadIdx.x / NP, i = threadIdx.x - e * NP;
+    const int ngroups = (K + EB - 1) / EB;
+    double rz = 0, rr = 0, rzo = 0;
+    for (int grp = blockIdx.x; grp < ngroups; grp += gridDim.x) {
+        const int k = grp * EB + e;
+        const bool act = e < EB && k < K;
+        const size_t idx = (size_t)k * NP + i;
+        double ri = 0, z = 0;
         if (act) {
-            v.x[idx] += alpha * v.p[idx];
-            v.r[idx] -= alpha * v.Ap[idx];
+            v.x[idx] += alpha * p[idx];
+            ri = v.r[idx] - alpha * v.Ap[idx];
+            v.r[idx] = ri;
+            if (v.P64) rs[e][i] = ri;
+            else rs32[e][i] = (float)ri;
         }
-        __syncthreads();  // the element's r rows are written by this CTA
+        __syncthreads();
         if (act) {
-            const double zo = v.z[idx];
-            const double z = bj_apply(v, Np, k, i);
-            v.z[idx] = z;
-            const double ri = v.r[idx];
-            rz += ri * z;
+            z = v.P64 ? bj_rowg<NP>(v.P64, rs[e], grp) : bj_rowg<NP>(v.P32, rs32[e], grp);
             rr += ri * ri;
-            rzo += ri * zo;
+            if (v.zb) {
+                v.zb[idx] = z;  // the learned kernel forms z and finishes the iteration
+            } else {
+                const double zo = v.z[idx];
+                v.z[idx] = z;
+                rz += ri * z;
+                rzo += ri * zo;
+                if (i == 0) zs0[e] = z;
+            }
+        }
+        if (v.dz && !v.zb) {
+            __syncthreads();
+            if (act) v.dz[idx] = (float)(z - zs0[e]);
         }
         __syncthreads();
     }
-    block_sum2(rz, rr, v.part_rz + parity * v.G + blockIdx.x, v.part_rr + blockIdx.x);
-    block_sum2(rzo, 0.0, v.part_rzo + blockIdx.x, nullptr);
+    double val[3] = {rz, rr, rzo}, tot[3];
+    if (grid_sum<3>(val, v.part, gridDim.x, &v.S->counter, tot) && threadIdx.x == 0) {
+        if (v.zb) v.S->rr = tot[1];
+        else pcg_finish(v.S, tot[0], tot[2], tot[1]);
+    }
 }
 
-// beta = rz_new / rz_old; p = z + beta p; convergence test on r.r
-__global__ void pcg_pupdate_kernel(PcgVecs v, size_t n, int parity) {
-    if (v.S->done) return;
-    __shared__ double s_beta;
-    __shared__ int s_stop;
-    if (threadIdx.x < 32) {
-        const double rz_new = warp_sum(v.part_rz + parity * v.G, v.G);
-        const double rz_old = warp_sum(v.part_rz + (parity ^ 1) * v.G, v.G);
-        const double rzo = warp_sum(v.part_rzo, v.G);
-        const double rr = warp_sum(v.part_rr, v.G);
-        if (threadIdx.x == 0) {
-            s_beta = (rz_new - rzo) / rz_old;
-            int stop = 0;
-            if (!(rr == rr) || !(rz_new == rz_new) || rz_old == 0.0) stop = 2;
-            else if (rr <= v.S->tol2) stop = 1;
-            s_stop = stop;
-            if (blockIdx.x == 0) {
-                v.S->it += 1;
-                if (stop) v.S->done = stop;
-            }
-        }
+// inverse blocks (row-major per element) -> grouped layout (zero padding)
+template <int NP>
+__global__ void group_blocks_kernel(const double* __restrict__ blk, double* __restrict__ P64,
+                                    float* __restrict__ P32, int K) {
+    constexpr int EB = RowDims<NP>::EB;
+    const int ngroups = (K + EB - 1) / EB;
+    const size_t total = (size_t)ngroups * NP * EB * NP;
+    for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < total; t += (size_t)gridDim.x * blockDim.x) {
+        const int i = (int)(t % NP);
+        const int e = (int)((t / NP) % EB);
+        const int j = (int)((t / ((size_t)NP * EB)) % NP);
+        const int grp = (int)(t / ((size_t)NP * EB * NP));
+        const int k = grp * EB + e;
+        const double val = k < K ? blk[(size_t)k * NP * NP + (size_t)i * NP + j] : 0.0;
+        P64[t] = val;
+        P32[t] = (float)val;
     }
-    __syncthreads();
-    if (s_stop) return;
-    const double beta = s_beta;
-    for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < n; t += (size_t)gridDim.x * blockDim.x)
-        v.p[t] = v.z[t] + beta * v.p[t];
 }
 
 __global__ void dot_kernel(const double* __restrict__ x, const double* __restrict__ y, size_t n, double* part) {
     double s = 0;
     for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < n; t += (size_t)gridDim.x * blockDim.x)
         s += x[t] * y[t];
-    block_sum2(s, 0.0, part + blockIdx.x, nullptr);
+    block_sum1(s, part + blockIdx.x);
 }
 
 __global__ void reduce_to_kernel(const double* __restrict__ part, int G, double* out) {
     if (threadIdx.x < 32) {
-        const double s = warp_sum(part, G);
+        double s = 0;
+        for (int i = threadIdx.x; i < G; i += 32) s += part[i];
+        for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
         if (threadIdx.x == 0) *out = s;
     }
 }
@@ -440,34 +576,46 @@ __global__ void permute_kernel(const double* __restrict__ in, double* __restrict
 // ---------------------------------------------------------------------------
 // launchers
 
+// persistent grid: CTAs per SM that fit (64 registers x 256 threads: 4), at most one per tile
 template <int N>
-static cudaError_t apply_n(const IpdgArgs& a, bool fp32, const double* u, double* y, double* part, int G,
-                           const int* done, cudaStream_t s) {
+static int apply_grid(const IpdgArgs& a) {
+    const int ntiles = (a.K + IpDims<N>::E - 1) / IpDims<N>::E;
+    return std::max(1, std::min(ntiles, 4 * a.sms));
+}
+
+template <int N>
+static cudaError_t apply_n(const IpdgArgs& a, bool fp32, const double* u, double* y, const ApplyPcg& pc,
+                           cudaStream_t s) {
     using D = IpDims<N>;
-    const int ntiles = (a.K + D::E - 1) / D::E;
-    const int grid = part ? G : (ntiles < 65535 * 8 ? ntiles : 65535 * 8);
-    if (fp32) ipdg_apply_kernel<N, float><<<grid, D::THREADS, 0, s>>>(a, u, y, part, done);
-    else ipdg_apply_kernel<N, double><<<grid, D::THREADS, 0, s>>>(a, u, y, part, done);
+    const int grid = apply_grid<N>(a);
+    if (fp32) ipdg_apply_kernel<N, float><<<grid, D::THREADS, 0, s>>>(a, u, y, pc);
+    else ipdg_apply_kernel<N, double><<<grid, D::THREADS, 0, s>>>(a, u, y, pc);
     return cudaGetLastError();
 }
 
-static cudaError_t apply_dispatch(const IpdgArgs& a, bool fp32, const double* u, double* y, double* part, int G,
-                                  const int* done, cudaStream_t s) {
+static cudaError_t apply_dispatch(const IpdgArgs& a, bool fp32, const double* u, double* y, const ApplyPcg& pc,
+                                  cudaStream_t s) {
     switch (a.N) {
-        case 1: return apply_n<1>(a, fp32, u, y, part, G, done, s);
-        case 2: return apply_n<2>(a, fp32, u, y, part, G, done, s);
-        case 3: return apply_n<3>(a, fp32, u, y, part, G, done, s);
-        case 4: return apply_n<4>(a, fp32, u, y, part, G, done, s);
-        case 5: return apply_n<5>(a, fp32, u, y, part, G, done, s);
-        case 6: return apply_n<6>(a, fp32, u, y, part, G, done, s);
-        case 7: return apply_n<7>(a, fp32, u, y, part, G, done, s);
+        case 1: return apply_n<1>(a, fp32, u, y, pc, s);
+        case 2: return apply_n<2>(a, fp32, u, y, pc, s);
+        case 3: return apply_n<3>(a, fp32, u, y, pc, s);
+        case 4: return apply_n<4>(a, fp32, u, y, pc, s);
+        case 5: return apply_n<5>(a, fp32, u, y, pc, s);
+        case 6: return apply_n<6>(a, fp32, u, y, pc, s);
+        case 7: return apply_n<7>(a, fp32, u, y, pc, s);
         default: return cudaErrorInvalidValue;
     }
 }
 
-cudaError_t launch_ipdg_apply(const IpdgArgs& a, bool fp32, const double* u, double* y, double* part, int G,
-                              cudaStream_t s) {
-    return apply_dispatch(a, fp32, u, y, part, G, nullptr, s);
+cudaError_t launch_ipdg_apply(const IpdgArgs& a, bool fp32, const double* u, double* y, cudaStream_t s) {
+    ApplyPcg pc{nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+    return apply_dispatch(a, fp32, u, y, pc, s);
+}
+
+int pcg_max_grid(int K, int N, int sms) {
+    (void)K;
+    (void)N;
+    return std::max(8 * sms, 1024);  // element kernels: up to 8 CTAs per SM; apply: 4; learned kernel: 608
 }
 
 cudaError_t launch_ipdg_diag(const IpdgArgs& a, double* blocks, cudaStream_t s) {
@@ -486,25 +634,83 @@ cudaError_t launch_invert_blocks(double* blocks, float* blocks32, int K, int Np,
     return cudaGetLastError();
 }
 
-// element-aligned CTA size: whole elements of Np rows, rounded up to full
-// warps (the extra lanes idle but take part in the warp reductions)
-static int rows_block(int Np) {
-    int eb = 256 / Np;
-    if (eb < 1) eb = 1;
-    return (eb * Np + 31) / 32 * 32;
+// element-aligned launches, dispatched on the order
+#define ROWS_DISPATCH(Np_, CALL)                         \
+    switch (Np_) {                                       \
+        case 3: { constexpr int NP = 3; CALL; } break;   \
+        case 6: { constexpr int NP = 6; CALL; } break;   \
+        case 10: { constexpr int NP = 10; CALL; } break; \
+        case 15: { constexpr int NP = 15; CALL; } break; \
+        case 21: { constexpr int NP = 21; CALL; } break; \
+        case 28: { constexpr int NP = 28; CALL; } break; \
+        case 36: { constexpr int NP = 36; CALL; } break; \
+        default: return cudaErrorInvalidValue;           \
+    }
+
+template <int NP>
+static int rows_grid(const IpdgArgs& a) {
+    const int ngroups = (a.K + RowDims<NP>::EB - 1) / RowDims<NP>::EB;
+    return std::max(1, std::min(ngroups, 8 * a.sms));  // 256 threads x 32 registers: 8 CTAs per SM
 }
 
-cudaError_t launch_pcg_init(const IpdgArgs& a, const PcgVecs& v, cudaStream_t s) {
-    pcg_init_kernel<<<v.G, rows_block(a.Np), 0, s>>>(v, a.K, a.Np);
+template <int NP>
+static size_t grouped_size(int K) {
+    const size_t ngroups = (K + RowDims<NP>::EB - 1) / RowDims<NP>::EB;
+    return ngroups * NP * RowDims<NP>::EB * NP;
+}
+
+size_t grouped_blocks_size(int K, int Np) {
+    switch (Np) {
+        case 3: return grouped_size<3>(K);
+        case 6: return grouped_size<6>(K);
+        case 10: return grouped_size<10>(K);
+        case 15: return grouped_size<15>(K);
+        case 21: return grouped_size<21>(K);
+        case 28: return grouped_size<28>(K);
+        case 36: return grouped_size<36>(K);
+        default: return 0;
+    }
+}
+
+cudaError_t launch_group_blocks(const IpdgArgs& a, const double* blocks, double* P64, float* P32, cudaStream_t s) {
+    ROWS_DISPATCH(a.Np, (group_blocks_kernel<NP><<<4 * a.sms, 256, 0, s>>>(blocks, P64, P32, a.K)));
     return cudaGetLastError();
 }
 
-cudaError_t launch_pcg_iteration(const IpdgArgs& a, const PcgVecs& v, bool fp32, int parity, cudaStream_t s) {
-    cudaError_t e = apply_dispatch(a, fp32, v.p, v.Ap, v.part_pap, v.G, &v.S->done, s);
+// mode 0 init, 1 refresh; learned mode adds the learned kernel
+static cudaError_t pcg_precondition(const IpdgArgs& a, const PcgVecs& v, const LpcNet* lpc, const LpcFeatArgs* fa,
+                                    int mode, cudaStream_t s) {
+    ROWS_DISPATCH(a.Np, (pcg_init_kernel<NP><<<rows_grid<NP>(a), RowDims<NP>::THREADS, 0, s>>>(v, a.K, mode)));
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess || !v.zb) return e;
+    return launch_lpc_precond(*lpc, *fa, v.r, v.z, mode == 0 ? LPC_PCG_INIT : LPC_PCG_REFRESH, v.S, v.part, v.dz,
+                              s);
+}
+
+cudaError_t launch_pcg_init(const IpdgArgs& a, const PcgVecs& v, const LpcNet* lpc, const LpcFeatArgs* fa,
+                            cudaStream_t s) {
+    return pcg_precondition(a, v, lpc, fa, 0, s);
+}
+
+cudaError_t launch_pcg_refresh(const IpdgArgs& a, const PcgVecs& v, const LpcNet* lpc, const LpcFeatArgs* fa,
+                               cudaStream_t s) {
+    return pcg_precondition(a, v, lpc, fa, 1, s);
+}
+
+cudaError_t launch_pcg_iteration(const IpdgArgs& a, const PcgVecs& v, bool fp32, int parity, const LpcNet* lpc,
+                                 const LpcFeatArgs* fa, cudaStream_t s) {
+    ApplyPcg pc{v.p[parity], v.p[parity ^ 1], v.S, v.part, v.dz, v.dp[parity], v.dp[parity ^ 1]};
+    cudaError_t e = apply_dispatch(a, fp32, v.z, v.Ap, pc, s);
     if (e != cudaSuccess) return e;
-    pcg_update_kernel<<<v.G, rows_block(a.Np), 0, s>>>(v, a.K, a.Np, parity);
+    ROWS_DISPATCH(a.Np,
+                  (pcg_update_kernel<NP><<<rows_grid<NP>(a), RowDims<NP>::THREADS, 0, s>>>(v, a.K, parity)));
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
-    pcg_pupdate_kernel<<<v.G, 256, 0, s>>>(v, (size_t)a.K * a.Np, parity);
+    if (v.zb) e = launch_lpc_precond(*lpc, *fa, v.r, v.z, LPC_PCG_ITERATION, v.S, v.part, v.dz, s);
+    return e;
+}
+
+cudaError_t launch_bj(const IpdgArgs& a, const float* P32, const double* r, double* z, cudaStream_t s) {
+    ROWS_DISPATCH(a.Np, (bj_kernel<NP><<<rows_grid<NP>(a), RowDims<NP>::THREADS, 0, s>>>(P32, r, z, a.K)));
     return cudaGetLastError();
 }
 

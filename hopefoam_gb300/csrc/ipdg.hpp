@@ -5,46 +5,91 @@
 
 namespace dgk {
 
+// reference operators in the arithmetic type of the apply (ring order)
+template <typename T>
+struct IpdgOps {
+    const T* Srr;   // Np x Np reference stiffness parts (symmetric)
+    const T* Srs2;
+    const T* Sss;
+    const T* Drf;   // [3 Nfq][Np]: d/dr of the nodal basis at face f's Gauss points
+    const T* Dsf;
+    const T* DrfT;  // [Np][3 Nfq] (transposed copies for the per-Gauss-point threads)
+    const T* DsfT;
+    const T* If;    // Nfq x Nfp
+    const T* fw;    // Nfq face Gauss weights
+    const T* fc;    // K x 3 x 6 per element face:
+                    //   [n.grad r, n.grad s, n.grad r of the neighbour, n.grad s of the neighbour, tau/2, sJ]
+    const T* vc;    // K x 3 volume coefficients J (rx^2+ry^2), J (rx sx+ry sy), J (sx^2+sy^2)
+};
+
 struct IpdgArgs {
     int K, N, Np, Nfp, Nfq;
+    int sms;             // SMs of the device (persistent grids)
     double tau_coef;
     const double* geo;   // K x 4 metrics
     const double* J;     // K Jacobians
     const int* conn;     // K x 3 packed neighbours
-    const double* Srr;   // Np x Np reference stiffness parts (ring order)
-    const double* Srs2;
-    const double* Sss;
-    const double* Drf;   // 3 x Nfq x Np: d/dr of the nodal basis at face f's Gauss points
-    const double* Dsf;
-    const double* If;    // Nfq x Nfp
-    const double* fw;    // Nfq face Gauss weights
+    IpdgOps<double> o64;
+    IpdgOps<float> o32;
 };
 
+constexpr int kFaceCoef = 6;
+
+// device-side CG state; the kernels read and update it, the host reads it
+// every few iterations
 struct PcgScalars {
-    double bb;      // ||b||^2 of the current (inner) system
+    double bb;      // ||b||^2
     double tol2;    // stop when r.r <= tol2
+    double rz;      // r.z of the current residual
+    double pap;     // p.Ap of the current search direction
+    double alpha;   // rz / pap
+    double beta;    // next p = z + beta p (0: restart from z)
+    double rr;      // recurrence residual r.r
     int done;       // 1 converged, 2 breakdown / non-finite
     int it;         // iterations taken
+    unsigned int counter;  // arrival counter of the grid-wide sums
 };
 
 struct PcgVecs {
-    double *x, *r, *z, *p, *Ap;  // ring-order FP64 vectors of length K*Np
-    double *part_pap;            // [G]
-    double *part_rz;             // [2][G]
-    double *part_rr;             // [G]
-    double *part_rzo;            // [G] r_new . z_old (flexible beta)
-    const float* P32;            // block-Jacobi inverse blocks (FP32), K x Np x Np
-    const double* P64;           // FP64 blocks; used instead of P32 when set
+    double *x, *r, *z, *Ap;      // ring-order FP64 vectors of length K*Np
+    double* p[2];                // search directions, ping-pong (iteration j reads p[j&1], writes p[(j+1)&1])
+    double* part;                // [3][nmax] per-CTA partial sums
+    int nmax;                    // largest grid of any PCG kernel
+    const float* P32;            // block-Jacobi inverse blocks (FP32), grouped layout
+    const double* P64;           // FP64 blocks (grouped); used instead of P32 when set
+    double* zb;                  // learned mode: block-Jacobi output (z holds the learned one)
     PcgScalars* S;
-    int G;                       // grid of the reduction kernels
+    // FP32 offset mirrors (value minus the element's first-node value) of z
+    // and of the search directions (ping-pong like p); null: the apply stages
+    // from the FP64 vectors
+    float* dz;
+    float* dp[2];
 };
 
-cudaError_t launch_ipdg_apply(const IpdgArgs& a, bool fp32, const double* u, double* y, double* part, int G,
-                              cudaStream_t s);
+// largest grid of the PCG kernels (sizes the partials)
+int pcg_max_grid(int K, int N, int sms);
+// grouped inverse-block layout of the element-aligned kernels: element count
+// of the padded storage, and the conversion from row-major blocks
+size_t grouped_blocks_size(int K, int Np);
+cudaError_t launch_group_blocks(const IpdgArgs& a, const double* blocks, double* P64, float* P32, cudaStream_t s);
+
+// y = S u (standalone)
+cudaError_t launch_ipdg_apply(const IpdgArgs& a, bool fp32, const double* u, double* y, cudaStream_t s);
 cudaError_t launch_ipdg_diag(const IpdgArgs& a, double* blocks, cudaStream_t s);
 cudaError_t launch_invert_blocks(double* blocks, float* blocks32, int K, int Np, int* status, cudaStream_t s);
-cudaError_t launch_pcg_init(const IpdgArgs& a, const PcgVecs& v, cudaStream_t s);
-cudaError_t launch_pcg_iteration(const IpdgArgs& a, const PcgVecs& v, bool fp32, int parity, cudaStream_t s);
+struct LpcNet;
+struct LpcFeatArgs;
+// lpc / fa may be null (block-Jacobi only).  init: z = M r, S->rz, S->rr, beta = 0
+cudaError_t launch_pcg_init(const IpdgArgs& a, const PcgVecs& v, const LpcNet* lpc, const LpcFeatArgs* fa,
+                            cudaStream_t s);
+// one iteration: p_new = z + beta p_old fused into Ap = S p_new (alpha on the
+// device), then x, r, z updates with beta and the stop test on the device
+cudaError_t launch_pcg_iteration(const IpdgArgs& a, const PcgVecs& v, bool fp32, int parity, const LpcNet* lpc,
+                                 const LpcFeatArgs* fa, cudaStream_t s);
+// residual replacement: z = M r, S->rz (and S->rr) from the current r; beta kept
+cudaError_t launch_pcg_refresh(const IpdgArgs& a, const PcgVecs& v, const LpcNet* lpc, const LpcFeatArgs* fa,
+                               cudaStream_t s);
+cudaError_t launch_bj(const IpdgArgs& a, const float* P32, const double* r, double* z, cudaStream_t s);
 cudaError_t launch_dot(const double* x, const double* y, size_t n, double* part, int G, cudaStream_t s);
 cudaError_t launch_reduce_to(const double* part, int G, double* out, cudaStream_t s);
 cudaError_t launch_axpy(double* y, const double* x, double alpha, size_t n, cudaStream_t s);      // y += alpha x

@@ -7,7 +7,11 @@
 
 #include "../../include/dgcu.h"
 #include "dg_ctx.hpp"
+#include "euler_flux.cuh"
 #include "ipdg.hpp"
+#include "lpc.hpp"
+
+#include <random>
 
 using namespace dgk;
 
@@ -16,17 +20,39 @@ struct IpdgState {
     double tau_coef = 20.0;
     IpdgArgs args;
     std::vector<void*> allocs;
-    double *d_J = nullptr, *d_Srr = nullptr, *d_Srs2 = nullptr, *d_Sss = nullptr, *d_Drf = nullptr, *d_Dsf = nullptr,
-           *d_fw = nullptr;
-    double* d_blocks = nullptr;  // FP64 inverse diagonal blocks
-    float* d_blocks32 = nullptr;
+    double* d_J = nullptr;
+    IpdgOps<double> o64h{};  // device pointers of the operator tables
+    IpdgOps<float> o32h{};
+    double* d_blocks = nullptr;  // FP64 inverse diagonal blocks (row-major per element)
+    double* d_P64 = nullptr;     // the same, grouped layout of the element-aligned kernels
+    float* d_P32 = nullptr;      // FP32 copy, grouped
     // solver vectors (ring order)
-    double *d_b = nullptr, *d_x = nullptr, *d_e = nullptr, *d_r = nullptr, *d_z = nullptr, *d_p = nullptr,
+    double *d_b = nullptr, *d_x = nullptr, *d_r = nullptr, *d_z = nullptr, *d_p = nullptr, *d_p2 = nullptr,
            *d_Ap = nullptr, *d_part = nullptr;
+    double* d_ppart = nullptr;  // [3][nmax] partials of the PCG grid-wide sums
+    float *d_dz = nullptr, *d_dp = nullptr, *d_dp2 = nullptr;  // FP32 offset mirrors of z and p
+    int nmax = 0;
+    int sms = 1;
     PcgScalars* d_S = nullptr;
     double* d_scal = nullptr;  // small FP64 results (dot products)
     int* d_status = nullptr;
     int G = 608;
+    // learned preconditioner
+    bool lpc_ready = false;
+    int F = 0, H = 128;
+    float *d_W1 = nullptr, *d_W2 = nullptr, *d_m1 = nullptr, *d_v1 = nullptr, *d_m2 = nullptr, *d_v2 = nullptr;
+    float *d_g1 = nullptr, *d_g2 = nullptr;
+    __nv_bfloat16 *d_W1b = nullptr, *d_W2b = nullptr;
+    int* d_perm = nullptr;
+    double* d_zb = nullptr;
+    float* d_sc = nullptr;  // per-element feature scale
+    __nv_bfloat16* d_X = nullptr;  // features of the current residual (K x F)
+    float *d_Hs = nullptr, *d_y = nullptr, *d_dY = nullptr;  // hidden (+ its gradient), output, output gradient
+    double *d_zt = nullptr, *d_w = nullptr;  // preconditioner output z and S z during training
+    double* d_lpart = nullptr;               // [5][G] partial sums of the training losses
+    double* d_R = nullptr;                   // stored training residuals (ring order, r.P r = 1)
+    size_t cap = 0, count = 0;
+    int adam_step = 0;
 };
 
 namespace {
@@ -63,7 +89,7 @@ int iupload(dg_ctx* c, IpdgState* s, T** p, const std::vector<T>& h) {
 // y = S x (FP64) on ring-order device vectors
 int apply64(dg_ctx* c, const double* x, double* y) {
     IpdgState* s = c->ipdg;
-    cudaError_t e = launch_ipdg_apply(s->args, false, x, y, nullptr, s->G, c->stream);
+    cudaError_t e = launch_ipdg_apply(s->args, false, x, y, c->stream);
     if (e != cudaSuccess) return ifail(c, DG_ERR_CUDA, std::string("ipdg apply: ") + cudaGetErrorString(e));
     return DG_OK;
 }
@@ -80,26 +106,82 @@ int dot_host(dg_ctx* c, const double* x, const double* y, double* out) {
 
 // runs PCG iterations on S e = r (vectors in v) until S->done or `limit`
 // iterations; returns the iterations taken and the stop code
-int run_cg(dg_ctx* c, const PcgVecs& v, bool fp32, double tol2, int limit, int* iters, int* stop) {
+void lpc_descr(dg_ctx* c, LpcNet& net, LpcFeatArgs& fa) {
     IpdgState* s = c->ipdg;
+    net.F = s->F;
+    net.H = s->H;
+    net.Np = c->Np;
+    net.W1 = s->d_W1b;
+    net.W2 = s->d_W2b;
+    net.perm = s->d_perm;
+    fa.K = c->K;
+    fa.Np = c->Np;
+    fa.zb = s->d_zb;
+    fa.conn = c->d_conn;
+    fa.geo = c->d_geo;
+    fa.perm = s->d_perm;
+}
+
+// PCG iterations on S x = b (vectors in v, r = b - S x given) until S->done
+// or `limit` iterations.  Every `refresh` host checks (0: never) the
+// recurrence residual is replaced by the true FP64 residual b - S x (residual
+// replacement: the search direction is kept), and a convergence claim of the
+// recurrence is confirmed against the true residual; a claim that fails
+// restarts the recurrence from the true residual.
+int run_cg(dg_ctx* c, const PcgVecs& v, bool fp32, double tol2, int limit, const double* b, int refresh, int* iters,
+           int* stop) {
+    IpdgState* s = c->ipdg;
+    const size_t n = (size_t)c->K * c->Np;
     PcgScalars h;
     memset(&h, 0, sizeof(h));
     h.tol2 = tol2;
+    LpcNet net;
+    LpcFeatArgs fa;
+    const LpcNet* pnet = nullptr;
+    const LpcFeatArgs* pfa = nullptr;
+    if (v.zb) {
+        lpc_descr(c, net, fa);
+        pnet = &net;
+        pfa = &fa;
+    }
     IP_CUDA(c, cudaMemcpyAsync(s->d_S, &h, sizeof(h), cudaMemcpyHostToDevice, c->stream));
-    IP_CUDA(c, launch_pcg_init(s->args, v, c->stream));
+    IP_CUDA(c, launch_pcg_init(s->args, v, pnet, pfa, c->stream));
     const int CHECK = 16;
-    int issued = 0;
+    int checks = 0;
     *stop = 0;
     *iters = 0;
-    while (issued < limit) {
-        const int batch = std::min(CHECK, limit - issued);
+    while (h.it < limit) {
+        const int batch = std::min(CHECK, limit - h.it);
         for (int j = 0; j < batch; j++) {
-            IP_CUDA(c, launch_pcg_iteration(s->args, v, fp32, (issued + j) & 1, c->stream));
+            IP_CUDA(c, launch_pcg_iteration(s->args, v, fp32, (h.it + j) & 1, pnet, pfa, c->stream));
         }
-        issued += batch;
         IP_CUDA(c, cudaMemcpyAsync(&h, s->d_S, sizeof(h), cudaMemcpyDeviceToHost, c->stream));
         IP_CUDA(c, cudaStreamSynchronize(c->stream));
-        if (h.done) break;
+        checks++;
+        if (h.done == 2) break;
+        const bool claim = h.done == 1;
+        const bool periodic = refresh > 0 && checks % refresh == 0;
+        if (!b || (!claim && !periodic)) {
+            if (claim) break;
+            continue;
+        }
+        // true residual into r (Ap is scratch here: the next iteration recomputes it)
+        int rc = apply64(c, v.x, v.Ap);
+        if (rc) return rc;
+        IP_CUDA(c, launch_xmy(v.r, b, v.Ap, n, c->stream));
+        if (claim) {
+            double rr = 0;
+            rc = dot_host(c, v.r, v.r, &rr);
+            if (rc) return rc;
+            if (rr <= tol2) break;
+            // the recurrence drifted: restart from the true residual (p = z)
+            h.done = 0;
+            const int zero = 0;
+            const double zbeta = 0.0;
+            IP_CUDA(c, cudaMemcpyAsync(&s->d_S->done, &zero, sizeof(int), cudaMemcpyHostToDevice, c->stream));
+            IP_CUDA(c, cudaMemcpyAsync(&s->d_S->beta, &zbeta, sizeof(double), cudaMemcpyHostToDevice, c->stream));
+        }
+        IP_CUDA(c, launch_pcg_refresh(s->args, v, pnet, pfa, c->stream));
     }
     *iters = h.it;
     *stop = h.done;
@@ -107,6 +189,33 @@ int run_cg(dg_ctx* c, const PcgVecs& v, bool fp32, double tol2, int limit, int* 
 }
 
 }  // namespace
+
+// node permutation (ring order) that rotates a neighbour's face fn onto face 0
+std::vector<int> rotation_perms(const dgb::RefOps& o) {
+    const int Np = o.Np;
+    std::vector<int> perm(3 * Np, -1);
+    auto bary = [&](int p, double* l) {
+        const double r = o.r[o.ring[p]], t = o.s[o.ring[p]];
+        l[0] = -(r + t) / 2;
+        l[1] = (1 + r) / 2;
+        l[2] = (1 + t) / 2;
+    };
+    for (int fn = 0; fn < 3; fn++)
+        for (int i = 0; i < Np; i++) {
+            double mu[3], want[3];
+            bary(i, mu);
+            for (int m = 0; m < 3; m++) want[(fn + m) % 3] = mu[m];
+            for (int j = 0; j < Np; j++) {
+                double l[3];
+                bary(j, l);
+                if (std::fabs(l[0] - want[0]) + std::fabs(l[1] - want[1]) + std::fabs(l[2] - want[2]) < 1e-9) {
+                    perm[fn * Np + i] = j;
+                    break;
+                }
+            }
+        }
+    return perm;
+}
 
 void ipdg_teardown(dg_ctx* c) {
     if (!c->ipdg) return;
@@ -157,28 +266,92 @@ int dg_ipdg_setup(dg_ctx* c, double tau_coef) {
                 Drf[((size_t)f * Nfq + g) * Np + p] = a;
                 Dsf[((size_t)f * Nfq + g) * Np + p] = b;
             }
-    std::vector<double> J(K);
+    const int NF = 3 * Nfq;
+    std::vector<double> DrfT((size_t)Np * NF), DsfT((size_t)Np * NF);
+    for (int fg = 0; fg < NF; fg++)
+        for (int p = 0; p < Np; p++) {
+            DrfT[(size_t)p * NF + fg] = Drf[(size_t)fg * Np + p];
+            DsfT[(size_t)p * NF + fg] = Dsf[(size_t)fg * Np + p];
+        }
+    std::vector<double> J(K), vc((size_t)K * 3), fc((size_t)K * 3 * kFaceCoef);
+    const double tau0 = tau_coef * (c->N + 1) * (c->N + 1);
     for (int k = 0; k < K; k++) {
         const double* g = &c->geo_host[4 * (size_t)k];
-        J[k] = 1.0 / (g[0] * g[3] - g[1] * g[2]);
+        const double rx = g[0], sx = g[1], ry = g[2], sy = g[3];
+        J[k] = 1.0 / (rx * sy - sx * ry);
+        vc[3 * (size_t)k] = J[k] * (rx * rx + ry * ry);
+        vc[3 * (size_t)k + 1] = J[k] * (rx * sx + ry * sy);
+        vc[3 * (size_t)k + 2] = J[k] * (sx * sx + sy * sy);
+        for (int f = 0; f < 3; f++) {
+            double nx, ny, fsc;
+            face_normal(f, rx, sx, ry, sy, nx, ny, fsc);
+            double* out = &fc[((size_t)k * 3 + f) * kFaceCoef];
+            out[0] = nx * rx + ny * ry;
+            out[1] = nx * sx + ny * sy;
+            out[2] = out[3] = 0.0;
+            double fmx = fsc;
+            const int cn = c->conn_host[(size_t)k * 3 + f];
+            if (cn >= 0) {
+                const int nb = cn >> 3, fn = cn & 3;
+                const double* gn = &c->geo_host[4 * (size_t)nb];
+                double nx2, ny2, fsc2;
+                face_normal(fn, gn[0], gn[1], gn[2], gn[3], nx2, ny2, fsc2);
+                fmx = std::max(fsc, fsc2);
+                out[2] = nx * gn[0] + ny * gn[2];
+                out[3] = nx * gn[1] + ny * gn[3];
+            }
+            out[4] = 0.5 * tau0 * fmx;
+            out[5] = fsc * J[k];
+        }
     }
+    std::vector<double> Ifh(o.If.begin(), o.If.end());
+    auto f32 = [](const std::vector<double>& v) { return std::vector<float>(v.begin(), v.end()); };
     int rc = 0;
+    IpdgOps<double>& o64 = s->o64h;
+    IpdgOps<float>& o32 = s->o32h;
     rc |= iupload(c, s, &s->d_J, J);
-    rc |= iupload(c, s, &s->d_Srr, Srr);
-    rc |= iupload(c, s, &s->d_Srs2, Srs2);
-    rc |= iupload(c, s, &s->d_Sss, Sss);
-    rc |= iupload(c, s, &s->d_Drf, Drf);
-    rc |= iupload(c, s, &s->d_Dsf, Dsf);
-    rc |= iupload(c, s, &s->d_fw, o.fw);
+    rc |= iupload(c, s, (double**)&o64.Srr, Srr);
+    rc |= iupload(c, s, (double**)&o64.Srs2, Srs2);
+    rc |= iupload(c, s, (double**)&o64.Sss, Sss);
+    rc |= iupload(c, s, (double**)&o64.Drf, Drf);
+    rc |= iupload(c, s, (double**)&o64.Dsf, Dsf);
+    rc |= iupload(c, s, (double**)&o64.DrfT, DrfT);
+    rc |= iupload(c, s, (double**)&o64.DsfT, DsfT);
+    rc |= iupload(c, s, (double**)&o64.If, Ifh);
+    rc |= iupload(c, s, (double**)&o64.fw, o.fw);
+    rc |= iupload(c, s, (double**)&o64.fc, fc);
+    rc |= iupload(c, s, (double**)&o64.vc, vc);
+    rc |= iupload(c, s, (float**)&o32.Srr, f32(Srr));
+    rc |= iupload(c, s, (float**)&o32.Srs2, f32(Srs2));
+    rc |= iupload(c, s, (float**)&o32.Sss, f32(Sss));
+    rc |= iupload(c, s, (float**)&o32.Drf, f32(Drf));
+    rc |= iupload(c, s, (float**)&o32.Dsf, f32(Dsf));
+    rc |= iupload(c, s, (float**)&o32.DrfT, f32(DrfT));
+    rc |= iupload(c, s, (float**)&o32.DsfT, f32(DsfT));
+    rc |= iupload(c, s, (float**)&o32.If, f32(Ifh));
+    rc |= iupload(c, s, (float**)&o32.fw, f32(o.fw));
+    rc |= iupload(c, s, (float**)&o32.fc, f32(fc));
+    rc |= iupload(c, s, (float**)&o32.vc, f32(vc));
     const size_t n = (size_t)K * Np;
     rc |= ialloc(c, s, &s->d_blocks, n * Np);
-    rc |= ialloc(c, s, &s->d_blocks32, n * Np);
+    const size_t ng = grouped_blocks_size(K, Np);
+    rc |= ialloc(c, s, &s->d_P64, ng);
+    rc |= ialloc(c, s, &s->d_P32, ng);
     rc |= ialloc(c, s, &s->d_b, n);
     rc |= ialloc(c, s, &s->d_x, n);
-    rc |= ialloc(c, s, &s->d_e, n);
     rc |= ialloc(c, s, &s->d_r, n);
     rc |= ialloc(c, s, &s->d_z, n);
     rc |= ialloc(c, s, &s->d_p, n);
+    rc |= ialloc(c, s, &s->d_p2, n);
+    rc |= ialloc(c, s, &s->d_dz, n);
+    rc |= ialloc(c, s, &s->d_dp, n);
+    rc |= ialloc(c, s, &s->d_dp2, n);
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    s->sms = sms > 0 ? sms : 1;
+    s->nmax = pcg_max_grid(K, c->N, s->sms);
+    rc |= ialloc(c, s, &s->d_ppart, (size_t)3 * s->nmax);
     rc |= ialloc(c, s, &s->d_Ap, n);
     rc |= ialloc(c, s, &s->d_part, (size_t)5 * s->G);
     rc |= ialloc(c, s, &s->d_S, 1);
@@ -195,16 +368,13 @@ int dg_ipdg_setup(dg_ctx* c, double tau_coef) {
     a.geo = c->d_geo;
     a.J = s->d_J;
     a.conn = c->d_conn;
-    a.Srr = s->d_Srr;
-    a.Srs2 = s->d_Srs2;
-    a.Sss = s->d_Sss;
-    a.Drf = s->d_Drf;
-    a.Dsf = s->d_Dsf;
-    a.If = c->d_If;
-    a.fw = s->d_fw;
+    a.sms = s->sms;
+    a.o64 = o64;
+    a.o32 = o32;
     IP_CUDA(c, cudaMemsetAsync(s->d_status, 0, sizeof(int), c->stream));
     IP_CUDA(c, launch_ipdg_diag(a, s->d_blocks, c->stream));
-    IP_CUDA(c, launch_invert_blocks(s->d_blocks, s->d_blocks32, K, Np, s->d_status, c->stream));
+    IP_CUDA(c, launch_invert_blocks(s->d_blocks, nullptr, K, Np, s->d_status, c->stream));
+    IP_CUDA(c, launch_group_blocks(a, s->d_blocks, s->d_P64, s->d_P32, c->stream));
     int st = 0;
     IP_CUDA(c, cudaMemcpyAsync(&st, s->d_status, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
     IP_CUDA(c, cudaStreamSynchronize(c->stream));
@@ -232,7 +402,10 @@ int dg_pcg_solve(dg_ctx* c, const double* b_host, double* x_host, double rtol, i
                  dg_solve_stats* stats) {
     if (!c || !b_host || !x_host || !(rtol > 0) || maxit < 1) return DG_ERR_ARG;
     if (!c->ipdg || !c->ipdg->ready) return ifail(c, DG_ERR_ARG, "dg_ipdg_setup not called");
-    if (pc != DG_PC_BLOCK_JACOBI) return ifail(c, DG_ERR_UNSUPPORTED, "preconditioner not available");
+    if (pc != DG_PC_BLOCK_JACOBI && pc != DG_PC_LEARNED && pc != DG_PC_LEARNED_ONLY)
+        return ifail(c, DG_ERR_ARG, "unknown preconditioner");
+    const bool learned = pc == DG_PC_LEARNED || pc == DG_PC_LEARNED_ONLY;
+    if (learned && !c->ipdg->lpc_ready) return ifail(c, DG_ERR_ARG, "dg_lpc_setup not called");
     if (precision != DG_PREC_FP64 && precision != DG_PREC_SPLIT) return ifail(c, DG_ERR_ARG, "unknown precision");
     IpdgState* s = c->ipdg;
     const size_t n = (size_t)c->K * c->Np;
@@ -250,16 +423,19 @@ int dg_pcg_solve(dg_ctx* c, const double* b_host, double* x_host, double rtol, i
     PcgVecs v;
     v.r = s->d_r;
     v.z = s->d_z;
-    v.p = s->d_p;
+    v.p[0] = s->d_p;
+    v.p[1] = s->d_p2;
     v.Ap = s->d_Ap;
-    v.part_pap = s->d_part;
-    v.part_rz = s->d_part + s->G;  // [2][G]
-    v.part_rr = s->d_part + 3 * s->G;
-    v.part_rzo = s->d_part + 4 * s->G;
-    v.P32 = s->d_blocks32;
+    v.part = s->d_ppart;
+    v.nmax = s->nmax;
+    v.P32 = s->d_P32;
     v.P64 = nullptr;
+    v.zb = learned ? s->d_zb : nullptr;
     v.S = s->d_S;
-    v.G = s->G;
+    const bool mirrors = precision == DG_PREC_SPLIT;  // the FP32 apply stages from FP32 offset mirrors
+    v.dz = mirrors ? s->d_dz : nullptr;
+    v.dp[0] = mirrors ? s->d_dp : nullptr;
+    v.dp[1] = mirrors ? s->d_dp2 : nullptr;
     int total_it = 0, stop = 0;
     double rel = 0;
     if (bb == 0.0) {
@@ -270,30 +446,19 @@ int dg_pcg_solve(dg_ctx* c, const double* b_host, double* x_host, double rtol, i
         if (rc) return rc;
         IP_CUDA(c, launch_xmy(s->d_r, s->d_b, s->d_Ap, n, c->stream));
         v.x = s->d_x;
-        v.P64 = s->d_blocks;  // FP64 preconditioner: an inexact one stalls CG at high condition numbers
-        rc = run_cg(c, v, false, rtol * rtol * bb, maxit, &total_it, &stop);
+        if (!v.zb) v.P64 = s->d_P64;  // FP64 preconditioner: an inexact one stalls CG at high condition numbers
+        rc = run_cg(c, v, false, rtol * rtol * bb, maxit, s->d_b, 0, &total_it, &stop);
         if (rc) return rc;
     } else {
-        // mixed-precision refinement: FP32-arithmetic operator inside CG, FP64 outer residual
-        for (int outer = 0; outer < 20 && total_it < maxit; outer++) {
-            rc = apply64(c, s->d_x, s->d_Ap);
-            if (rc) return rc;
-            IP_CUDA(c, launch_xmy(s->d_r, s->d_b, s->d_Ap, n, c->stream));
-            double rr = 0;
-            rc = dot_host(c, s->d_r, s->d_r, &rr);
-            if (rc) return rc;
-            if (!(rr == rr)) { stop = 2; break; }
-            if (rr <= rtol * rtol * bb) { stop = 1; break; }
-            IP_CUDA(c, cudaMemsetAsync(s->d_e, 0, n * sizeof(double), c->stream));
-            v.x = s->d_e;
-            const double tol2 = std::max(0.25 * rtol * rtol * bb, 1e-12 * rr);
-            int it = 0, st = 0;
-            rc = run_cg(c, v, true, tol2, maxit - total_it, &it, &st);
-            if (rc) return rc;
-            total_it += it;
-            if (st == 2) { stop = 2; break; }
-            IP_CUDA(c, launch_axpy(s->d_x, s->d_e, 1.0, n, c->stream));
-        }
+        // FP32-arithmetic operator inside CG with FP64 vectors and recurrences;
+        // the recurrence residual is replaced by the true FP64 residual every
+        // 64 iterations
+        rc = apply64(c, s->d_x, s->d_Ap);
+        if (rc) return rc;
+        IP_CUDA(c, launch_xmy(s->d_r, s->d_b, s->d_Ap, n, c->stream));
+        v.x = s->d_x;
+        rc = run_cg(c, v, true, rtol * rtol * bb, maxit, s->d_b, 4, &total_it, &stop);
+        if (rc) return rc;
     }
     // true FP64 residual
     rc = apply64(c, s->d_x, s->d_Ap);
@@ -303,6 +468,15 @@ int dg_pcg_solve(dg_ctx* c, const double* b_host, double* x_host, double rtol, i
     rc = dot_host(c, s->d_r, s->d_r, &rr);
     if (rc) return rc;
     cudaEventRecord(e1, c->stream);
+    rel = bb > 0 ? std::sqrt(rr / bb) : 0.0;
+    if (pc == DG_PC_LEARNED && (!(rel == rel) || stop == 2 || rel > rtol)) {
+        // block-Jacobi PCG is the fallback: solve again from the caller's x0
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        int rc2 = dg_pcg_solve(c, b_host, x_host, rtol, maxit, DG_PC_BLOCK_JACOBI, precision, stats);
+        if (stats) stats->iterations = -stats->iterations;  // negative: the learned solve fell back
+        return rc2;
+    }
     IP_CUDA(c, launch_permute(s->d_x, s->d_z, c->d_ring, c->K, c->Np, false, c->stream));
     IP_CUDA(c, cudaMemcpyAsync(x_host, s->d_z, n * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
     IP_CUDA(c, cudaStreamSynchronize(c->stream));
@@ -318,6 +492,375 @@ int dg_pcg_solve(dg_ctx* c, const double* b_host, double* x_host, double rtol, i
     }
     if (!(rel == rel) || stop == 2) return ifail(c, DG_ERR_NONFINITE, "PCG breakdown or non-finite residual");
     if (rel > rtol) return ifail(c, DG_ERR_NOT_CONVERGED, "PCG reached the iteration limit");
+    return DG_OK;
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// learned preconditioner
+//
+// Training objective (self-supervised, over whole residual vectors r of the
+// method's own PCG iterates): the energy loss of one preconditioned step
+// with the optimal step length,
+//     L(r) = -(r.z)^2 / (z.S z),   z = M(r) = P r + s W2 relu(W1 x),
+// which is -1/2 of the largest decrease of the S-norm of the error along z
+// (-(r.P r)^2 / (P r.S P r) for block Jacobi alone).  dL/dz is proportional
+// to (a/b) S z - r (a = r.z, b = z.S z): one SIPG apply per step, then the
+// hand-written backward kernels.  Residuals are scaled to r.P r = 1 when
+// they are stored, so every residual weighs the same.
+
+namespace {
+
+__global__ void f32_to_bf16_kernel(const float* in, __nv_bfloat16* out, long long n) {
+    for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x)
+        out[t] = __float2bfloat16(in[t]);
+}
+
+__global__ void scale_kernel(double* x, const double* part, int G, size_t n) {
+    __shared__ double s_f;
+    if (threadIdx.x < 32) {
+        double a = 0;
+        for (int i = threadIdx.x; i < G; i += 32) a += part[i];
+        for (int o = 16; o > 0; o >>= 1) a += __shfl_xor_sync(0xffffffffu, a, o);
+        if (threadIdx.x == 0) s_f = a > 0 ? rsqrt(a) : 0.0;
+    }
+    __syncthreads();
+    const double f = s_f;
+    for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < n; t += (size_t)gridDim.x * blockDim.x) x[t] *= f;
+}
+
+// forward pass of the learned preconditioner on the ring-order residual r:
+// zb = P r, features, hidden layer, z = zb + s y (into s->d_zt), w = S z
+// (FP32-arithmetic apply) and the partials of a = r.z, b = z.w
+int lpc_forward_vec(dg_ctx* c, const double* r, bool with_bj_loss) {
+    IpdgState* s = c->ipdg;
+    const int K = c->K, Np = c->Np;
+    const size_t n = (size_t)K * Np;
+    LpcNet net;
+    LpcFeatArgs fa;
+    lpc_descr(c, net, fa);
+    IP_CUDA(c, launch_bj(s->args, s->d_P32, r, s->d_zb, c->stream));
+    if (with_bj_loss) {
+        IP_CUDA(c, launch_ipdg_apply(s->args, true, s->d_zb, s->d_w, c->stream));
+        IP_CUDA(c, launch_dot(r, s->d_zb, n, s->d_lpart + 2 * s->G, s->G, c->stream));
+        IP_CUDA(c, launch_dot(s->d_zb, s->d_w, n, s->d_lpart + 3 * s->G, s->G, c->stream));
+    }
+    IP_CUDA(c, launch_lpc_features(fa, s->d_X, s->d_sc, c->stream));
+    IP_CUDA(c, launch_lpc_forward(net, s->d_X, nullptr, K, s->d_Hs, s->d_y, s->d_lpart + 4 * s->G, s->G, c->stream));
+    IP_CUDA(c, launch_lpc_combine(s->d_zb, s->d_sc, s->d_y, K, Np, s->d_zt, c->stream));
+    IP_CUDA(c, launch_ipdg_apply(s->args, true, s->d_zt, s->d_w, c->stream));
+    IP_CUDA(c, launch_dot(r, s->d_zt, n, s->d_lpart, s->G, c->stream));
+    IP_CUDA(c, launch_dot(s->d_zt, s->d_w, n, s->d_lpart + s->G, s->G, c->stream));
+    return DG_OK;
+}
+
+// gradients of L(r) into s->d_g1 / d_g2
+int lpc_backward_vec(dg_ctx* c, const double* r) {
+    IpdgState* s = c->ipdg;
+    LpcNet net;
+    LpcFeatArgs fa;
+    lpc_descr(c, net, fa);
+    IP_CUDA(c, launch_lpc_energy_dy(r, s->d_w, s->d_sc, s->d_lpart, s->d_lpart + s->G, s->G, c->K, c->Np, s->d_dY,
+                                    c->stream));
+    IP_CUDA(c, launch_lpc_backward(net, s->d_X, s->d_Hs, s->d_dY, c->K, s->d_g1, s->d_g2, c->stream));
+    return DG_OK;
+}
+
+// host value of a partial sum block
+int lpc_sum(dg_ctx* c, const double* part, double* out) {
+    IpdgState* s = c->ipdg;
+    IP_CUDA(c, launch_reduce_to(part, s->G, s->d_scal, c->stream));
+    IP_CUDA(c, cudaMemcpyAsync(out, s->d_scal, sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    IP_CUDA(c, cudaStreamSynchronize(c->stream));
+    return DG_OK;
+}
+
+int lpc_losses(dg_ctx* c, double* loss, double* loss_bj) {
+    IpdgState* s = c->ipdg;
+    double a = 0, b = 0;
+    int rc = lpc_sum(c, s->d_lpart, &a);
+    if (!rc) rc = lpc_sum(c, s->d_lpart + s->G, &b);
+    if (rc) return rc;
+    if (loss) *loss = b > 0 ? -(a * a) / b : 0.0;
+    if (loss_bj) {
+        double a0 = 0, b0 = 0;
+        rc = lpc_sum(c, s->d_lpart + 2 * s->G, &a0);
+        if (!rc) rc = lpc_sum(c, s->d_lpart + 3 * s->G, &b0);
+        if (rc) return rc;
+        *loss_bj = b0 > 0 ? -(a0 * a0) / b0 : 0.0;
+    }
+    return DG_OK;
+}
+
+int lpc_adam_step(dg_ctx* c, double lr) {
+    IpdgState* s = c->ipdg;
+    const int n1 = s->H * s->F, n2 = c->Np * s->H;
+    s->adam_step++;
+    IP_CUDA(c, launch_lpc_adam(s->d_W1, s->d_m1, s->d_v1, s->d_g1, s->d_W1b, n1, (float)lr, 0.9f, 0.999f, 1e-8f,
+                               s->adam_step, 1.f, c->stream));
+    IP_CUDA(c, launch_lpc_adam(s->d_W2, s->d_m2, s->d_v2, s->d_g2, s->d_W2b, n2, (float)lr, 0.9f, 0.999f, 1e-8f,
+                               s->adam_step, 1.f, c->stream));
+    return DG_OK;
+}
+
+// BF16 copies of the master weights (an Adam step with zero gradient and zero
+// learning rate only converts)
+int lpc_refresh_bf16(dg_ctx* c) {
+    IpdgState* s = c->ipdg;
+    const int n1 = s->H * s->F, n2 = c->Np * s->H;
+    IP_CUDA(c, cudaMemsetAsync(s->d_g1, 0, n1 * sizeof(float), c->stream));
+    IP_CUDA(c, cudaMemsetAsync(s->d_g2, 0, n2 * sizeof(float), c->stream));
+    IP_CUDA(c, launch_lpc_adam(s->d_W1, s->d_m1, s->d_v1, s->d_g1, s->d_W1b, n1, 0.f, 0.9f, 0.999f, 1e-8f, 1, 1.f,
+                               c->stream));
+    IP_CUDA(c, launch_lpc_adam(s->d_W2, s->d_m2, s->d_v2, s->d_g2, s->d_W2b, n2, 0.f, 0.9f, 0.999f, 1e-8f, 1, 1.f,
+                               c->stream));
+    return DG_OK;
+}
+
+// host residual (reference order) -> ring order into dst
+int lpc_upload_residual(dg_ctx* c, const double* r_host, double* dst) {
+    IpdgState* s = c->ipdg;
+    const size_t n = (size_t)c->K * c->Np;
+    IP_CUDA(c, cudaMemcpyAsync(s->d_z, r_host, n * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+    IP_CUDA(c, launch_permute(s->d_z, dst, c->d_ring, c->K, c->Np, true, c->stream));
+    return DG_OK;
+}
+
+bool lpc_ok(dg_ctx* c) { return c && c->ipdg && c->ipdg->lpc_ready; }
+
+}  // namespace
+
+extern "C" {
+
+int dg_lpc_setup(dg_ctx* c, int hidden, unsigned long long seed, int capacity) {
+    if (!c || hidden < 8 || hidden > 256 || capacity < 0) return DG_ERR_ARG;
+    if (!c->ipdg || !c->ipdg->ready) return ifail(c, DG_ERR_ARG, "dg_ipdg_setup not called");
+    IpdgState* s = c->ipdg;
+    if (s->lpc_ready) return ifail(c, DG_ERR_ARG, "learned preconditioner already set up");
+    const int Np = c->Np, K = c->K;
+    if (Np > 36) return ifail(c, DG_ERR_UNSUPPORTED, "learned preconditioner supports N <= 7");
+    s->H = hidden;
+    s->F = 4 * Np + 4;
+    const int n1 = s->H * s->F, n2 = Np * s->H;
+    std::mt19937_64 rng(seed);
+    std::normal_distribution<float> nd(0.f, 1.f);
+    std::vector<float> W1(n1), W2(n2);
+    for (auto& w : W1) w = nd(rng) * std::sqrt(2.0f / s->F);
+    for (auto& w : W2) w = nd(rng) * 0.01f / std::sqrt((float)s->H);
+    std::vector<int> perm = rotation_perms(c->ops);
+    for (int v : perm)
+        if (v < 0) return ifail(c, DG_ERR_ARG, "node set is not rotation symmetric");
+    const size_t n = (size_t)K * Np;
+    int rc = 0;
+    rc |= iupload(c, s, &s->d_W1, W1);
+    rc |= iupload(c, s, &s->d_W2, W2);
+    rc |= iupload(c, s, &s->d_perm, perm);
+    rc |= ialloc(c, s, &s->d_m1, n1);
+    rc |= ialloc(c, s, &s->d_v1, n1);
+    rc |= ialloc(c, s, &s->d_g1, n1);
+    rc |= ialloc(c, s, &s->d_m2, n2);
+    rc |= ialloc(c, s, &s->d_v2, n2);
+    rc |= ialloc(c, s, &s->d_g2, n2);
+    rc |= ialloc(c, s, &s->d_W1b, n1);
+    rc |= ialloc(c, s, &s->d_W2b, n2);
+    rc |= ialloc(c, s, &s->d_zb, n);
+    rc |= ialloc(c, s, &s->d_sc, (size_t)K);
+    rc |= ialloc(c, s, &s->d_X, (size_t)K * s->F);
+    rc |= ialloc(c, s, &s->d_Hs, (size_t)2 * K * s->H);
+    rc |= ialloc(c, s, &s->d_y, n);
+    rc |= ialloc(c, s, &s->d_dY, n);
+    rc |= ialloc(c, s, &s->d_zt, n);
+    rc |= ialloc(c, s, &s->d_w, n);
+    rc |= ialloc(c, s, &s->d_lpart, (size_t)5 * s->G);
+    s->cap = (size_t)capacity;
+    if (s->cap) rc |= ialloc(c, s, &s->d_R, s->cap * n);
+    if (rc) return DG_ERR_NOMEM;
+    IP_CUDA(c, cudaMemsetAsync(s->d_m1, 0, n1 * sizeof(float), c->stream));
+    IP_CUDA(c, cudaMemsetAsync(s->d_v1, 0, n1 * sizeof(float), c->stream));
+    IP_CUDA(c, cudaMemsetAsync(s->d_m2, 0, n2 * sizeof(float), c->stream));
+    IP_CUDA(c, cudaMemsetAsync(s->d_v2, 0, n2 * sizeof(float), c->stream));
+    rc = lpc_refresh_bf16(c);
+    if (rc) return rc;
+    IP_CUDA(c, cudaStreamSynchronize(c->stream));
+    s->count = 0;
+    s->adam_step = 0;
+    s->lpc_ready = true;
+    return DG_OK;
+}
+
+int dg_lpc_add_residual(dg_ctx* c, const double* r_host) {
+    if (!c || !r_host) return DG_ERR_ARG;
+    if (!lpc_ok(c)) return ifail(c, DG_ERR_ARG, "dg_lpc_setup not called");
+    IpdgState* s = c->ipdg;
+    if (s->count >= s->cap) return ifail(c, DG_ERR_ARG, "training set capacity reached");
+    const size_t n = (size_t)c->K * c->Np;
+    double* dst = s->d_R + s->count * n;
+    int rc = lpc_upload_residual(c, r_host, dst);
+    if (rc) return rc;
+    // scale to r.P r = 1
+    IP_CUDA(c, launch_bj(s->args, s->d_P32, dst, s->d_zb, c->stream));
+    IP_CUDA(c, launch_dot(dst, s->d_zb, n, s->d_lpart, s->G, c->stream));
+    double rpr = 0;
+    rc = lpc_sum(c, s->d_lpart, &rpr);
+    if (rc) return rc;
+    if (!(rpr > 0) || !std::isfinite(rpr)) return ifail(c, DG_ERR_ARG, "residual is zero or not finite");
+    scale_kernel<<<608, 256, 0, c->stream>>>(dst, s->d_lpart, s->G, n);
+    IP_CUDA(c, cudaGetLastError());
+    IP_CUDA(c, cudaStreamSynchronize(c->stream));
+    s->count++;
+    return DG_OK;
+}
+
+int dg_lpc_train(dg_ctx* c, int epochs, double lr, unsigned long long seed, double* final_loss,
+                 double* final_loss_bj) {
+    if (!c || epochs < 1 || !(lr >= 0)) return DG_ERR_ARG;
+    if (!lpc_ok(c)) return ifail(c, DG_ERR_ARG, "dg_lpc_setup not called");
+    IpdgState* s = c->ipdg;
+    if (s->count < 1) return ifail(c, DG_ERR_ARG, "no training residuals");
+    const size_t n = (size_t)c->K * c->Np;
+    std::vector<size_t> order(s->count);
+    for (size_t i = 0; i < s->count; i++) order[i] = i;
+    std::mt19937_64 rng(seed);
+    int rc = DG_OK;
+    for (int ep = 0; ep < epochs && !rc; ep++) {
+        std::shuffle(order.begin(), order.end(), rng);
+        for (size_t j = 0; j < s->count && !rc; j++) {
+            const double* r = s->d_R + order[j] * n;
+            rc = lpc_forward_vec(c, r, false);
+            if (!rc) rc = lpc_backward_vec(c, r);
+            if (!rc) rc = lpc_adam_step(c, lr);
+        }
+    }
+    if (rc) return rc;
+    // mean loss over the stored residuals (learned and block Jacobi alone)
+    double L = 0, Lbj = 0;
+    for (size_t j = 0; j < s->count && !rc; j++) {
+        double l = 0, lb = 0;
+        rc = lpc_forward_vec(c, s->d_R + j * n, true);
+        if (!rc) rc = lpc_losses(c, &l, &lb);
+        L += l;
+        Lbj += lb;
+    }
+    if (rc) return rc;
+    if (final_loss) *final_loss = L / s->count;
+    if (final_loss_bj) *final_loss_bj = Lbj / s->count;
+    if (!std::isfinite(L)) return ifail(c, DG_ERR_NONFINITE, "training diverged");
+    return DG_OK;
+}
+
+int dg_lpc_loss(dg_ctx* c, const double* r_host, double* loss, double* loss_bj) {
+    if (!c || !r_host) return DG_ERR_ARG;
+    if (!lpc_ok(c)) return ifail(c, DG_ERR_ARG, "dg_lpc_setup not called");
+    IpdgState* s = c->ipdg;
+    int rc = lpc_upload_residual(c, r_host, s->d_r);
+    if (!rc) rc = lpc_forward_vec(c, s->d_r, true);
+    if (!rc) rc = lpc_losses(c, loss, loss_bj);
+    return rc;
+}
+
+int dg_lpc_energy_gradients(dg_ctx* c, const double* r_host, float* gW1, float* gW2, double* loss) {
+    if (!c || !r_host || !gW1 || !gW2) return DG_ERR_ARG;
+    if (!lpc_ok(c)) return ifail(c, DG_ERR_ARG, "dg_lpc_setup not called");
+    IpdgState* s = c->ipdg;
+    int rc = lpc_upload_residual(c, r_host, s->d_r);
+    if (!rc) rc = lpc_forward_vec(c, s->d_r, false);
+    if (!rc) rc = lpc_backward_vec(c, s->d_r);
+    if (!rc) rc = lpc_losses(c, loss, nullptr);
+    if (rc) return rc;
+    IP_CUDA(c, cudaMemcpyAsync(gW1, s->d_g1, (size_t)s->H * s->F * sizeof(float), cudaMemcpyDeviceToHost, c->stream));
+    IP_CUDA(c, cudaMemcpyAsync(gW2, s->d_g2, (size_t)c->Np * s->H * sizeof(float), cudaMemcpyDeviceToHost, c->stream));
+    IP_CUDA(c, cudaStreamSynchronize(c->stream));
+    return DG_OK;
+}
+
+int dg_lpc_get_weights(dg_ctx* c, float* W1, float* W2) {
+    if (!c || !W1 || !W2) return DG_ERR_ARG;
+    if (!lpc_ok(c)) return ifail(c, DG_ERR_ARG, "dg_lpc_setup not called");
+    IpdgState* s = c->ipdg;
+    IP_CUDA(c, cudaMemcpyAsync(W1, s->d_W1, (size_t)s->H * s->F * sizeof(float), cudaMemcpyDeviceToHost, c->stream));
+    IP_CUDA(c, cudaMemcpyAsync(W2, s->d_W2, (size_t)c->Np * s->H * sizeof(float), cudaMemcpyDeviceToHost, c->stream));
+    IP_CUDA(c, cudaStreamSynchronize(c->stream));
+    return DG_OK;
+}
+
+int dg_lpc_set_weights(dg_ctx* c, const float* W1, const float* W2) {
+    if (!c || !W1 || !W2) return DG_ERR_ARG;
+    if (!lpc_ok(c)) return ifail(c, DG_ERR_ARG, "dg_lpc_setup not called");
+    IpdgState* s = c->ipdg;
+    const int n1 = s->H * s->F, n2 = c->Np * s->H;
+    IP_CUDA(c, cudaMemcpyAsync(s->d_W1, W1, n1 * sizeof(float), cudaMemcpyHostToDevice, c->stream));
+    IP_CUDA(c, cudaMemcpyAsync(s->d_W2, W2, n2 * sizeof(float), cudaMemcpyHostToDevice, c->stream));
+    IP_CUDA(c, cudaMemsetAsync(s->d_m1, 0, n1 * sizeof(float), c->stream));
+    IP_CUDA(c, cudaMemsetAsync(s->d_v1, 0, n1 * sizeof(float), c->stream));
+    IP_CUDA(c, cudaMemsetAsync(s->d_m2, 0, n2 * sizeof(float), c->stream));
+    IP_CUDA(c, cudaMemsetAsync(s->d_v2, 0, n2 * sizeof(float), c->stream));
+    s->adam_step = 0;
+    int rc = lpc_refresh_bf16(c);
+    if (rc) return rc;
+    IP_CUDA(c, cudaStreamSynchronize(c->stream));
+    return DG_OK;
+}
+
+int dg_lpc_gradients(dg_ctx* c, const float* X_host, const float* T_host, int B, float* gW1, float* gW2,
+                     double* loss) {
+    if (!c || !X_host || !T_host || B < 1 || !gW1 || !gW2) return DG_ERR_ARG;
+    if (!lpc_ok(c)) return ifail(c, DG_ERR_ARG, "dg_lpc_setup not called");
+    IpdgState* s = c->ipdg;
+    const int Np = c->Np;
+    float *Xf = nullptr, *Td = nullptr, *Hs = nullptr, *dY = nullptr;
+    __nv_bfloat16* Xb = nullptr;
+    bool ok = cudaMalloc(&Xf, (size_t)B * s->F * sizeof(float)) == cudaSuccess &&
+              cudaMalloc(&Xb, (size_t)B * s->F * sizeof(__nv_bfloat16)) == cudaSuccess &&
+              cudaMalloc(&Td, (size_t)B * Np * sizeof(float)) == cudaSuccess &&
+              cudaMalloc(&Hs, (size_t)2 * B * s->H * sizeof(float)) == cudaSuccess &&
+              cudaMalloc(&dY, (size_t)B * Np * sizeof(float)) == cudaSuccess;
+    int rc = DG_OK;
+    if (!ok) rc = ifail(c, DG_ERR_NOMEM, "dg_lpc_gradients: allocation failed");
+    if (rc == DG_OK) {
+        LpcNet net;
+        LpcFeatArgs fa;
+        lpc_descr(c, net, fa);
+        cudaMemcpyAsync(Xf, X_host, (size_t)B * s->F * sizeof(float), cudaMemcpyHostToDevice, c->stream);
+        cudaMemcpyAsync(Td, T_host, (size_t)B * Np * sizeof(float), cudaMemcpyHostToDevice, c->stream);
+        f32_to_bf16_kernel<<<256, 256, 0, c->stream>>>(Xf, Xb, (long long)B * s->F);
+        cudaError_t e = launch_lpc_forward(net, Xb, Td, B, Hs, dY, s->d_lpart, s->G, c->stream);
+        if (e == cudaSuccess) e = launch_lpc_backward(net, Xb, Hs, dY, B, s->d_g1, s->d_g2, c->stream);
+        double l = 0;
+        if (e != cudaSuccess) rc = ifail(c, DG_ERR_CUDA, std::string("lpc kernels: ") + cudaGetErrorString(e));
+        if (rc == DG_OK) rc = lpc_sum(c, s->d_lpart, &l);
+        if (rc == DG_OK) {
+            cudaMemcpyAsync(gW1, s->d_g1, (size_t)s->H * s->F * sizeof(float), cudaMemcpyDeviceToHost, c->stream);
+            cudaMemcpyAsync(gW2, s->d_g2, (size_t)Np * s->H * sizeof(float), cudaMemcpyDeviceToHost, c->stream);
+            cudaStreamSynchronize(c->stream);
+            if (loss) *loss = l / (2.0 * B * Np);
+        }
+    }
+    cudaFree(Xf);
+    cudaFree(Xb);
+    cudaFree(Td);
+    cudaFree(Hs);
+    cudaFree(dY);
+    return rc;
+}
+
+int dg_lpc_apply(dg_ctx* c, const double* r_host, double* z_host) {
+    if (!c || !r_host || !z_host) return DG_ERR_ARG;
+    if (!lpc_ok(c)) return ifail(c, DG_ERR_ARG, "dg_lpc_setup not called");
+    IpdgState* s = c->ipdg;
+    const int K = c->K, Np = c->Np;
+    const size_t n = (size_t)K * Np;
+    int rc = lpc_upload_residual(c, r_host, s->d_r);
+    if (rc) return rc;
+    IP_CUDA(c, launch_bj(s->args, s->d_P32, s->d_r, s->d_zb, c->stream));
+    LpcNet net;
+    LpcFeatArgs fa;
+    lpc_descr(c, net, fa);
+    IP_CUDA(c, cudaMemsetAsync(s->d_z, 0, n * sizeof(double), c->stream));
+    IP_CUDA(c, launch_lpc_precond(net, fa, s->d_r, s->d_z, LPC_APPLY, nullptr, nullptr, nullptr, c->stream));
+    IP_CUDA(c, launch_permute(s->d_z, s->d_p, c->d_ring, K, Np, false, c->stream));
+    IP_CUDA(c, cudaMemcpyAsync(z_host, s->d_p, n * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    IP_CUDA(c, cudaStreamSynchronize(c->stream));
     return DG_OK;
 }
 

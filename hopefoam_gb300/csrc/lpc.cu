@@ -1,0 +1,311 @@
+// lpc.cu -- learned element-block preconditioner: features, BF16 training
+// kernels (BF16 operands, FP32 accumulation, FP32 master weights with Adam)
+// and the inference kernel used inside the flexible PCG.
+//
+// Network (no biases, so it is positively homogeneous: M(a r) = a M(r), a > 0):
+//   x_k   = [z_k, Rot(z_n0), Rot(z_n1), Rot(z_n2)] / s_k  ++  h_k (rx, sx, ry, sy)
+//   z_k  <- z_k + s_k W2 relu(W1 x_k)
+// with z = P r the block-Jacobi output, Rot the node permutation that turns a
+// neighbour's shared face into its face 0 (3-fold symmetry of the node set),
+// s_k the RMS of the element's 4 z blocks and h_k = sqrt(J_k).  Trained on
+// (r, e) pairs from the method's own PCG solves: target (e_k - z_k) / s_k.
+#include <cuda_bf16.h>
+
+#include "lpc.hpp"
+#include "pcg_reduce.cuh"
+
+namespace dgk {
+
+__device__ __forceinline__ float bf(float x) { return __bfloat162float(__float2bfloat16(x)); }
+
+// features of element k into x[0..F) (FP32) and its scale; returns s
+__device__ __forceinline__ float lpc_element_features(const LpcFeatArgs& a, int k, float* x) {
+    const int Np = a.Np;
+    const double* zk = a.zb + (size_t)k * Np;
+    double ss = 0;
+    for (int i = 0; i < Np; i++) {
+        x[i] = (float)zk[i];
+        ss += zk[i] * zk[i];
+    }
+    for (int f = 0; f < 3; f++) {
+        const int c = a.conn[(size_t)k * 3 + f];
+        float* xf = x + (f + 1) * Np;
+        if (c >= 0) {
+            const int nb = c >> 3, fn = c & 3;
+            const double* zn = a.zb + (size_t)nb * Np;
+            const int* pm = a.perm + fn * Np;
+            for (int i = 0; i < Np; i++) {
+                const double v = zn[pm[i]];
+                xf[i] = (float)v;
+                ss += v * v;
+            }
+        } else {
+            for (int i = 0; i < Np; i++) xf[i] = 0.f;
+        }
+    }
+    const float s = (float)sqrt(ss / (4.0 * Np)) + 1e-30f;
+    const float inv = 1.f / s;
+    for (int i = 0; i < 4 * Np; i++) x[i] *= inv;
+    const double* g = a.geo + (size_t)k * 4;
+    const double J = 1.0 / (g[0] * g[3] - g[1] * g[2]);
+    const double h = sqrt(J);
+    x[4 * Np + 0] = (float)(g[0] * h);
+    x[4 * Np + 1] = (float)(g[1] * h);
+    x[4 * Np + 2] = (float)(g[2] * h);
+    x[4 * Np + 3] = (float)(g[3] * h);
+    return s;
+}
+
+constexpr int kMaxF = 4 * 36 + 4;
+
+__global__ void lpc_features_kernel(LpcFeatArgs a, __nv_bfloat16* __restrict__ X, float* __restrict__ s) {
+    const int F = 4 * a.Np + 4;
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < a.K; k += gridDim.x * blockDim.x) {
+        float x[kMaxF];
+        s[k] = lpc_element_features(a, k, x);
+        for (int i = 0; i < F; i++) X[(size_t)k * F + i] = __float2bfloat16(x[i]);
+    }
+}
+
+__global__ void lpc_targets_kernel(const double* __restrict__ e, const double* __restrict__ zb,
+                                   const float* __restrict__ s, int K, int Np, float* __restrict__ T) {
+    const size_t n = (size_t)K * Np;
+    for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < n; t += (size_t)gridDim.x * blockDim.x) {
+        const int k = (int)(t / Np);
+        T[t] = (float)((e[t] - zb[t]) / (double)s[k]);
+    }
+}
+
+// forward on a batch: Hs[b][h] = bf16(relu(W1 x_b)), dY[b][j] = W2 Hs_b - T_b (T null: the
+// network output itself); loss partials.
+// CTA = 128 threads, 32 samples per tile, grid-stride over tiles.
+__global__ void lpc_forward_kernel(LpcNet n, const __nv_bfloat16* __restrict__ X, const float* __restrict__ T, int B,
+                                   float* __restrict__ Hs, float* __restrict__ dY, double* __restrict__ part) {
+    extern __shared__ float fsm[];
+    const int F = n.F, H = n.H, Np = n.Np;
+    float* xs = fsm;             // [32][F]
+    float* hs = xs + 32 * F;     // [32][H]
+    __shared__ double red[4];
+    double loss = 0;
+    const int ntiles = (B + 31) / 32;
+    for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        const int b0 = tile * 32, nb = min(32, B - b0);
+        for (int i = threadIdx.x; i < nb * F; i += blockDim.x) xs[i] = __bfloat162float(X[(size_t)b0 * F + i]);
+        __syncthreads();
+        for (int it = threadIdx.x; it < nb * H; it += blockDim.x) {
+            const int sidx = it / H, h = it - sidx * H;
+            const __nv_bfloat16* w = n.W1 + (size_t)h * F;
+            float acc = 0.f;
+            for (int k = 0; k < F; k++) acc = fmaf(__bfloat162float(w[k]), xs[sidx * F + k], acc);
+            const float hv = bf(fmaxf(acc, 0.f));
+            hs[sidx * H + h] = hv;
+            Hs[(size_t)(b0 + sidx) * H + h] = hv;
+        }
+        __syncthreads();
+        for (int it = threadIdx.x; it < nb * Np; it += blockDim.x) {
+            const int sidx = it / Np, j = it - sidx * Np;
+            const __nv_bfloat16* w = n.W2 + (size_t)j * H;
+            float acc = 0.f;
+            for (int h = 0; h < H; h++) acc = fmaf(__bfloat162float(w[h]), hs[sidx * H + h], acc);
+            const float d = T ? acc - T[(size_t)(b0 + sidx) * Np + j] : acc;
+            dY[(size_t)(b0 + sidx) * Np + j] = d;
+            loss += (double)d * d;
+        }
+        __syncthreads();
+    }
+    for (int o = 16; o > 0; o >>= 1) loss += __shfl_xor_sync(0xffffffffu, loss, o);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = loss;
+    __syncthreads();
+    if (threadIdx.x == 0) part[blockIdx.x] = red[0] + red[1] + red[2] + red[3];
+}
+
+// dH[b][h] = (W2^T dY_b)_h * (Hs[b][h] > 0), written over Hs' companion buffer
+__global__ void lpc_dh_kernel(LpcNet n, const float* __restrict__ Hs, const float* __restrict__ dY, int B,
+                              float* __restrict__ dH) {
+    const int H = n.H, Np = n.Np;
+    const size_t tot = (size_t)B * H;
+    for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < tot; t += (size_t)gridDim.x * blockDim.x) {
+        const int b = (int)(t / H), h = (int)(t - (size_t)b * H);
+        float acc = 0.f;
+        if (Hs[t] > 0.f)
+            for (int j = 0; j < Np; j++) acc = fmaf(__bfloat162float(n.W2[(size_t)j * H + h]), dY[(size_t)b * Np + j], acc);
+        dH[t] = bf(acc);
+    }
+}
+
+// gW2[j][h] = sum_b dY[b][j] Hs[b][h] / B ; gW1[h][k] = sum_b dH[b][h] X[b][k] / B
+__global__ void lpc_gw_kernel(LpcNet n, const __nv_bfloat16* __restrict__ X, const float* __restrict__ Hs,
+                              const float* __restrict__ dY, const float* __restrict__ dH, int B,
+                              float* __restrict__ gW1, float* __restrict__ gW2) {
+    const int F = n.F, H = n.H, Np = n.Np;
+    const int n1 = H * F, n2 = Np * H;
+    const float invB = 1.f / (float)B;
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n1 + n2; t += gridDim.x * blockDim.x) {
+        float acc = 0.f;
+        if (t < n1) {
+            const int h = t / F, k = t - h * F;
+            for (int b = 0; b < B; b++) acc = fmaf(dH[(size_t)b * H + h], __bfloat162float(X[(size_t)b * F + k]), acc);
+            gW1[t] = acc * invB;
+        } else {
+            const int u = t - n1, j = u / H, h = u - j * H;
+            for (int b = 0; b < B; b++) acc = fmaf(dY[(size_t)b * Np + j], Hs[(size_t)b * H + h], acc);
+            gW2[u] = acc * invB;
+        }
+    }
+}
+
+__global__ void lpc_adam_kernel(float* W, float* m, float* v, const float* g, __nv_bfloat16* Wb, int n, float lr,
+                                float b1, float b2, float eps, int step, float gscale) {
+    const float c1 = 1.f - powf(b1, (float)step), c2 = 1.f - powf(b2, (float)step);
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const float gi = g[i] * gscale;
+        const float mi = b1 * m[i] + (1.f - b1) * gi;
+        const float vi = b2 * v[i] + (1.f - b2) * gi * gi;
+        m[i] = mi;
+        v[i] = vi;
+        const float w = W[i] - lr * (mi / c1) / (sqrtf(vi / c2) + eps);
+        W[i] = w;
+        Wb[i] = __float2bfloat16(w);
+    }
+}
+
+// PCG preconditioner: z_k = zb_k + s_k W2 relu(W1 x_k), with the CG scalars
+// it completes (mode): LPC_APPLY none; LPC_PCG_INIT / LPC_PCG_REFRESH S->rz;
+// LPC_PCG_ITERATION beta and the stop test (r.z, r.z_old, S->rr).
+// Weights staged in shared memory (BF16); one thread per element; grid-stride.
+__global__ void lpc_precond_kernel(LpcNet n, LpcFeatArgs a, const double* __restrict__ r, double* __restrict__ z,
+                                   int mode, PcgScalars* S, double* part, float* __restrict__ dz) {
+    extern __shared__ __nv_bfloat16 wsm[];
+    if (mode == LPC_PCG_ITERATION && S->done) return;
+    const int F = n.F, H = n.H, Np = n.Np;
+    __nv_bfloat16* w1 = wsm;
+    __nv_bfloat16* w2 = wsm + H * F;
+    for (int i = threadIdx.x; i < H * F; i += blockDim.x) w1[i] = n.W1[i];
+    for (int i = threadIdx.x; i < Np * H; i += blockDim.x) w2[i] = n.W2[i];
+    __syncthreads();
+    double rz = 0, rzo = 0;
+    const int nthr = gridDim.x * blockDim.x;
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < a.K; k += nthr) {
+        float x[kMaxF];
+        const float s = lpc_element_features(a, k, x);
+        for (int i = 0; i < F; i++) x[i] = bf(x[i]);
+        float y[36];
+        for (int j = 0; j < Np; j++) y[j] = 0.f;
+        for (int h = 0; h < H; h++) {
+            const __nv_bfloat16* wr = w1 + h * F;
+            float acc = 0.f;
+            for (int i = 0; i < F; i++) acc = fmaf(__bfloat162float(wr[i]), x[i], acc);
+            const float hv = bf(fmaxf(acc, 0.f));
+            for (int j = 0; j < Np; j++) y[j] = fmaf(__bfloat162float(w2[j * H + h]), hv, y[j]);
+        }
+        const double* zbk = a.zb + (size_t)k * Np;
+        const double* rk = r + (size_t)k * Np;
+        double* zk = z + (size_t)k * Np;
+        const double z0 = zbk[0] + (double)s * (double)y[0];
+        for (int j = 0; j < Np; j++) {
+            const double zn = zbk[j] + (double)s * (double)y[j];
+            if (mode == LPC_PCG_ITERATION) rzo += rk[j] * zk[j];
+            rz += rk[j] * zn;
+            zk[j] = zn;
+            if (dz) dz[(size_t)k * Np + j] = (float)(zn - z0);
+        }
+    }
+    if (mode == LPC_APPLY) return;
+    double val[2] = {rz, rzo}, tot[2];
+    if (grid_sum<2>(val, part, gridDim.x, &S->counter, tot) && threadIdx.x == 0) {
+        if (mode == LPC_PCG_ITERATION) pcg_finish(S, tot[0], tot[1], S->rr);
+        else S->rz = tot[0];
+    }
+}
+
+// z = zb + s y (the preconditioner output the PCG uses), ring order
+__global__ void lpc_combine_kernel(const double* __restrict__ zb, const float* __restrict__ s,
+                                   const float* __restrict__ y, int K, int Np, double* __restrict__ z) {
+    const size_t n = (size_t)K * Np;
+    for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < n; t += (size_t)gridDim.x * blockDim.x) {
+        const int k = (int)(t / Np);
+        z[t] = zb[t] + (double)s[k] * (double)y[t];
+    }
+}
+
+// output gradient of the energy loss L = -(r.z)|r.z| / (z.Sz): dL/dz is a
+// positive multiple (2|a|/b) of (a/b) Sz - r (a = r.z, b = z.Sz, each reduced
+// from G partials); chained through z = zb + s y: dY = s ((a/b) w - r)
+__global__ void lpc_energy_dy_kernel(const double* __restrict__ r, const double* __restrict__ w,
+                                     const float* __restrict__ s, const double* __restrict__ part_a,
+                                     const double* __restrict__ part_b, int G, int K, int Np,
+                                     float* __restrict__ dY) {
+    __shared__ double s_ab;
+    if (threadIdx.x < 32) {
+        double a = 0, b = 0;
+        for (int i = threadIdx.x; i < G; i += 32) { a += part_a[i]; b += part_b[i]; }
+        for (int o = 16; o > 0; o >>= 1) {
+            a += __shfl_xor_sync(0xffffffffu, a, o);
+            b += __shfl_xor_sync(0xffffffffu, b, o);
+        }
+        if (threadIdx.x == 0) s_ab = (b > 0) ? a / b : 0.0;
+    }
+    __syncthreads();
+    const double ab = s_ab;
+    const size_t n = (size_t)K * Np;
+    for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < n; t += (size_t)gridDim.x * blockDim.x) {
+        const int k = (int)(t / Np);
+        dY[t] = (float)((double)s[k] * (ab * w[t] - r[t]));
+    }
+}
+
+cudaError_t launch_lpc_combine(const double* zb, const float* s, const float* y, int K, int Np, double* z,
+                               cudaStream_t st) {
+    lpc_combine_kernel<<<608, 256, 0, st>>>(zb, s, y, K, Np, z);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_lpc_energy_dy(const double* r, const double* w, const float* s, const double* part_a,
+                                 const double* part_b, int G, int K, int Np, float* dY, cudaStream_t st) {
+    lpc_energy_dy_kernel<<<608, 256, 0, st>>>(r, w, s, part_a, part_b, G, K, Np, dY);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_lpc_features(const LpcFeatArgs& a, __nv_bfloat16* X, float* s, cudaStream_t st) {
+    lpc_features_kernel<<<(a.K + 127) / 128, 128, 0, st>>>(a, X, s);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_lpc_targets(const double* e, const double* zb, const float* s, int K, int Np, float* T,
+                               cudaStream_t st) {
+    lpc_targets_kernel<<<608, 256, 0, st>>>(e, zb, s, K, Np, T);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_lpc_forward(const LpcNet& n, const __nv_bfloat16* X, const float* T, int B, float* Hs, float* dY,
+                               double* loss_part, int G, cudaStream_t st) {
+    const size_t smem = sizeof(float) * 32 * (n.F + n.H);
+    lpc_forward_kernel<<<G, 128, smem, st>>>(n, X, T, B, Hs, dY, loss_part);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_lpc_backward(const LpcNet& n, const __nv_bfloat16* X, const float* Hs, const float* dY, int B,
+                                float* gW1, float* gW2, cudaStream_t st) {
+    // dH is stored in the second half of the Hs buffer (caller allocates 2 x B x H)
+    float* dH = const_cast<float*>(Hs) + (size_t)B * n.H;
+    lpc_dh_kernel<<<608, 256, 0, st>>>(n, Hs, dY, B, dH);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    lpc_gw_kernel<<<(n.H * n.F + n.Np * n.H + 127) / 128, 128, 0, st>>>(n, X, Hs, dY, dH, B, gW1, gW2);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_lpc_adam(float* W, float* m, float* v, const float* g, __nv_bfloat16* Wb, int n, float lr, float b1,
+                            float b2, float eps, int step, float gscale, cudaStream_t st) {
+    lpc_adam_kernel<<<(n + 255) / 256, 256, 0, st>>>(W, m, v, g, Wb, n, lr, b1, b2, eps, step, gscale);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_lpc_precond(const LpcNet& n, const LpcFeatArgs& fa, const double* r, double* z, int mode,
+                               PcgScalars* S, double* part, float* dz, cudaStream_t st) {
+    const size_t smem = sizeof(__nv_bfloat16) * (size_t)(n.H * n.F + n.Np * n.H);
+    lpc_precond_kernel<<<608, 128, smem, st>>>(n, fa, r, z, mode, S, part, dz);
+    return cudaGetLastError();
+}
+
+}  // namespace dgk

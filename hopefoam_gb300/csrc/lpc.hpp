@@ -1,0 +1,56 @@
+// lpc.hpp -- learned element-block preconditioner for the SIPG PCG.
+#pragma once
+
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "ipdg.hpp"
+
+namespace dgk {
+
+// z_k = (P r)_k + s_k * W2 relu(W1 x_k / s_k)   with the feature vector
+// x_k = [(P r)_k, rotated (P r) of the 3 neighbours, 4 scaled metrics]
+struct LpcNet {
+    int F = 0;       // features = 4 Np + 4
+    int H = 128;     // hidden width
+    int Np = 0;      // outputs
+    const __nv_bfloat16* W1 = nullptr;  // H x F (BF16 copy used by the kernels)
+    const __nv_bfloat16* W2 = nullptr;  // Np x H
+    const int* perm = nullptr;          // 3 x Np ring-order node permutation per neighbour face
+};
+
+struct LpcFeatArgs {
+    int K, Np;
+    const double* zb;     // block-Jacobi output, ring order, K x Np
+    const int* conn;      // packed neighbours
+    const double* geo;    // metrics
+    const int* perm;      // 3 x Np
+};
+
+// features X (K x F, BF16) and per-element scale s (K) from zb
+cudaError_t launch_lpc_features(const LpcFeatArgs& a, __nv_bfloat16* X, float* s, cudaStream_t st);
+// targets T (K x Np) = (e - zb) / s
+cudaError_t launch_lpc_targets(const double* e, const double* zb, const float* s, int K, int Np, float* T,
+                               cudaStream_t st);
+// training step pieces on a batch of B samples (rows of X, T)
+cudaError_t launch_lpc_forward(const LpcNet& n, const __nv_bfloat16* X, const float* T, int B, float* Hs, float* dY,
+                               double* loss_part, int G, cudaStream_t st);
+cudaError_t launch_lpc_backward(const LpcNet& n, const __nv_bfloat16* X, const float* Hs, const float* dY, int B,
+                                float* gW1, float* gW2, cudaStream_t st);
+cudaError_t launch_lpc_adam(float* W, float* m, float* v, const float* g, __nv_bfloat16* Wb, int n, float lr,
+                            float b1, float b2, float eps, int step, float gscale, cudaStream_t st);
+// z = zb + s y
+cudaError_t launch_lpc_combine(const double* zb, const float* s, const float* y, int K, int Np, double* z,
+                               cudaStream_t st);
+// dY = s ((a/b) w - r) with a, b the sums of G partials each (energy-loss output gradient)
+cudaError_t launch_lpc_energy_dy(const double* r, const double* w, const float* s, const double* part_a,
+                                 const double* part_b, int G, int K, int Np, float* dY, cudaStream_t st);
+// inference: z = zb + s * MLP(x); the CG scalars completed depend on mode
+enum { LPC_APPLY = 0, LPC_PCG_INIT = 1, LPC_PCG_REFRESH = 2, LPC_PCG_ITERATION = 3 };
+// dz (may be null): FP32 offset mirror of z (z minus the element's first-node value)
+cudaError_t launch_lpc_precond(const LpcNet& n, const LpcFeatArgs& fa, const double* r, double* z, int mode,
+                               PcgScalars* S, double* part, float* dz, cudaStream_t st);
+
+}  // namespace dgk

@@ -16,6 +16,38 @@ from . import _lib as L
 from .euler import EulerContext, _check
 
 
+def poisson_rhs(mesh, order, seed=0, kmax=16, tg_weight=1.0, t=0.0, nu=0.01):
+    """Right-hand side of the pressure benchmark on [0, 2pi]^2: the pressure
+    source of the Taylor-Green vortex, cos 2x + cos 2y (the divergence of
+    u.grad u for u = (sin x cos y, -cos x sin y) e^{-2 nu t}, Re = 1/nu = 100),
+    plus seeded Gaussian random Fourier modes with |k| <= kmax, amplitudes
+    ~ N(0, 1/|k|^2); projected with the element mass matrices (b = M f)."""
+    from .euler import node_coords, reference_operators
+
+    ops = reference_operators(order)
+    x, y = node_coords(mesh, ops["r"], ops["s"])
+    f = tg_weight * np.exp(-4 * nu * t) * (np.cos(2 * x) + np.cos(2 * y))
+    rng = np.random.default_rng(seed)
+    kxs = np.arange(-kmax, kmax + 1)
+    kys = np.arange(0, kmax + 1)
+    C = np.zeros((kxs.size, kys.size), np.complex128)
+    for i, kx in enumerate(kxs):
+        for j, ky in enumerate(kys):
+            k2 = kx * kx + ky * ky
+            if k2 == 0 or k2 > kmax * kmax or (ky == 0 and kx < 0):
+                continue
+            a, b = rng.standard_normal(2) / np.sqrt(k2)
+            C[i, j] = a - 1j * b  # a cos(phase) + b sin(phase) = Re((a - i b) e^{i phase})
+    xf, yf = x.reshape(-1), y.reshape(-1)
+    Ex = np.exp(1j * np.outer(xf, kxs))
+    Ey = np.exp(1j * np.outer(yf, kys))
+    f += np.sum((Ex @ C) * Ey, axis=1).real.reshape(x.shape)
+    v = mesh.VXY
+    J = 0.25 * ((v[:, 1, 0] - v[:, 0, 0]) * (v[:, 2, 1] - v[:, 0, 1]) - (v[:, 2, 0] - v[:, 0, 0]) * (v[:, 1, 1] - v[:, 0, 1]))
+    b = J[:, None] * (f @ ops["Mref"].T)
+    return b.reshape(-1), f
+
+
 class PressureSolver:
     def __init__(self, mesh, order, tau_coef=20.0, ctx=None):
         self.ctx = ctx if ctx is not None else EulerContext(mesh, order)
@@ -39,3 +71,94 @@ class PressureSolver:
         if rc != L.DG_OK and raise_on_fail:
             _check(self.ctx.h, rc)
         return x, {"iterations": st.iterations, "rel_residual": st.rel_residual, "ms": st.ms, "status": rc}
+
+    # ------------------------------------------------------------------
+    # learned element-block preconditioner (DG_PC_LEARNED)
+
+    def lpc_setup(self, hidden=128, seed=0, capacity=0):
+        """Allocates the network (He-initialised W1, small W2) and room for
+        `capacity` training residual vectors on the device."""
+        self.lpc_hidden = int(hidden)
+        self.lpc_F = 4 * self.Np + 4
+        _check(self.ctx.h, self.ctx.lib.dg_lpc_setup(self.ctx.h, int(hidden), int(seed), int(capacity)))
+
+    def lpc_add_residual(self, r):
+        r = np.ascontiguousarray(r, np.float64).reshape(-1)
+        _check(self.ctx.h, self.ctx.lib.dg_lpc_add_residual(self.ctx.h, L.dptr(r)))
+
+    def lpc_collect(self, rhs_list, snapshots=(1, 2, 3, 5, 8, 13, 21, 34, 55, 89, 144, 233), rtol=1e-10,
+                    precision=L.DG_PREC_SPLIT):
+        """Training residuals from this solver's own block-Jacobi PCG: for
+        each right-hand side b, the residuals b - S x_j of the iterates after
+        j iterations (j in `snapshots`).  Returns the number added."""
+        n = 0
+        for b in rhs_list:
+            for j in snapshots:
+                xj, st = self.solve(b, rtol=rtol, maxit=int(j), pc=L.DG_PC_BLOCK_JACOBI, precision=precision,
+                                    raise_on_fail=False)
+                if st["status"] not in (L.DG_OK, L.DG_ERR_NOT_CONVERGED):
+                    _check(self.ctx.h, st["status"])
+                self.lpc_add_residual(b - self.apply(xj))
+                n += 1
+        return n
+
+    def lpc_train(self, epochs=20, lr=1e-3, seed=0):
+        """Adam epochs over the stored residuals on the GPU; returns the mean
+        energy loss with the network and with block Jacobi alone."""
+        loss, loss_bj = ctypes.c_double(0.0), ctypes.c_double(0.0)
+        _check(self.ctx.h, self.ctx.lib.dg_lpc_train(self.ctx.h, int(epochs), float(lr), int(seed),
+                                                     ctypes.byref(loss), ctypes.byref(loss_bj)))
+        return loss.value, loss_bj.value
+
+    def lpc_loss(self, r):
+        r = np.ascontiguousarray(r, np.float64).reshape(-1)
+        loss, loss_bj = ctypes.c_double(0.0), ctypes.c_double(0.0)
+        _check(self.ctx.h, self.ctx.lib.dg_lpc_loss(self.ctx.h, L.dptr(r), ctypes.byref(loss), ctypes.byref(loss_bj)))
+        return loss.value, loss_bj.value
+
+    def lpc_energy_gradients(self, r):
+        r = np.ascontiguousarray(r, np.float64).reshape(-1)
+        gW1 = np.zeros((self.lpc_hidden, self.lpc_F), np.float32)
+        gW2 = np.zeros((self.Np, self.lpc_hidden), np.float32)
+        loss = ctypes.c_double(0.0)
+        fp = ctypes.POINTER(ctypes.c_float)
+        _check(self.ctx.h, self.ctx.lib.dg_lpc_energy_gradients(self.ctx.h, L.dptr(r), gW1.ctypes.data_as(fp),
+                                                                gW2.ctypes.data_as(fp), ctypes.byref(loss)))
+        return gW1, gW2, loss.value
+
+    def lpc_weights(self):
+        W1 = np.zeros((self.lpc_hidden, self.lpc_F), np.float32)
+        W2 = np.zeros((self.Np, self.lpc_hidden), np.float32)
+        fp = ctypes.POINTER(ctypes.c_float)
+        _check(self.ctx.h, self.ctx.lib.dg_lpc_get_weights(self.ctx.h, W1.ctypes.data_as(fp), W2.ctypes.data_as(fp)))
+        return W1, W2
+
+    def lpc_set_weights(self, W1, W2):
+        W1 = np.ascontiguousarray(W1, np.float32)
+        W2 = np.ascontiguousarray(W2, np.float32)
+        if W1.shape != (self.lpc_hidden, self.lpc_F) or W2.shape != (self.Np, self.lpc_hidden):
+            raise ValueError("weight shapes do not match the network")
+        fp = ctypes.POINTER(ctypes.c_float)
+        _check(self.ctx.h, self.ctx.lib.dg_lpc_set_weights(self.ctx.h, W1.ctypes.data_as(fp), W2.ctypes.data_as(fp)))
+
+    def lpc_gradients(self, X, T):
+        """One forward/backward of the training kernels on a host batch:
+        (dL/dW1, dL/dW2, loss)."""
+        X = np.ascontiguousarray(X, np.float32)
+        T = np.ascontiguousarray(T, np.float32)
+        B = X.shape[0]
+        gW1 = np.zeros((self.lpc_hidden, self.lpc_F), np.float32)
+        gW2 = np.zeros((self.Np, self.lpc_hidden), np.float32)
+        loss = ctypes.c_double(0.0)
+        fp = ctypes.POINTER(ctypes.c_float)
+        _check(self.ctx.h, self.ctx.lib.dg_lpc_gradients(self.ctx.h, X.ctypes.data_as(fp), T.ctypes.data_as(fp), B,
+                                                         gW1.ctypes.data_as(fp), gW2.ctypes.data_as(fp),
+                                                         ctypes.byref(loss)))
+        return gW1, gW2, loss.value
+
+    def lpc_apply(self, r):
+        """The learned preconditioner applied once: z = M(r)."""
+        r = np.ascontiguousarray(r, np.float64).reshape(-1)
+        z = np.empty_like(r)
+        _check(self.ctx.h, self.ctx.lib.dg_lpc_apply(self.ctx.h, L.dptr(r), L.dptr(z)))
+        return z

@@ -55,7 +55,7 @@ enum {
 enum { DG_BC_INTERIOR = 0, DG_BC_FIXED = 1 };
 
 /* preconditioners for dg_pcg_solve */
-enum { DG_PC_NONE = 0, DG_PC_BLOCK_JACOBI = 1, DG_PC_LEARNED = 2 };
+enum { DG_PC_NONE = 0, DG_PC_BLOCK_JACOBI = 1, DG_PC_LEARNED = 2, DG_PC_LEARNED_ONLY = 3 };
 
 typedef struct dg_ctx dg_ctx;
 
@@ -156,13 +156,59 @@ int dg_ipdg_apply(dg_ctx* ctx, const double* x_host, double* y_host);
 /* Solves S x = b to ||b - S x|| <= rtol ||b|| with preconditioned CG
  * (replaces dgMatrix::solve -> KSPSolve, dgMatrices/dgMatrix/dgMatrix.C:162-283,
  * dgMatrixSolve.C:91-213).  x_host holds the initial guess and receives the
- * solution.  pc: DG_PC_BLOCK_JACOBI or DG_PC_LEARNED (after dg_lpc_*).
+ * solution.  pc: DG_PC_BLOCK_JACOBI, DG_PC_LEARNED (after dg_lpc_*; falls back
+ * to block Jacobi) or DG_PC_LEARNED_ONLY (no fallback: reports the learned
+ * solve's own outcome).
  * precision DG_PREC_FP64: FP64 operator in every iteration; DG_PREC_SPLIT:
- * mixed-precision refinement (FP32-arithmetic operator inside CG, FP64 outer
- * residual, FP64 vectors and dot products).  The returned rel_residual is
- * the true FP64 residual.  DG_ERR_NOT_CONVERGED when maxit is reached. */
+ * FP32-arithmetic operator inside CG with FP64 vectors, dot products and
+ * recurrences, the recurrence residual replaced by the true FP64 residual
+ * b - S x every 64 iterations.  Either way a convergence claim of the
+ * recurrence is confirmed against the true FP64 residual.  The returned
+ * rel_residual is the true FP64 residual.  DG_ERR_NOT_CONVERGED when maxit is
+ * reached (x_host still receives the last iterate). */
 int dg_pcg_solve(dg_ctx* ctx, const double* b_host, double* x_host, double rtol, int maxit, int pc, int precision,
                  dg_solve_stats* stats);
+
+/* Learned element-block preconditioner for dg_pcg_solve (DG_PC_LEARNED).  No
+ * counterpart in the reference (its KSP uses jacobi / LU, dgMatrix.C:199-222).
+ * z = M(r) = P r + s W2 relu(W1 x / s): P the block-Jacobi inverse, x the
+ * block-Jacobi outputs of the element and its three neighbours (neighbours
+ * rotated so the shared face is their face 0) and four scaled metrics, s
+ * their RMS; W1 (hidden x F), W2 (Np x hidden), F = 4 Np + 4, BF16 for the
+ * kernels, FP32 master copies.  The solve is flexible CG; when a learned
+ * solve does not reach rtol, dg_pcg_solve repeats it with block Jacobi from
+ * the same initial guess and reports negative iterations.
+ *   dg_lpc_setup: after dg_ipdg_setup; capacity = training residual vectors
+ *     kept on the device.
+ *   dg_lpc_add_residual: one residual r = b - S x of the method's own PCG
+ *     (host array, reference node order), stored scaled to r.P r = 1.
+ *   dg_lpc_train: Adam epochs, one step per stored residual, minimising the
+ *     energy loss L(r) = -(r.z)^2 / (z.S z), z = M(r) (the S-norm error
+ *     decrease of one optimally scaled step along z, negated, times 2), with
+ *     the hand-written BF16 forward/backward kernels (FP32 accumulation).
+ *     final_loss / final_loss_bj: mean L over the stored residuals with the
+ *     network and with block Jacobi alone (more negative is better).
+ *   dg_lpc_loss: L(r) for one host residual, with and without the network.
+ *   dg_lpc_energy_gradients: dL/dW1, dL/dW2 and L for one host residual.
+ *   dg_lpc_get/set_weights: FP32 W1 (hidden x F), W2 (Np x hidden) row-major
+ *     (set also resets the Adam moments).
+ *   dg_lpc_gradients: gradients of the mean-squared loss
+ *     sum_b 0.5 ||W2 h_b - t_b||^2 / B of the network alone on a host batch
+ *     (X: B x F, T: B x Np; X rounded to BF16 on the device; loss reported
+ *     per output), a direct check of the backward kernels.
+ *   dg_lpc_apply: z = M(r) once (host arrays of K*Np doubles, reference node
+ *     order). */
+int dg_lpc_setup(dg_ctx* ctx, int hidden, unsigned long long seed, int capacity);
+int dg_lpc_add_residual(dg_ctx* ctx, const double* r_host);
+int dg_lpc_train(dg_ctx* ctx, int epochs, double lr, unsigned long long seed, double* final_loss,
+                 double* final_loss_bj);
+int dg_lpc_loss(dg_ctx* ctx, const double* r_host, double* loss, double* loss_bj);
+int dg_lpc_energy_gradients(dg_ctx* ctx, const double* r_host, float* gW1, float* gW2, double* loss);
+int dg_lpc_get_weights(dg_ctx* ctx, float* W1, float* W2);
+int dg_lpc_set_weights(dg_ctx* ctx, const float* W1, const float* W2);
+int dg_lpc_gradients(dg_ctx* ctx, const float* X_host, const float* T_host, int B, float* gW1, float* gW2,
+                     double* loss);
+int dg_lpc_apply(dg_ctx* ctx, const double* r_host, double* z_host);
 
 /* Allocation-free right-hand side.  No counterpart in the reference: it is an
  * addition for callers that must not allocate device memory while they run

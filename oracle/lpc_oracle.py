@@ -1,0 +1,176 @@
+"""CPU restatement of the learned element-block preconditioner (numpy).
+
+TEST INFRASTRUCTURE ONLY: the checker for the library's BF16 training and
+inference kernels (hopefoam_gb300/csrc/lpc.cu).  Nothing in the product path
+imports this module.
+
+The learned preconditioner has no counterpart in the reference (its pressure
+solve hands the assembled matrix to PETSc KSP with a jacobi / LU
+preconditioner, DG/dgMatrices/dgMatrix/dgMatrix.C:199-222), so the parity
+anchor is this restatement of the network the kernels implement, written
+from its definition:
+
+    x_k = [z_k, Rot(z_n0), Rot(z_n1), Rot(z_n2)] / s_k ++ sqrt(J_k) (rx, sx, ry, sy)
+    M(r)_k = z_k + s_k W2 relu(W1 x_k),         z = P r (block Jacobi)
+
+with element vectors in the library's ring node order (the 3N boundary nodes
+face by face, then the interior nodes), Rot the node permutation that turns
+the neighbour's shared face into its face 0, s_k the RMS of the element's
+four z blocks.  Kernel arithmetic rules restated here: BF16 operands (inputs,
+weights, hidden activations and the hidden-layer gradient rounded to BF16,
+round to nearest even), sums accumulated in FP32 or wider, block Jacobi with
+FP32 blocks and FP32 accumulation.
+
+Loss of a batch of B samples: L = sum_b 0.5 ||W2 h_b - t_b||^2 / B; the
+library reports L / Np.
+"""
+import numpy as np
+
+
+def bf16(x):
+    """Round to the nearest BF16 value (ties to even), returned as float32."""
+    a = np.ascontiguousarray(x, np.float32)
+    u = a.view(np.uint32).astype(np.uint64)
+    u = (u + 0x7FFF + ((u >> 16) & 1)) & 0xFFFF0000
+    return u.astype(np.uint32).view(np.float32).reshape(a.shape)
+
+
+def face_nodes(order):
+    N = order
+    Np = (N + 1) * (N + 2) // 2
+    f = np.zeros((3, N + 1), np.int64)
+    f[0] = np.arange(N + 1)
+    f[1, 0] = N
+    f[2, 0] = Np - 1
+    for i in range(1, N + 1):
+        f[1, i] = f[1, i - 1] + (N + 1 - i)
+        f[2, i] = f[2, i - 1] - i - 1
+    return f
+
+
+def ring_order(order):
+    """Reference node id at each ring position."""
+    N = order
+    Np = (N + 1) * (N + 2) // 2
+    fn = face_nodes(order)
+    ring = [int(fn[f, j]) for f in range(3) for j in range(N)]
+    onb = set(ring)
+    ring += [i for i in range(Np) if i not in onb]
+    return np.array(ring, np.int64)
+
+
+def rotation_perms(r, s, ring):
+    """perm[fn, i]: ring position of the node that the rotation taking face fn
+    to face 0 maps onto ring position i (barycentric coordinates cycled)."""
+    rr, ss = r[ring], s[ring]
+    lam = np.stack([-(rr + ss) / 2, (1 + rr) / 2, (1 + ss) / 2], axis=1)
+    Np = ring.size
+    perm = np.full((3, Np), -1, np.int64)
+    for fn in range(3):
+        for i in range(Np):
+            want = np.empty(3)
+            for m in range(3):
+                want[(fn + m) % 3] = lam[i, m]
+            d = np.abs(lam - want).sum(axis=1)
+            j = int(np.argmin(d))
+            assert d[j] < 1e-9
+            perm[fn, i] = j
+    return perm
+
+
+def block_jacobi32(S_blocks, r):
+    """z = P r per element with P = inv(S_kk) rounded to FP32 and FP32
+    accumulation (reference node order)."""
+    P = np.linalg.inv(S_blocks).astype(np.float32)
+    rk = r.reshape(S_blocks.shape[0], -1).astype(np.float32)
+    return np.einsum("kij,kj->ki", P, rk).astype(np.float64)
+
+
+def features(zb_ring, EToE, EToF, geo, perm):
+    """X (K x F, float32, before BF16 rounding) and s (K) from the block
+    Jacobi output in ring order; geo = K x 4 (rx, sx, ry, sy); boundary faces
+    (EToE[k, f] < 0) give zero blocks."""
+    K, Np = zb_ring.shape
+    blocks = [zb_ring]
+    for f in range(3):
+        nb = EToE[:, f]
+        bnd = nb < 0
+        nbc = np.where(bnd, 0, nb)
+        fn = np.where(bnd, 0, EToF[:, f])
+        zn = zb_ring[nbc][np.arange(K)[:, None], perm[fn]]
+        zn[bnd] = 0.0
+        blocks.append(zn)
+    Z = np.concatenate(blocks, axis=1)
+    s = (np.sqrt((Z * Z).sum(axis=1) / (4.0 * Np))).astype(np.float32) + np.float32(1e-30)
+    X = (Z.astype(np.float32) * (np.float32(1.0) / s)[:, None]).astype(np.float32)
+    J = 1.0 / (geo[:, 0] * geo[:, 3] - geo[:, 1] * geo[:, 2])
+    h = np.sqrt(J)
+    X = np.concatenate([X, (geo * h[:, None]).astype(np.float32)], axis=1)
+    return X, s
+
+
+def forward(W1, W2, X, T):
+    """Hidden activations (BF16-rounded), output residuals dY and the loss
+    (library convention: mean over samples and outputs of 0.5 dY^2)."""
+    W1b, W2b, Xb = bf16(W1).astype(np.float64), bf16(W2).astype(np.float64), bf16(X).astype(np.float64)
+    A = (Xb @ W1b.T).astype(np.float32)
+    Hs = bf16(np.maximum(A, 0.0)).astype(np.float64)
+    Y = (Hs @ W2b.T).astype(np.float32)
+    dY = (Y - np.asarray(T, np.float32)).astype(np.float64)
+    loss = 0.5 * float((dY * dY).sum()) / (X.shape[0] * W2.shape[0])
+    return Hs, dY, loss
+
+
+def gradients(W1, W2, X, T):
+    """dL/dW1, dL/dW2 (L = sum_b 0.5 ||dY_b||^2 / B) under the kernel rounding
+    rules, and the library's loss value."""
+    B = X.shape[0]
+    Hs, dY, loss = forward(W1, W2, X, T)
+    W2b = bf16(W2).astype(np.float64)
+    dH = bf16(((dY @ W2b) * (Hs > 0)).astype(np.float32)).astype(np.float64)
+    Xb = bf16(X).astype(np.float64)
+    gW2 = dY.T @ Hs / B
+    gW1 = dH.T @ Xb / B
+    return gW1, gW2, loss
+
+
+def gradients_exact(W1, W2, X, T):
+    """FP64 gradients of the same loss without any rounding (for the finite
+    difference check of the restatement itself)."""
+    B = X.shape[0]
+    A = X @ W1.T
+    Hs = np.maximum(A, 0.0)
+    dY = Hs @ W2.T - T
+    dH = (dY @ W2) * (A > 0)
+    return dH.T @ X / B, dY.T @ Hs / B, 0.5 * float((dY * dY).sum()) / B
+
+
+def precond(W1, W2, zb_ring, EToE, EToF, geo, perm):
+    """Learned preconditioner output in ring order."""
+    X, s = features(zb_ring, EToE, EToF, geo, perm)
+    W1b, W2b = bf16(W1).astype(np.float64), bf16(W2).astype(np.float64)
+    Hs = bf16(np.maximum((bf16(X).astype(np.float64) @ W1b.T).astype(np.float32), 0.0)).astype(np.float64)
+    Y = (Hs @ W2b.T).astype(np.float32).astype(np.float64)
+    return zb_ring + s.astype(np.float64)[:, None] * Y
+
+
+def energy_gradients(W1, W2, r_ring, zb_ring, EToE, EToF, geo, perm, S_apply_ring):
+    """Gradients of the training loss for one residual (ring order): the
+    output gradient dY = s ((a/b) S z - r) (a = r.z, b = z.S z; the loss
+    -(r.z)|r.z| / (z.S z) has gradient 2|a|/b times this) chained through the
+    network, averaged over the K elements like the batch gradients.
+    Returns gW1, gW2 and the reported loss -(a^2)/b."""
+    X, s = features(zb_ring, EToE, EToF, geo, perm)
+    W1b, W2b = bf16(W1).astype(np.float64), bf16(W2).astype(np.float64)
+    Xb = bf16(X).astype(np.float64)
+    Hs = bf16(np.maximum((Xb @ W1b.T).astype(np.float32), 0.0)).astype(np.float64)
+    Y = (Hs @ W2b.T).astype(np.float32).astype(np.float64)
+    s64 = s.astype(np.float64)[:, None]
+    z = zb_ring + s64 * Y
+    w = S_apply_ring(z)
+    a = float((r_ring * z).sum())
+    b = float((z * w).sum())
+    dY = (s64 * ((a / b) * w - r_ring)).astype(np.float32).astype(np.float64)
+    dH = bf16(((dY @ W2b) * (Hs > 0)).astype(np.float32)).astype(np.float64)
+    K = X.shape[0]
+    return dH.T @ Xb / K, dY.T @ Hs / K, -(a * a) / b

@@ -1,0 +1,139 @@
+"""Learned element-block preconditioner on the GPU against its CPU
+restatement (oracle/lpc_oracle.py), through the C ABI:
+  * the BF16 training kernels' gradients on a random batch (rel L2 5e-3:
+    BF16 rounding of the hidden layer may fall differently where the FP32
+    sums differ in the last bit);
+  * the inference kernel (features, block Jacobi with FP32 blocks, network)
+    on a random residual (rel L2 1e-4 of z, 5e-3 of the network's part);
+  * the energy-loss gradients of one residual (rel L2 5e-3; the library's
+    S z runs in FP32 arithmetic, the oracle's in FP64);
+  * training on the method's own PCG residuals lowers the energy loss
+    below block Jacobi's, and a learned solve still ends at 1e-10 (through
+    its block-Jacobi fallback when the learned iteration does not get there).
+"""
+import numpy as np
+import pytest
+
+from conftest import rel_l2
+
+pytestmark = pytest.mark.gpu
+
+TAU = 1.0
+
+
+def _setup(n_interior=300, N=3, seed=5, hidden=32, capacity=0):
+    from hopefoam_gb300.mesh import delaunay_square, load_cubature
+    from hopefoam_gb300.poisson import PressureSolver
+    from oracle import oracle
+
+    mesh = delaunay_square(n_interior, seed=seed)
+    ps = PressureSolver(mesh, N, tau_coef=TAU)
+    ps.lpc_setup(hidden=hidden, seed=1, capacity=capacity)
+    orc = oracle.Oracle(mesh, N, load_cubature(3 * (N + 1)))
+    diag, off, _ = orc.ipdg_blocks(tau_coef=TAU)
+    return mesh, ps, orc, diag, off
+
+
+def _geometry(mesh):
+    v = mesh.VXY
+    xr, xs = (v[:, 1, 0] - v[:, 0, 0]) / 2, (v[:, 2, 0] - v[:, 0, 0]) / 2
+    yr, ys = (v[:, 1, 1] - v[:, 0, 1]) / 2, (v[:, 2, 1] - v[:, 0, 1]) / 2
+    J = xr * ys - xs * yr
+    return np.stack([ys / J, -yr / J, -xs / J, xr / J], axis=1)
+
+
+def _ring_tools(N):
+    from hopefoam_gb300.euler import reference_operators
+    from oracle import lpc_oracle as lo
+
+    ops = reference_operators(N)
+    ring = lo.ring_order(N)
+    perm = lo.rotation_perms(ops["r"], ops["s"], ring)
+    return ring, perm
+
+
+def _random_weights(ps, seed=3, scale=1.0):
+    rng = np.random.default_rng(seed)
+    W1 = (rng.standard_normal((ps.lpc_hidden, ps.lpc_F)) * np.sqrt(2.0 / ps.lpc_F)).astype(np.float32)
+    W2 = (rng.standard_normal((ps.Np, ps.lpc_hidden)) * scale / np.sqrt(ps.lpc_hidden)).astype(np.float32)
+    ps.lpc_set_weights(W1, W2)
+    return W1, W2
+
+
+def test_mlp_gradients_match_oracle(gpu_lib):
+    from oracle import lpc_oracle as lo
+
+    _, ps, _, _, _ = _setup(hidden=64)
+    W1, W2 = _random_weights(ps, seed=11, scale=0.5)
+    rng = np.random.default_rng(2)
+    B = 512
+    X = lo.bf16(rng.standard_normal((B, ps.lpc_F)).astype(np.float32))
+    T = rng.standard_normal((B, ps.Np)).astype(np.float32)
+    g1, g2, loss = ps.lpc_gradients(X, T)
+    o1, o2, oloss = lo.gradients(W1, W2, X, T)
+    assert rel_l2(g1, o1) < 5e-3, rel_l2(g1, o1)
+    assert rel_l2(g2, o2) < 5e-3, rel_l2(g2, o2)
+    assert abs(loss - oloss) <= 1e-4 * abs(oloss)
+
+
+def test_apply_matches_oracle(gpu_lib):
+    from oracle import lpc_oracle as lo
+
+    mesh, ps, _, diag, _ = _setup()
+    W1, W2 = _random_weights(ps, seed=4, scale=1.0)
+    ring, perm = _ring_tools(3)
+    rng = np.random.default_rng(9)
+    r = rng.standard_normal(ps.K * ps.Np)
+    z = ps.lpc_apply(r).reshape(ps.K, ps.Np)
+    zb = lo.block_jacobi32(-diag, r)
+    zb_ring = zb[:, ring]
+    z_ring = lo.precond(W1, W2, zb_ring, mesh.EToE, mesh.EToF, _geometry(mesh), perm)
+    z_ref = np.empty_like(z_ring)
+    z_ref[:, ring] = z_ring
+    assert rel_l2(z, z_ref) < 1e-4, rel_l2(z, z_ref)
+    zbr = np.empty_like(zb_ring)
+    zbr[:, ring] = zb_ring
+    assert rel_l2(z - zbr, z_ref - zbr) < 5e-3, rel_l2(z - zbr, z_ref - zbr)
+
+
+def test_energy_gradients_match_oracle(gpu_lib):
+    from oracle import lpc_oracle as lo
+
+    mesh, ps, orc, diag, off = _setup()
+    W1, W2 = _random_weights(ps, seed=6, scale=0.3)
+    ring, perm = _ring_tools(3)
+    rng = np.random.default_rng(10)
+    r = rng.standard_normal(ps.K * ps.Np)
+    g1, g2, loss = ps.lpc_energy_gradients(r)
+    Np = ps.Np
+
+    def S_ring(z_ring):
+        zr = np.empty_like(z_ring)
+        zr[:, ring] = z_ring
+        y = -orc.blk_apply(diag, off, zr.reshape(-1)).reshape(-1, Np)
+        return y[:, ring]
+
+    zb_ring = lo.block_jacobi32(-diag, r)[:, ring]
+    o1, o2, oloss = lo.energy_gradients(W1, W2, r.reshape(-1, Np)[:, ring], zb_ring, mesh.EToE, mesh.EToF,
+                                        _geometry(mesh), perm, S_ring)
+    assert rel_l2(g1, o1) < 5e-3, rel_l2(g1, o1)
+    assert rel_l2(g2, o2) < 5e-3, rel_l2(g2, o2)
+    assert abs(loss - oloss) <= 1e-5 * abs(oloss)
+
+
+def test_training_gains_and_solve(gpu_lib):
+    from hopefoam_gb300 import _lib as L
+    from hopefoam_gb300.poisson import poisson_rhs
+
+    mesh, ps, _, _, _ = _setup(n_interior=800, N=3, hidden=64, capacity=8 * 10)
+    rhs = [poisson_rhs(mesh, 3, seed=40 + i)[0] for i in range(8)]
+    n = ps.lpc_collect(rhs, snapshots=(1, 3, 8, 21, 55, 89, 144, 233, 377, 610))
+    assert n == 80
+    loss, loss_bj = ps.lpc_train(epochs=20, lr=1e-3, seed=0)
+    # the trained step removes more S-norm error than block Jacobi's
+    assert loss < 1.5 * loss_bj, (loss, loss_bj)
+    b = poisson_rhs(mesh, 3, seed=99)[0]
+    x, st = ps.solve(b, rtol=1e-10, pc=L.DG_PC_LEARNED, maxit=5000)
+    assert st["rel_residual"] <= 1e-10
+    xb, stb = ps.solve(b, rtol=1e-10, pc=L.DG_PC_BLOCK_JACOBI, maxit=5000)
+    assert rel_l2(x, xb) < 1e-8

@@ -178,6 +178,7 @@ def main():
     ap.add_argument("--order", type=int, default=5)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-poisson", action="store_true")
+    ap.add_argument("--no-batch", action="store_true")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
@@ -298,10 +299,45 @@ def main():
             line["poisson"] = poisson_bench(with_cpu=not args.no_cpu_baseline)
         except Exception as exc:  # reported, never hides the Euler line
             line["poisson"] = {"error": str(exc)}
+    if rank == 0 and not args.no_batch:
+        try:
+            line["batched"] = batch_bench(prec)
+        except Exception as exc:
+            line["batched"] = {"error": str(exc)}
     if rank == 0:
         print(json.dumps(line))
     if world > 1:
         torch.distributed.destroy_process_group()
+
+
+def batch_bench(prec, n_cases=512, nsteps=100):
+    """Batched workload: 512 seeded isentropic-vortex cases (strength U(1,6),
+    Mach U(0.1,0.8), N uniform in 2..6, K log-uniform in [800, 20000] as
+    m x m x 2 perturbed periodic grids), each at its own CFL-0.5 step, all
+    advanced nsteps LSERK4 steps in one CUDA-graph launch after autotuning."""
+    from hopefoam_gb300.batch import EulerBatch, batch_cases
+
+    t0 = time.perf_counter()
+    cases = batch_cases(n_cases, seed=0)
+    b = EulerBatch(cases)
+    setup_s = time.perf_counter() - t0
+    tune = b.tune(precision=prec, steps_per_trial=2)
+    b.run(nsteps, precision=prec)  # capture + warm-up launch
+    ms = b.run(nsteps, precision=prec)  # graph replay, device time
+    dof_stage = b.dofs * 5 * nsteps
+    bytes_stage = sum(g["ctx"].K * alg_bytes_per_elem_stage(g["order"]) for g in b.groups)
+    peak, peak_kind = peaks()
+    finite = all(bool(np.isfinite(q).all()) for q in b.states())
+    out = {"workload": "%d isentropic-vortex cases, N in 2..6, K in [800,20000] log-uniform, %d LSERK4 steps, "
+                       "one CUDA-graph launch" % (n_cases, nsteps),
+           "elements": b.elements, "dofs": b.dofs, "value": dof_stage / (ms * 1e-3), "unit": UNIT,
+           "ms": ms, "setup_s": setup_s, "tuning": tune, "state_finite": finite,
+           "roofline": {"bound": "hbm", "achieved": bytes_stage * 5 * nsteps / (ms * 1e-3) / 1e9, "peak": peak,
+                        "unit": "GB/s", "peak_kind": peak_kind},
+           "groups": [{"order": g["order"], "cases": len(g["cases"]), "K": g["ctx"].K} for g in b.groups]}
+    out["roofline"]["frac"] = out["roofline"]["achieved"] / peak
+    b.close()
+    return out
 
 
 def poisson_bench(with_cpu, n_interior=50000, order=4, tau_coef=1.0, rtol=1e-10):

@@ -36,6 +36,10 @@ class Info(ctypes.Structure):
                 ("device_bytes", ctypes.c_size_t)]
 
 
+class BatchTuning(ctypes.Structure):
+    _fields_ = [("concurrent", ctypes.c_int32), ("ms_sequential", ctypes.c_double), ("ms_concurrent", ctypes.c_double)]
+
+
 class SolveStats(ctypes.Structure):
     _fields_ = [("iterations", ctypes.c_int32), ("rel_residual", ctypes.c_double), ("ms", ctypes.c_double)]
 
@@ -70,6 +74,14 @@ SIGNATURES = {
     "dg_lpc_set_weights": (ctypes.c_int, [_vp, _fp, _fp]),
     "dg_lpc_gradients": (ctypes.c_int, [_vp, _fp, _fp, ctypes.c_int, _fp, _fp, _dp]),
     "dg_lpc_apply": (ctypes.c_int, [_vp, _dp, _dp]),
+    "dg_set_element_dt": (ctypes.c_int, [_vp, _dp]),
+    "dg_batch_create": (ctypes.c_int, [ctypes.POINTER(_vp), ctypes.c_int, ctypes.POINTER(_vp)]),
+    "dg_batch_destroy": (ctypes.c_int, [_vp]),
+    "dg_batch_last_error": (ctypes.c_char_p, [_vp]),
+    "dg_batch_tune": (ctypes.c_int, [_vp, ctypes.c_double, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                     ctypes.POINTER(BatchTuning)]),
+    "dg_batch_get_shape": (ctypes.c_int, [_vp, ctypes.c_int, _ip, _ip, _ip]),
+    "dg_batch_run": (ctypes.c_int, [_vp, ctypes.c_double, ctypes.c_int, ctypes.c_int, ctypes.c_int, _dp]),
 }
 DG_NOALLOC_MAX_VALUES = 524288
 

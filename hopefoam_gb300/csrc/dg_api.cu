@@ -58,6 +58,7 @@ int upload(dg_ctx* c, T** p, const std::vector<T>& h) {
 EulerArgs base_args(dg_ctx* c, int flux) {
     EulerArgs a;
     memset(&a, 0, sizeof(a));
+    a.dtk = c->d_dtk;
     a.geo = c->d_geo;
     a.conn = c->d_conn;
     a.btrace = c->d_btrace;
@@ -78,7 +79,7 @@ int run_stage(dg_ctx* c, const EulerArgs& a, int precision) {
 }
 
 // The split kernel reports bounded-wait timeouts in a device status word.
-int check_split_status(dg_ctx* c, int precision) {
+int split_status_impl(dg_ctx* c, int precision) {
     if (precision != DG_PREC_SPLIT) return DG_OK;
     int st = 0;
     DG_CUDA(c, cudaMemcpyAsync(&st, c->split.d_status, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
@@ -90,7 +91,7 @@ int check_split_status(dg_ctx* c, int precision) {
     return DG_OK;
 }
 
-int check_run_args(dg_ctx* c, int flux, int precision) {
+int run_args_impl(dg_ctx* c, int flux, int precision) {
     if (!c) return DG_ERR_ARG;
     if (flux != DG_FLUX_LF && flux != DG_FLUX_ROE) return fail(c, DG_ERR_ARG, "unknown flux");
     if (precision != DG_PREC_FP64 && precision != DG_PREC_SPLIT) return fail(c, DG_ERR_ARG, "unknown precision");
@@ -100,6 +101,24 @@ int check_run_args(dg_ctx* c, int flux, int precision) {
 }
 
 }  // namespace
+
+int check_split_status(dg_ctx* c, int precision) { return split_status_impl(c, precision); }
+int check_run_args(dg_ctx* c, int flux, int precision) { return run_args_impl(c, flux, precision); }
+
+int lserk_stage(dg_ctx* c, double dt, int stage, int flux, int precision) {
+    EulerArgs a = base_args(c, flux);
+    a.res = c->d_res;
+    a.mode = MODE_LSERK;
+    a.dt = dt;
+    a.qin = c->d_q[c->cur];
+    a.qout = c->d_q[c->cur ^ 1];
+    a.rka = kRk4a[stage];
+    a.rkb = kRk4b[stage];
+    int rc = run_stage(c, a, precision);
+    if (rc) return rc;
+    c->cur ^= 1;
+    return DG_OK;
+}
 
 extern "C" {
 
@@ -237,6 +256,23 @@ int dg_get_info(const dg_ctx* c, dg_info* info) {
 }
 
 const char* dg_last_error(const dg_ctx* c) { return c ? c->err.c_str() : "null context"; }
+
+int dg_set_element_dt(dg_ctx* c, const double* dtk_host) {
+    if (!c) return DG_ERR_ARG;
+    if (!dtk_host) {
+        c->d_dtk = nullptr;  // the buffer stays allocated for a later call
+        return DG_OK;
+    }
+    for (int k = 0; k < c->K; k++)
+        if (!(dtk_host[k] > 0) || !std::isfinite(dtk_host[k])) return fail(c, DG_ERR_ARG, "time-step factors must be positive");
+    if (!c->dtk_buf) {
+        int rc = dmalloc(c, &c->dtk_buf, (size_t)c->K);
+        if (rc) return rc;
+    }
+    DG_CUDA(c, cudaMemcpy(c->dtk_buf, dtk_host, (size_t)c->K * sizeof(double), cudaMemcpyHostToDevice));
+    c->d_dtk = c->dtk_buf;
+    return DG_OK;
+}
 
 int dg_upload_state_device(dg_ctx* c, const double* q_dev) {
     if (!c || !q_dev) return DG_ERR_ARG;

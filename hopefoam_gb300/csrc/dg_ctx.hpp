@@ -21,6 +21,8 @@ struct SplitPlan {
     size_t b2_offset = 0;     // in floats
     int* d_status = nullptr;  // bounded-wait timeout flag
     float* d_res32 = nullptr; // FP32 low-storage RK register
+    int ctas_per_sm = 1;      // launch shape (persistent grid = SMs used x CTAs per SM)
+    int sm_budget = 0;        // SMs the grid is sized for (0: all)
 };
 
 cudaError_t launch_euler_split(int N, const EulerArgs& a, const SplitPlan& plan, cudaStream_t s);
@@ -45,6 +47,8 @@ struct dg_ctx {
     int* d_conn = nullptr;
     int* d_ring = nullptr;
     double *d_Vg = nullptr, *d_Sr = nullptr, *d_Ss = nullptr, *d_Lift = nullptr, *d_If = nullptr;
+    double* d_dtk = nullptr;  // per-element time-step factors (dg_set_element_dt), null: none
+    double* dtk_buf = nullptr;
     int cur = 0;
     bool btrace_set = false;
     dgk::SplitPlan split;
@@ -56,6 +60,14 @@ struct dg_ctx {
 
 int split_setup(dg_ctx* c);
 void split_teardown(dg_ctx* c);
+
+// one LSERK4 stage (0..4) of a context on c->stream, no host synchronisation
+// (usable inside a stream capture); flips c->cur
+int lserk_stage(dg_ctx* c, double dt, int stage, int flux, int precision);
+// validates flux / precision / boundary state for stepping
+int check_run_args(dg_ctx* c, int flux, int precision);
+// reads and clears the split kernel's timeout flag (synchronises c->stream)
+int check_split_status(dg_ctx* c, int precision);
 
 // SIPG / PCG state (ipdg_api.cu)
 struct IpdgState;

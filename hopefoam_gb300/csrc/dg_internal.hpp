@@ -50,6 +50,7 @@ struct EulerArgs {
     int flux;
     int mode;
     double gamma, dt, rka, rkb;
+    const double* dtk;     // per-element time-step factors (null: 1); the step of element k is dt * dtk[k]
 };
 
 // launchers (return cudaError_t of the launch)

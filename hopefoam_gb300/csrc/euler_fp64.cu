@@ -178,15 +178,16 @@ __global__ void __launch_bounds__(256) euler_stage_fp64_kernel(EulerArgs a) {
         const double R = acc - accf;
         const size_t idx = (size_t)k0 * 4 * Np + it;
         const double q0 = qs[it];
+        const double dt = a.dtk ? a.dt * a.dtk[k0 + e] : a.dt;
         switch (a.mode) {
             case MODE_RHS: a.rhs[idx] = R; break;
             case MODE_LSERK: {
-                const double r = a.rka * a.res[idx] + a.dt * R;
+                const double r = a.rka * a.res[idx] + dt * R;
                 a.res[idx] = r;
                 a.qout[idx] = q0 + a.rkb * r;
             } break;
-            case MODE_EULER: a.qout[idx] = q0 + a.dt * R; break;
-            default: a.qout[idx] = 0.5 * a.qold[idx] + 0.5 * (q0 + a.dt * R); break;
+            case MODE_EULER: a.qout[idx] = q0 + dt * R; break;
+            default: a.qout[idx] = 0.5 * a.qold[idx] + 0.5 * (q0 + dt * R); break;
         }
     }
 }

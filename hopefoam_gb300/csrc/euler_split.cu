@@ -431,11 +431,12 @@ __global__ void __launch_bounds__(512, 1) euler_stage_split_kernel(SplitArgs sa)
         {
             const size_t base = (size_t)k0 * 4 * Np;
             const bool first = (a.rka == 0.0);
-            const float rka = (float)a.rka, dtf = (float)a.dt, rkb = (float)a.rkb;
+            const float rka = (float)a.rka, dtf0 = (float)a.dt, rkb = (float)a.rkb;
             for (int i = tid; i < ne * 4 * Np; i += blockDim.x) {
                 const float R = sRS[i];
                 const double q0 = sQ64[i];
                 const size_t idx = base + i;
+                const float dtf = a.dtk ? (float)(a.dt * a.dtk[k0 + i / (4 * Np)]) : dtf0;
                 switch (a.mode) {
                     case MODE_RHS: a.rhs[idx] = (double)R; break;
                     case MODE_LSERK: {
@@ -536,7 +537,9 @@ static cudaError_t launch_split_n(const EulerArgs& a, const SplitPlan& plan, cud
     sa.b2 = static_cast<const float*>(plan.d_ops) + plan.b2_offset;
     sa.status = plan.d_status;
     const int ntiles = (a.K + D::E - 1) / D::E;
-    const int grid = ntiles < plan.sms ? ntiles : plan.sms;
+    const int sms = (plan.sm_budget > 0 && plan.sm_budget < plan.sms) ? plan.sm_budget : plan.sms;
+    const int want = sms * (plan.ctas_per_sm > 0 ? plan.ctas_per_sm : 1);
+    const int grid = ntiles < want ? ntiles : want;
     euler_stage_split_kernel<N><<<grid, D::THREADS, D::SMEM, s>>>(sa);
     return cudaGetLastError();
 }

@@ -69,7 +69,8 @@ __device__ __forceinline__ bool grid_sum(double (&val)[NV], double* part, int nb
 }
 
 // CG scalars after a new residual r (recurrence) and preconditioned z:
-// beta (flexible, Polak-Ribiere: (r.z - r.z_old_precond) / r_old.z_old),
+// beta = (r.z - rzo) / r_old.z_old with rzo = r.z_old for the flexible
+// (Polak-Ribiere) form of a nonlinear preconditioner, 0 for the standard form;
 // stop test on r.r.  Thread 0 of the last CTA only.
 __device__ __forceinline__ void pcg_finish(PcgScalars* S, double rz_new, double rzo, double rr) {
     const double rz_old = S->rz;

@@ -139,6 +139,35 @@ int dg_ssprk2_step(dg_ctx* ctx, double dt, int nsteps, int flux, int precision);
  * (the reference uses a fixed dt, controlDict). */
 int dg_cfl_dt(dg_ctx* ctx, double cfl, double* dt);
 
+/* Per-element time-step factors: after this call the step of element k in
+ * dg_lserk4_step / dg_ssprk2_step / dg_batch_run is dt * dtk_host[k] (K
+ * positive values); NULL restores the uniform dt.  Lets one context hold many
+ * independent cases (disjoint meshes) that each keep their own CFL step.  No
+ * counterpart in the reference (one case per process, fixed deltaT). */
+int dg_set_element_dt(dg_ctx* ctx, const double* dtk_host);
+
+/* Batched Euler cases.  A batch holds groups (contexts, typically one per
+ * order, each over the disjoint meshes of its cases); dg_batch_run advances
+ * every group nsteps LSERK4 steps in one CUDA-graph launch (captured on the
+ * first run with these arguments, replayed after).  dg_batch_tune measures
+ * launch shapes on the live state (restored afterwards): CTAs per SM of the
+ * split kernel where two fit, and the groups run one after another on the
+ * whole GPU or side by side on SM shares proportional to their measured cost;
+ * the fastest is kept.  No counterpart in the reference.  The groups must not
+ * be used on their own streams while a dg_batch_run is in flight. */
+typedef struct dg_batch dg_batch;
+typedef struct dg_batch_tuning {
+    int32_t concurrent;      /* 1: groups side by side */
+    double ms_sequential;    /* per step */
+    double ms_concurrent;    /* per step */
+} dg_batch_tuning;
+int dg_batch_create(dg_ctx* const* groups, int n_groups, dg_batch** out);
+int dg_batch_destroy(dg_batch* batch);
+const char* dg_batch_last_error(const dg_batch* batch);
+int dg_batch_tune(dg_batch* batch, double dt, int flux, int precision, int steps_per_trial, dg_batch_tuning* result);
+int dg_batch_get_shape(const dg_batch* batch, int group, int* ctas_per_sm, int* sm_budget, int* concurrent);
+int dg_batch_run(dg_batch* batch, double dt, int nsteps, int flux, int precision, double* ms);
+
 /* Symmetric interior-penalty Laplacian of the pressure equation on the
  * context's mesh, penalty tau = tau_coef (N+1)^2 max(sJ/J) per face
  * (tau_coef = 20 is the reference's value,

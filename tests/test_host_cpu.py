@@ -103,3 +103,23 @@ def test_delaunay_and_fluent_meshes():
     assert m.K > 700 and (m.EToE < 0).sum() > 0
     g = golden_mesh("vortex0256")
     assert g.K == 256 and (g.EToE < 0).sum() == 32
+
+
+def test_batch_case_list_is_seeded():
+    from hopefoam_gb300.batch import batch_cases, concat_meshes
+    from hopefoam_gb300.mesh import periodic_square
+
+    a = batch_cases(n=64, seed=0)
+    b = batch_cases(n=64, seed=0)
+    assert a == b
+    assert {c["order"] for c in a} <= {2, 3, 4, 5, 6}
+    ks = [2 * c["m"] ** 2 for c in a]
+    assert min(ks) >= 2 * 20 ** 2 * 0.9 and max(ks) <= 20000 * 1.1
+    m1 = periodic_square(3, 3, seed=1)
+    m2 = periodic_square(4, 4, seed=2)
+    big = concat_meshes([m1, m2])
+    assert big.K == m1.K + m2.K
+    # the cases stay disconnected: every neighbour lies in the same case
+    own = np.repeat([0, 1], [m1.K, m2.K])
+    nb = big.EToE
+    assert np.all(own[nb] == own[:, None])

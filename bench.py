@@ -179,6 +179,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-poisson", action="store_true")
     ap.add_argument("--no-batch", action="store_true")
+    ap.add_argument("--no-configs", action="store_true")
+    ap.add_argument("--kh-steps", type=int, default=2)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
@@ -299,6 +301,12 @@ def main():
             line["poisson"] = poisson_bench(with_cpu=not args.no_cpu_baseline)
         except Exception as exc:  # reported, never hides the Euler line
             line["poisson"] = {"error": str(exc)}
+    if rank == 0 and not args.no_configs:
+        for key, fn in (("c1", c1_bench), ("c5", c5_bench)):
+            try:
+                line[key] = fn() if key == "c1" else fn(nsteps=args.kh_steps)
+            except Exception as exc:
+                line[key] = {"error": str(exc)}
     if rank == 0 and not args.no_batch:
         try:
             line["batched"] = batch_bench(prec)
@@ -308,6 +316,83 @@ def main():
         print(json.dumps(line))
     if world > 1:
         torch.distributed.destroy_process_group()
+
+
+def c1_bench(nsteps=100, order=3):
+    """The reference's CPU-sized case: isentropic vortex on the periodic
+    40x40x2 mesh of [0,10]^2 (K = 3200), N = 3, LF flux, LSERK4 at CFL 0.5,
+    100 steps on the FP64 path; L2 / Linf errors of density against the exact
+    advected vortex, and the throughput (the working set fits in L2: a latency
+    case, not a roofline case)."""
+    from hopefoam_gb300 import _lib as L
+    from hopefoam_gb300 import euler
+    from hopefoam_gb300.mesh import periodic_square
+
+    mesh = periodic_square(40, 40, 10.0, 10.0)
+    ops = euler.reference_operators(order)
+    x, y = euler.node_coords(mesh, ops["r"], ops["s"])
+    q0 = euler.isentropic_vortex(x, y, x0=5.0, y0=5.0)
+    ctx = euler.EulerContext(mesh, order)
+    ctx.upload(q0)
+    dt = ctx.cfl_dt(0.5)
+    ctx.lserk4(dt, 1, flux=L.DG_FLUX_LF, precision=L.DG_PREC_FP64)
+    ctx.upload(q0)
+    import torch
+
+    stream = torch.cuda.ExternalStream(ctx.stream)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    ctx.lserk4(dt, nsteps, flux=L.DG_FLUX_LF, precision=L.DG_PREC_FP64)
+    e1.record(stream)
+    e1.synchronize()
+    ms = e0.elapsed_time(e1)
+    q = ctx.download()
+    ex = euler.isentropic_vortex(x, y, t=nsteps * dt, x0=5.0, y0=5.0)
+    d = q[0] - ex[0]
+    ctx.close()
+    return {"workload": "isentropic vortex, periodic 40x40x2 (K=3200), N=3, LF, LSERK4 CFL 0.5, %d steps, FP64"
+                        % nsteps, "dt": dt, "t": nsteps * dt,
+            "rho_err_l2": float(np.linalg.norm(d) / np.linalg.norm(ex[0])), "rho_err_linf": float(np.abs(d).max()),
+            "value": mesh.K * ops["r"].size * 4 * 5 * nsteps / (ms * 1e-3), "unit": UNIT, "ms": ms}
+
+
+def c5_bench(nsteps=None, order=7, n=708):
+    """Large shear layer: periodic [0,1]^2, 708x708x2 = 1,002,528 triangles,
+    N = 7 (Np = 36), Kelvin-Helmholtz initial state, Roe flux, LSERK4 at CFL
+    0.5 on the FP64 path (the split path stops at N = 6); throughput over a few
+    steps (the 500-step run is a separate long job)."""
+    from hopefoam_gb300 import _lib as L
+    from hopefoam_gb300 import euler
+    from hopefoam_gb300.mesh import periodic_square
+
+    import torch
+
+    nsteps = nsteps or 2
+    t0 = time.perf_counter()
+    mesh = periodic_square(n, n, 1.0, 1.0)
+    ops = euler.reference_operators(order)
+    x, y = euler.node_coords(mesh, ops["r"], ops["s"])
+    q0 = euler.kelvin_helmholtz(x, y, seed=0)
+    ctx = euler.EulerContext(mesh, order)
+    ctx.upload(q0)
+    del x, y, q0
+    dt = ctx.cfl_dt(0.5)
+    setup_s = time.perf_counter() - t0
+    ctx.lserk4(dt, 1, flux=L.DG_FLUX_ROE, precision=L.DG_PREC_FP64)
+    stream = torch.cuda.ExternalStream(ctx.stream)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    ctx.lserk4(dt, nsteps, flux=L.DG_FLUX_ROE, precision=L.DG_PREC_FP64)
+    e1.record(stream)
+    e1.synchronize()
+    ms = e0.elapsed_time(e1)
+    q = ctx.download()
+    finite = bool(np.isfinite(q).all())
+    K, Np = mesh.K, ctx.Np
+    ctx.close()
+    return {"workload": "Kelvin-Helmholtz, periodic 708x708x2 (K=%d), N=7, Roe, LSERK4 CFL 0.5, FP64 path" % K,
+            "steps": nsteps, "ms_per_step": ms / nsteps, "value": K * Np * 4 * 5 * nsteps / (ms * 1e-3),
+            "unit": UNIT, "state_finite": finite, "setup_s": setup_s, "dt": dt}
 
 
 def batch_bench(prec, n_cases=512, nsteps=100):

@@ -67,7 +67,7 @@ struct SplitDims {
     static constexpr int SZ_AF = 2 * ROWS * NF * 4;   // face flux hi/lo
     static constexpr int SZ_QF = E * 4 * Np * 4;      // FP32 deltas of the tile state
     static constexpr int SZ_Q64 = E * 4 * Np * 8;     // FP64 tile state
-    static constexpr int SZ_QB = ROWS * 4;            // FP32 reference state per (element, variable)
+    static constexpr int SZ_QB = ROWS * 4 + ROWS * 8 + E * 4 * 4;  // reference state FP32 + FP64, FP32 metrics
     static constexpr int al(int x) { return (x + 1023) / 1024 * 1024; }
     static constexpr int OFF_B1 = 0;
     static constexpr int OFF_B2 = OFF_B1 + al(SZ_B1);
@@ -117,7 +117,9 @@ __global__ void __launch_bounds__(512, 1) euler_stage_split_kernel(SplitArgs sa)
     float* sAF = reinterpret_cast<float*>(smem + D::OFF_AF);
     float* sQF = reinterpret_cast<float*>(smem + D::OFF_QF);
     double* sQ64 = reinterpret_cast<double*>(smem + D::OFF_Q64);
-    float* sQB = reinterpret_cast<float*>(smem + D::OFF_QB);
+    float* sQB = reinterpret_cast<float*>(smem + D::OFF_QB);                      // [ROWS]
+    double* sQBd = reinterpret_cast<double*>(smem + D::OFF_QB + D::ROWS * 4);    // the same values in FP64
+    float* sGeo = reinterpret_cast<float*>(smem + D::OFF_QB + D::ROWS * 12);     // [E][rx, sx, ry, sy]
     float* sRS = reinterpret_cast<float*>(smem + D::OFF_AC);  // after GEMM2 completed
     uint64_t* bar1 = reinterpret_cast<uint64_t*>(smem + D::OFF_BAR);
     uint64_t* bar2 = bar1 + 1;  // [NBUF]
@@ -174,7 +176,11 @@ __global__ void __launch_bounds__(512, 1) euler_stage_split_kernel(SplitArgs sa)
         const int k0 = tile * E;
         const int ne = min(E, a.K - k0);
         // ---- (A) stage the tile: FP64 copy, per-(element, variable) reference
-        //      state (row mean, FP32), FP32 deltas, TF32 hi/lo of the deltas
+        //      state (mean of the three vertex values, rounded to FP32 and kept
+        //      in both precisions), FP32 metrics, FP32 deltas, TF32 hi/lo of the
+        //      deltas.  FP64 work is one subtraction and one conversion per
+        //      value: GB300 retires 2 FP64 operations per clock per SM, and
+        //      conversions there are the kernel's scarcest resource.
         {
             const double* qin = a.qin + (size_t)k0 * 4 * Np;
             for (int i = tid; i < ne * 4 * Np; i += blockDim.x) sQ64[i] = qin[i];
@@ -182,19 +188,22 @@ __global__ void __launch_bounds__(512, 1) euler_stage_split_kernel(SplitArgs sa)
         __syncthreads();
         if (tid < D::ROWS) {
             const int e = tid >> 2, v = tid & 3;
-            float s = 0.f;
+            float qb = 1.f;
             if (e < ne) {
-                const double* row = sQ64 + e * 4 * Np + v * Np;
-#pragma unroll 4
-                for (int p = 0; p < Np; p++) s += (float)row[p];
+                const double* row = sQ64 + e * 4 * Np + v * Np;  // ring order: vertices at 0, N, 2N
+                qb = (float)((row[0] + row[N] + row[2 * N]) * (1.0 / 3.0));
             }
-            sQB[tid] = e < ne ? s * (1.f / Np) : 1.f;
+            sQB[tid] = qb;
+            sQBd[tid] = (double)qb;
+        } else if (tid < D::ROWS + 4 * E) {
+            const int e = (tid - D::ROWS) >> 2, c = (tid - D::ROWS) & 3;
+            sGeo[tid - D::ROWS] = e < ne ? (float)a.geo[(size_t)(k0 + e) * 4 + c] : 0.f;
         }
         __syncthreads();
         for (int i = tid; i < ne * 4 * Np; i += blockDim.x) {
             const int e = i / (4 * Np), rem = i - e * 4 * Np, v = rem / Np, p = rem - v * Np;
             const int r = 4 * e + v;
-            const float d = (float)(sQ64[i] - (double)sQB[r]);
+            const float d = (float)(sQ64[i] - sQBd[r]);
             sQF[i] = d;
             float hi, lo;
             umma::split_tf32(d, hi, lo);
@@ -233,8 +242,12 @@ __global__ void __launch_bounds__(512, 1) euler_stage_split_kernel(SplitArgs sa)
                 const int k = k0 + (valid ? e : 0);
                 float own[4] = {0.f, 0.f, 0.f, 0.f}, nbr[4] = {0.f, 0.f, 0.f, 0.f};
                 float qbv[4];
+                double qbd[4];
 #pragma unroll
-                for (int v = 0; v < 4; v++) qbv[v] = sQB[4 * (valid ? e : 0) + v];
+                for (int v = 0; v < 4; v++) {
+                    qbv[v] = sQB[4 * (valid ? e : 0) + v];
+                    qbd[v] = sQBd[4 * (valid ? e : 0) + v];
+                }
                 if (valid && i < Nfp) {
                     const int pos = (f * N + i) % NB;
 #pragma unroll
@@ -246,11 +259,11 @@ __global__ void __launch_bounds__(512, 1) euler_stage_split_kernel(SplitArgs sa)
                         const int npos = (fn * N + jj) % NB;
                         const double* qn = a.qin + (size_t)nb * 4 * Np + npos;
 #pragma unroll
-                        for (int v = 0; v < 4; v++) nbr[v] = (float)(__ldg(qn + v * Np) - (double)qbv[v]);
+                        for (int v = 0; v < 4; v++) nbr[v] = (float)(__ldg(qn + v * Np) - qbd[v]);
                     } else {
                         const double* bt = a.btrace + (size_t)(-1 - c) * 4 * Nfp + i;
 #pragma unroll
-                        for (int v = 0; v < 4; v++) nbr[v] = (float)(__ldg(bt + v * Nfp) - (double)qbv[v]);
+                        for (int v = 0; v < 4; v++) nbr[v] = (float)(__ldg(bt + v * Nfp) - qbd[v]);
                     }
                 }
                 // interpolate both traces to Gauss point i (shuffles within the 8-lane group)
@@ -265,9 +278,9 @@ __global__ void __launch_bounds__(512, 1) euler_stage_split_kernel(SplitArgs sa)
                         dp[v] = fmaf(w, __shfl_sync(0xffffffffu, nbr[v], jn, 8), dp[v]);
                     }
                 }
-                const double* gk = a.geo + (size_t)k * 4;
+                const float* gk = sGeo + 4 * (valid ? e : 0);
                 float nx, ny, fsc;
-                face_normal_f(f, (float)gk[0], (float)gk[1], (float)gk[2], (float)gk[3], nx, ny, fsc);
+                face_normal_f(f, gk[0], gk[1], gk[2], gk[3], nx, ny, fsc);
                 const RefState b = make_ref(gamma, qbv);
                 const DeltaPrim pm = delta_prim(gamma, b, dm), pp = delta_prim(gamma, b, dp);
                 float F[4];
@@ -298,11 +311,7 @@ __global__ void __launch_bounds__(512, 1) euler_stage_split_kernel(SplitArgs sa)
 #pragma unroll
         for (int v = 0; v < 4; v++) qbe[v] = sQB[4 * my_e + v];
         const RefState bref = make_ref(gamma, qbe);
-        float rx = 0.f, sx = 0.f, ry = 0.f, sy = 0.f;
-        if (my_e < ne) {
-            const double* gk = a.geo + (size_t)(k0 + my_e) * 4;
-            rx = (float)gk[0]; sx = (float)gk[1]; ry = (float)gk[2]; sy = (float)gk[3];
-        }
+        const float rx = sGeo[4 * my_e], sx = sGeo[4 * my_e + 1], ry = sGeo[4 * my_e + 2], sy = sGeo[4 * my_e + 3];
         // ---- (C) wait for GEMM1, then the volume flux per chunk of cubature points
         bool ok = umma::mbar_wait(bar1, ph1, kWaitLimit);
         ph1 ^= 1;

@@ -33,6 +33,20 @@ def isentropic_vortex(x, y, t=0.0, beta=5.0, x0=5.0, y0=0.0, uinf=1.0, vinf=0.0,
     return np.stack([rho, rho * u, rho * v, E])
 
 
+def kelvin_helmholtz(x, y, seed=0, gamma=1.4, noise=1e-3):
+    """Periodic shear layer on [0,1]^2: rho = 2, u = 0.5 in |y - 0.5| < 0.25,
+    rho = 1, u = -0.5 outside; p = 2.5; v = 0.01 sin(4 pi x) plus seeded
+    uniform white noise of amplitude `noise` per node."""
+    inside = np.abs(y - 0.5) < 0.25
+    rho = np.where(inside, 2.0, 1.0)
+    u = np.where(inside, 0.5, -0.5)
+    rng = np.random.default_rng(seed)
+    v = 0.01 * np.sin(4.0 * np.pi * x) + noise * rng.uniform(-1.0, 1.0, size=np.shape(x))
+    p = np.full(np.shape(x), 2.5)
+    E = p / (gamma - 1.0) + 0.5 * rho * (u * u + v * v)
+    return np.stack([rho, rho * u, rho * v, E])
+
+
 def _check(ctx_handle, rc):
     if rc != L.DG_OK:
         msg = ""

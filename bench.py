@@ -41,14 +41,20 @@ def initial_state(mesh, order):
     return euler.isentropic_vortex(x, y, x0=5.0, y0=5.0), x, y
 
 
-def alg_bytes_per_elem_stage(order):
+def alg_bytes_per_elem_stage(order, split=True):
     """Minimum HBM bytes one element moves per RK stage in the fused kernel:
-    q read + q write + res read + res write (4 vars x Np x 8 B each), the three
-    neighbour face traces (3 x 4 x Nfp x 8 B), 4 FP64 metrics and 3 int32
-    neighbour words."""
+    q read + q write (4 vars x Np x 8 B each), the RK register read + write
+    (FP32 in the split path, FP64 in the FP64 path), the three neighbour face
+    traces (3 x 4 x Nfp x 8 B), 4 FP64 metrics and 3 int32 neighbour words."""
     Np = (order + 1) * (order + 2) // 2
     Nfp = order + 1
-    return 128 * Np + 96 * Nfp + 32 + 12
+    res = 4 if split else 8
+    return 4 * Np * (8 + 8 + 2 * res) + 96 * Nfp + 32 + 12
+
+
+# dram__bytes_read.sum + dram__bytes_write.sum of one stage launch at this
+# workload (profiles/euler_stage_split_N5.md)
+SPLIT_STAGE_TRAFFIC_N5 = 223.4e6
 
 
 class ClockSampler:
@@ -243,7 +249,7 @@ def main():
     value = dof_stage * world / (ms * 1e-3)
     launches = 5 * args.steps
     per_launch_s = ms * 1e-3 / launches
-    bpe = alg_bytes_per_elem_stage(order)
+    bpe = alg_bytes_per_elem_stage(order, split=(prec_name == "split"))
     achieved = bpe * mesh.K / per_launch_s / 1e9
     peak, peak_kind = peaks()
     qfin = ctx.download()
@@ -281,8 +287,11 @@ def main():
                                "CFL 0.5", "K": mesh.K, "order": order, "precision": prec_name,
                    "l2": "working set (q in/out + res) %.0f MB > 129 MB L2, no flush" % (3 * n * 8 / 1e6)},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "traffic": None, "peak_kind": peak_kind, "bytes_per_elem_stage": bpe,
-                     "kernel": "euler_stage_%s" % prec_name},
+                     "traffic": SPLIT_STAGE_TRAFFIC_N5 if (prec_name == "split" and order == 5 and args.nx == 256)
+                     else None, "peak_kind": peak_kind, "bytes_per_elem_stage": bpe,
+                     "kernel": "euler_stage_%s" % prec_name,
+                     "note": "the stage is bound by FP64 conversions and SIMT issue, not HBM "
+                             "(profiles/euler_stage_split_N5.md)"},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": n * 8, "d2h_bytes_per_step": n * 8},
         "gpu_launches": launches,
         "clocks": ck,
@@ -410,7 +419,7 @@ def batch_bench(prec, n_cases=512, nsteps=100):
     b.run(nsteps, precision=prec)  # capture + warm-up launch
     ms = b.run(nsteps, precision=prec)  # graph replay, device time
     dof_stage = b.dofs * 5 * nsteps
-    bytes_stage = sum(g["ctx"].K * alg_bytes_per_elem_stage(g["order"]) for g in b.groups)
+    bytes_stage = sum(g["ctx"].K * alg_bytes_per_elem_stage(g["order"], split=True) for g in b.groups)
     peak, peak_kind = peaks()
     finite = all(bool(np.isfinite(q).all()) for q in b.states())
     out = {"workload": "%d isentropic-vortex cases, N in 2..6, K in [800,20000] log-uniform, %d LSERK4 steps, "
@@ -451,7 +460,10 @@ def poisson_bench(with_cpu, n_interior=50000, order=4, tau_coef=1.0, rtol=1e-10)
     bytes_it = mesh.K * (8 * Np * 11 + 4 * Np * Np + 136)
     if st["iterations"]:
         per_it = st["ms"] * 1e-3 / st["iterations"]
-        out["bj_mixed"]["GBps_per_iteration"] = bytes_it / per_it / 1e9
+        peak, peak_kind = peaks()
+        out["bj_mixed"]["roofline"] = {"bound": "hbm", "achieved": bytes_it / per_it / 1e9, "peak": peak,
+                                       "unit": "GB/s", "frac": bytes_it / per_it / 1e9 / peak,
+                                       "bytes_per_iteration": bytes_it, "peak_kind": peak_kind}
     if with_cpu:
         from hopefoam_gb300.mesh import load_cubature
         from oracle import oracle

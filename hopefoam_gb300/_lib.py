@@ -13,6 +13,7 @@ ERR_NAMES = {0: "DG_OK", 1: "DG_ERR_ARG", 2: "DG_ERR_CUDA", 3: "DG_ERR_TIMEOUT",
 DG_FLUX_LF, DG_FLUX_ROE = 0, 1
 DG_PREC_FP64, DG_PREC_SPLIT = 0, 1
 DG_PC_NONE, DG_PC_BLOCK_JACOBI, DG_PC_LEARNED, DG_PC_LEARNED_ONLY = 0, 1, 2, 3
+DG_LPC_RELU, DG_LPC_LINEAR = 0, 1
 
 _dp = ctypes.POINTER(ctypes.c_double)
 _ip = ctypes.POINTER(ctypes.c_int32)
@@ -65,7 +66,7 @@ SIGNATURES = {
     "dg_pcg_solve": (ctypes.c_int, [_vp, _dp, _dp, ctypes.c_double, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                     ctypes.POINTER(SolveStats)]),
     "dg_euler_rhs_noalloc": (ctypes.c_int, [_vp, _vp, _vp, ctypes.c_int]),
-    "dg_lpc_setup": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_ulonglong, ctypes.c_int]),
+    "dg_lpc_setup": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_ulonglong, ctypes.c_int, ctypes.c_int]),
     "dg_lpc_add_residual": (ctypes.c_int, [_vp, _dp]),
     "dg_lpc_train": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_double, ctypes.c_ulonglong, _dp, _dp]),
     "dg_lpc_loss": (ctypes.c_int, [_vp, _dp, _dp, _dp]),

@@ -40,6 +40,7 @@ struct IpdgState {
     // learned preconditioner
     bool lpc_ready = false;
     int F = 0, H = 128;
+    int lpc_linear = 0;
     float *d_W1 = nullptr, *d_W2 = nullptr, *d_m1 = nullptr, *d_v1 = nullptr, *d_m2 = nullptr, *d_v2 = nullptr;
     float *d_g1 = nullptr, *d_g2 = nullptr;
     __nv_bfloat16 *d_W1b = nullptr, *d_W2b = nullptr;
@@ -110,12 +111,14 @@ void lpc_descr(dg_ctx* c, LpcNet& net, LpcFeatArgs& fa) {
     IpdgState* s = c->ipdg;
     net.F = s->F;
     net.H = s->H;
+    net.linear = s->lpc_linear;
     net.Np = c->Np;
     net.W1 = s->d_W1b;
     net.W2 = s->d_W2b;
     net.perm = s->d_perm;
     fa.K = c->K;
     fa.Np = c->Np;
+    fa.linear = s->lpc_linear;
     fa.zb = s->d_zb;
     fa.conn = c->d_conn;
     fa.geo = c->d_geo;
@@ -633,8 +636,9 @@ bool lpc_ok(dg_ctx* c) { return c && c->ipdg && c->ipdg->lpc_ready; }
 
 extern "C" {
 
-int dg_lpc_setup(dg_ctx* c, int hidden, unsigned long long seed, int capacity) {
+int dg_lpc_setup(dg_ctx* c, int hidden, unsigned long long seed, int capacity, int form) {
     if (!c || hidden < 8 || hidden > 256 || capacity < 0) return DG_ERR_ARG;
+    if (form != DG_LPC_RELU && form != DG_LPC_LINEAR) return DG_ERR_ARG;
     if (!c->ipdg || !c->ipdg->ready) return ifail(c, DG_ERR_ARG, "dg_ipdg_setup not called");
     IpdgState* s = c->ipdg;
     if (s->lpc_ready) return ifail(c, DG_ERR_ARG, "learned preconditioner already set up");
@@ -642,6 +646,7 @@ int dg_lpc_setup(dg_ctx* c, int hidden, unsigned long long seed, int capacity) {
     if (Np > 36) return ifail(c, DG_ERR_UNSUPPORTED, "learned preconditioner supports N <= 7");
     s->H = hidden;
     s->F = 4 * Np + 4;
+    s->lpc_linear = form == DG_LPC_LINEAR ? 1 : 0;
     const int n1 = s->H * s->F, n2 = Np * s->H;
     std::mt19937_64 rng(seed);
     std::normal_distribution<float> nd(0.f, 1.f);

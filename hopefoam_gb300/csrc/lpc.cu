@@ -49,10 +49,11 @@ __device__ __forceinline__ float lpc_element_features(const LpcFeatArgs& a, int 
     const double* g = a.geo + (size_t)k * 4;
     const double J = 1.0 / (g[0] * g[3] - g[1] * g[2]);
     const double h = sqrt(J);
-    x[4 * Np + 0] = (float)(g[0] * h);
-    x[4 * Np + 1] = (float)(g[1] * h);
-    x[4 * Np + 2] = (float)(g[2] * h);
-    x[4 * Np + 3] = (float)(g[3] * h);
+    const float gm = a.linear ? 0.f : 1.f;  // the linear form takes no (scale-free) metric input
+    x[4 * Np + 0] = gm * (float)(g[0] * h);
+    x[4 * Np + 1] = gm * (float)(g[1] * h);
+    x[4 * Np + 2] = gm * (float)(g[2] * h);
+    x[4 * Np + 3] = gm * (float)(g[3] * h);
     return s;
 }
 
@@ -97,7 +98,7 @@ __global__ void lpc_forward_kernel(LpcNet n, const __nv_bfloat16* __restrict__ X
             const __nv_bfloat16* w = n.W1 + (size_t)h * F;
             float acc = 0.f;
             for (int k = 0; k < F; k++) acc = fmaf(__bfloat162float(w[k]), xs[sidx * F + k], acc);
-            const float hv = bf(fmaxf(acc, 0.f));
+            const float hv = bf(n.linear ? acc : fmaxf(acc, 0.f));
             hs[sidx * H + h] = hv;
             Hs[(size_t)(b0 + sidx) * H + h] = hv;
         }
@@ -127,7 +128,7 @@ __global__ void lpc_dh_kernel(LpcNet n, const float* __restrict__ Hs, const floa
     for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < tot; t += (size_t)gridDim.x * blockDim.x) {
         const int b = (int)(t / H), h = (int)(t - (size_t)b * H);
         float acc = 0.f;
-        if (Hs[t] > 0.f)
+        if (n.linear || Hs[t] > 0.f)
             for (int j = 0; j < Np; j++) acc = fmaf(__bfloat162float(n.W2[(size_t)j * H + h]), dY[(size_t)b * Np + j], acc);
         dH[t] = bf(acc);
     }
@@ -195,7 +196,7 @@ __global__ void lpc_precond_kernel(LpcNet n, LpcFeatArgs a, const double* __rest
             const __nv_bfloat16* wr = w1 + h * F;
             float acc = 0.f;
             for (int i = 0; i < F; i++) acc = fmaf(__bfloat162float(wr[i]), x[i], acc);
-            const float hv = bf(fmaxf(acc, 0.f));
+            const float hv = bf(n.linear ? acc : fmaxf(acc, 0.f));
             for (int j = 0; j < Np; j++) y[j] = fmaf(__bfloat162float(w2[j * H + h]), hv, y[j]);
         }
         const double* zbk = a.zb + (size_t)k * Np;

@@ -15,6 +15,7 @@ namespace dgk {
 struct LpcNet {
     int F = 0;       // features = 4 Np + 4
     int H = 128;     // hidden width
+    int linear = 0;  // 1: identity activation and no metric features, so M(r) is linear in r
     int Np = 0;      // outputs
     const __nv_bfloat16* W1 = nullptr;  // H x F (BF16 copy used by the kernels)
     const __nv_bfloat16* W2 = nullptr;  // Np x H
@@ -23,6 +24,7 @@ struct LpcNet {
 
 struct LpcFeatArgs {
     int K, Np;
+    int linear;           // metric features zero (linear preconditioner)
     const double* zb;     // block-Jacobi output, ring order, K x Np
     const int* conn;      // packed neighbours
     const double* geo;    // metrics

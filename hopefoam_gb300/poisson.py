@@ -75,12 +75,15 @@ class PressureSolver:
     # ------------------------------------------------------------------
     # learned element-block preconditioner (DG_PC_LEARNED)
 
-    def lpc_setup(self, hidden=128, seed=0, capacity=0):
+    def lpc_setup(self, hidden=128, seed=0, capacity=0, linear=False):
         """Allocates the network (He-initialised W1, small W2) and room for
-        `capacity` training residual vectors on the device."""
+        `capacity` training residual vectors on the device.  linear=True:
+        identity activation without metric features (a linear preconditioner)."""
         self.lpc_hidden = int(hidden)
         self.lpc_F = 4 * self.Np + 4
-        _check(self.ctx.h, self.ctx.lib.dg_lpc_setup(self.ctx.h, int(hidden), int(seed), int(capacity)))
+        self.lpc_linear = bool(linear)
+        form = L.DG_LPC_LINEAR if linear else L.DG_LPC_RELU
+        _check(self.ctx.h, self.ctx.lib.dg_lpc_setup(self.ctx.h, int(hidden), int(seed), int(capacity), form))
 
     def lpc_add_residual(self, r):
         r = np.ascontiguousarray(r, np.float64).reshape(-1)

@@ -208,7 +208,10 @@ int dg_pcg_solve(dg_ctx* ctx, const double* b_host, double* x_host, double rtol,
  * solve does not reach rtol, dg_pcg_solve repeats it with block Jacobi from
  * the same initial guess and reports negative iterations.
  *   dg_lpc_setup: after dg_ipdg_setup; capacity = training residual vectors
- *     kept on the device.
+ *     kept on the device; form DG_LPC_RELU (the network above) or
+ *     DG_LPC_LINEAR (identity activation, no metric features: M is then a
+ *     learned linear coupling of the element's and its neighbours' block-Jacobi
+ *     outputs, z = P r + W2 W1 x, which keeps CG's optimality).
  *   dg_lpc_add_residual: one residual r = b - S x of the method's own PCG
  *     (host array, reference node order), stored scaled to r.P r = 1.
  *   dg_lpc_train: Adam epochs, one step per stored residual, minimising the
@@ -227,7 +230,8 @@ int dg_pcg_solve(dg_ctx* ctx, const double* b_host, double* x_host, double rtol,
  *     per output), a direct check of the backward kernels.
  *   dg_lpc_apply: z = M(r) once (host arrays of K*Np doubles, reference node
  *     order). */
-int dg_lpc_setup(dg_ctx* ctx, int hidden, unsigned long long seed, int capacity);
+enum { DG_LPC_RELU = 0, DG_LPC_LINEAR = 1 };
+int dg_lpc_setup(dg_ctx* ctx, int hidden, unsigned long long seed, int capacity, int form);
 int dg_lpc_add_residual(dg_ctx* ctx, const double* r_host);
 int dg_lpc_train(dg_ctx* ctx, int epochs, double lr, unsigned long long seed, double* final_loss,
                  double* final_loss_bj);

@@ -86,7 +86,7 @@ def block_jacobi32(S_blocks, r):
     return np.einsum("kij,kj->ki", P, rk).astype(np.float64)
 
 
-def features(zb_ring, EToE, EToF, geo, perm):
+def features(zb_ring, EToE, EToF, geo, perm, linear=False):
     """X (K x F, float32, before BF16 rounding) and s (K) from the block
     Jacobi output in ring order; geo = K x 4 (rx, sx, ry, sy); boundary faces
     (EToE[k, f] < 0) give zero blocks."""
@@ -105,29 +105,35 @@ def features(zb_ring, EToE, EToF, geo, perm):
     X = (Z.astype(np.float32) * (np.float32(1.0) / s)[:, None]).astype(np.float32)
     J = 1.0 / (geo[:, 0] * geo[:, 3] - geo[:, 1] * geo[:, 2])
     h = np.sqrt(J)
-    X = np.concatenate([X, (geo * h[:, None]).astype(np.float32)], axis=1)
+    g = np.zeros_like(geo) if linear else geo * h[:, None]
+    X = np.concatenate([X, g.astype(np.float32)], axis=1)
     return X, s
 
 
-def forward(W1, W2, X, T):
+def _act(A, linear):
+    return A if linear else np.maximum(A, 0.0)
+
+
+def forward(W1, W2, X, T, linear=False):
     """Hidden activations (BF16-rounded), output residuals dY and the loss
     (library convention: mean over samples and outputs of 0.5 dY^2)."""
     W1b, W2b, Xb = bf16(W1).astype(np.float64), bf16(W2).astype(np.float64), bf16(X).astype(np.float64)
     A = (Xb @ W1b.T).astype(np.float32)
-    Hs = bf16(np.maximum(A, 0.0)).astype(np.float64)
+    Hs = bf16(_act(A, linear)).astype(np.float64)
     Y = (Hs @ W2b.T).astype(np.float32)
     dY = (Y - np.asarray(T, np.float32)).astype(np.float64)
     loss = 0.5 * float((dY * dY).sum()) / (X.shape[0] * W2.shape[0])
     return Hs, dY, loss
 
 
-def gradients(W1, W2, X, T):
+def gradients(W1, W2, X, T, linear=False):
     """dL/dW1, dL/dW2 (L = sum_b 0.5 ||dY_b||^2 / B) under the kernel rounding
     rules, and the library's loss value."""
     B = X.shape[0]
-    Hs, dY, loss = forward(W1, W2, X, T)
+    Hs, dY, loss = forward(W1, W2, X, T, linear)
     W2b = bf16(W2).astype(np.float64)
-    dH = bf16(((dY @ W2b) * (Hs > 0)).astype(np.float32)).astype(np.float64)
+    mask = 1.0 if linear else (Hs > 0)
+    dH = bf16(((dY @ W2b) * mask).astype(np.float32)).astype(np.float64)
     Xb = bf16(X).astype(np.float64)
     gW2 = dY.T @ Hs / B
     gW1 = dH.T @ Xb / B
@@ -145,25 +151,25 @@ def gradients_exact(W1, W2, X, T):
     return dH.T @ X / B, dY.T @ Hs / B, 0.5 * float((dY * dY).sum()) / B
 
 
-def precond(W1, W2, zb_ring, EToE, EToF, geo, perm):
+def precond(W1, W2, zb_ring, EToE, EToF, geo, perm, linear=False):
     """Learned preconditioner output in ring order."""
-    X, s = features(zb_ring, EToE, EToF, geo, perm)
+    X, s = features(zb_ring, EToE, EToF, geo, perm, linear)
     W1b, W2b = bf16(W1).astype(np.float64), bf16(W2).astype(np.float64)
-    Hs = bf16(np.maximum((bf16(X).astype(np.float64) @ W1b.T).astype(np.float32), 0.0)).astype(np.float64)
+    Hs = bf16(_act((bf16(X).astype(np.float64) @ W1b.T).astype(np.float32), linear)).astype(np.float64)
     Y = (Hs @ W2b.T).astype(np.float32).astype(np.float64)
     return zb_ring + s.astype(np.float64)[:, None] * Y
 
 
-def energy_gradients(W1, W2, r_ring, zb_ring, EToE, EToF, geo, perm, S_apply_ring):
+def energy_gradients(W1, W2, r_ring, zb_ring, EToE, EToF, geo, perm, S_apply_ring, linear=False):
     """Gradients of the training loss for one residual (ring order): the
     output gradient dY = s ((a/b) S z - r) (a = r.z, b = z.S z; the loss
     -(r.z)|r.z| / (z.S z) has gradient 2|a|/b times this) chained through the
     network, averaged over the K elements like the batch gradients.
     Returns gW1, gW2 and the reported loss -(a^2)/b."""
-    X, s = features(zb_ring, EToE, EToF, geo, perm)
+    X, s = features(zb_ring, EToE, EToF, geo, perm, linear)
     W1b, W2b = bf16(W1).astype(np.float64), bf16(W2).astype(np.float64)
     Xb = bf16(X).astype(np.float64)
-    Hs = bf16(np.maximum((Xb @ W1b.T).astype(np.float32), 0.0)).astype(np.float64)
+    Hs = bf16(_act((Xb @ W1b.T).astype(np.float32), linear)).astype(np.float64)
     Y = (Hs @ W2b.T).astype(np.float32).astype(np.float64)
     s64 = s.astype(np.float64)[:, None]
     z = zb_ring + s64 * Y
@@ -171,6 +177,6 @@ def energy_gradients(W1, W2, r_ring, zb_ring, EToE, EToF, geo, perm, S_apply_rin
     a = float((r_ring * z).sum())
     b = float((z * w).sum())
     dY = (s64 * ((a / b) * w - r_ring)).astype(np.float32).astype(np.float64)
-    dH = bf16(((dY @ W2b) * (Hs > 0)).astype(np.float32)).astype(np.float64)
+    dH = bf16(((dY @ W2b) * (1.0 if linear else (Hs > 0))).astype(np.float32)).astype(np.float64)
     K = X.shape[0]
     return dH.T @ Xb / K, dY.T @ Hs / K, -(a * a) / b

@@ -21,14 +21,14 @@ pytestmark = pytest.mark.gpu
 TAU = 1.0
 
 
-def _setup(n_interior=300, N=3, seed=5, hidden=32, capacity=0):
+def _setup(n_interior=300, N=3, seed=5, hidden=32, capacity=0, linear=False):
     from hopefoam_gb300.mesh import delaunay_square, load_cubature
     from hopefoam_gb300.poisson import PressureSolver
     from oracle import oracle
 
     mesh = delaunay_square(n_interior, seed=seed)
     ps = PressureSolver(mesh, N, tau_coef=TAU)
-    ps.lpc_setup(hidden=hidden, seed=1, capacity=capacity)
+    ps.lpc_setup(hidden=hidden, seed=1, capacity=capacity, linear=linear)
     orc = oracle.Oracle(mesh, N, load_cubature(3 * (N + 1)))
     diag, off, _ = orc.ipdg_blocks(tau_coef=TAU)
     return mesh, ps, orc, diag, off
@@ -60,26 +60,28 @@ def _random_weights(ps, seed=3, scale=1.0):
     return W1, W2
 
 
-def test_mlp_gradients_match_oracle(gpu_lib):
+@pytest.mark.parametrize("linear", [False, True])
+def test_mlp_gradients_match_oracle(gpu_lib, linear):
     from oracle import lpc_oracle as lo
 
-    _, ps, _, _, _ = _setup(hidden=64)
+    _, ps, _, _, _ = _setup(hidden=64, linear=linear)
     W1, W2 = _random_weights(ps, seed=11, scale=0.5)
     rng = np.random.default_rng(2)
     B = 512
     X = lo.bf16(rng.standard_normal((B, ps.lpc_F)).astype(np.float32))
     T = rng.standard_normal((B, ps.Np)).astype(np.float32)
     g1, g2, loss = ps.lpc_gradients(X, T)
-    o1, o2, oloss = lo.gradients(W1, W2, X, T)
+    o1, o2, oloss = lo.gradients(W1, W2, X, T, linear=linear)
     assert rel_l2(g1, o1) < 5e-3, rel_l2(g1, o1)
     assert rel_l2(g2, o2) < 5e-3, rel_l2(g2, o2)
     assert abs(loss - oloss) <= 1e-4 * abs(oloss)
 
 
-def test_apply_matches_oracle(gpu_lib):
+@pytest.mark.parametrize("linear", [False, True])
+def test_apply_matches_oracle(gpu_lib, linear):
     from oracle import lpc_oracle as lo
 
-    mesh, ps, _, diag, _ = _setup()
+    mesh, ps, _, diag, _ = _setup(linear=linear)
     W1, W2 = _random_weights(ps, seed=4, scale=1.0)
     ring, perm = _ring_tools(3)
     rng = np.random.default_rng(9)
@@ -87,7 +89,7 @@ def test_apply_matches_oracle(gpu_lib):
     z = ps.lpc_apply(r).reshape(ps.K, ps.Np)
     zb = lo.block_jacobi32(-diag, r)
     zb_ring = zb[:, ring]
-    z_ring = lo.precond(W1, W2, zb_ring, mesh.EToE, mesh.EToF, _geometry(mesh), perm)
+    z_ring = lo.precond(W1, W2, zb_ring, mesh.EToE, mesh.EToF, _geometry(mesh), perm, linear=linear)
     z_ref = np.empty_like(z_ring)
     z_ref[:, ring] = z_ring
     assert rel_l2(z, z_ref) < 1e-4, rel_l2(z, z_ref)

@@ -464,6 +464,27 @@ def poisson_bench(with_cpu, n_interior=50000, order=4, tau_coef=1.0, rtol=1e-10)
         out["bj_mixed"]["roofline"] = {"bound": "hbm", "achieved": bytes_it / per_it / 1e9, "peak": peak,
                                        "unit": "GB/s", "frac": bytes_it / per_it / 1e9 / peak,
                                        "bytes_per_iteration": bytes_it, "peak_kind": peak_kind}
+    # learned preconditioner: trained on a small mesh from the solver's own
+    # residuals, transferred, then the learned solve alone and with its
+    # block-Jacobi fallback
+    try:
+        from hopefoam_gb300.poisson import train_learned_preconditioner
+
+        W1, W2, info = train_learned_preconditioner(order, tau_coef=tau_coef)
+        ps.lpc_setup(hidden=128, seed=0, capacity=0)
+        ps.lpc_set_weights(W1, W2)
+        _, stl = ps.solve(b, rtol=rtol, maxit=20000, pc=L.DG_PC_LEARNED_ONLY, precision=L.DG_PREC_SPLIT,
+                          raise_on_fail=False)
+        _, stf = ps.solve(b, rtol=rtol, maxit=20000, pc=L.DG_PC_LEARNED, precision=L.DG_PREC_SPLIT,
+                          raise_on_fail=False)
+        out["learned"] = {"training": info, "ms": stf["ms"], "iterations": stf["iterations"],
+                          "rel_residual": stf["rel_residual"],
+                          "learned_only": {"ms": stl["ms"], "iterations": stl["iterations"],
+                                           "rel_residual": stl["rel_residual"], "converged": stl["status"] == L.DG_OK},
+                          "speedup_vs_block_jacobi": st["ms"] / stf["ms"] if stf["ms"] else None,
+                          "note": "negative iterations: the learned solve stalled and block Jacobi finished it"}
+    except Exception as exc:
+        out["learned"] = {"error": str(exc)}
     if with_cpu:
         from hopefoam_gb300.mesh import load_cubature
         from oracle import oracle

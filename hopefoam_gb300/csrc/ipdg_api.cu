@@ -153,6 +153,11 @@ int run_cg(dg_ctx* c, const PcgVecs& v, bool fp32, double tol2, int limit, const
     int checks = 0;
     *stop = 0;
     *iters = 0;
+    // learned mode: give up when the best residual has not halved over a window
+    // (the caller then falls back to block Jacobi instead of running to maxit)
+    const int STALL = 256;
+    double best_rr = -1.0;
+    int best_it = 0;
     while (h.it < limit) {
         const int batch = std::min(CHECK, limit - h.it);
         for (int j = 0; j < batch; j++) {
@@ -162,6 +167,16 @@ int run_cg(dg_ctx* c, const PcgVecs& v, bool fp32, double tol2, int limit, const
         IP_CUDA(c, cudaStreamSynchronize(c->stream));
         checks++;
         if (h.done == 2) break;
+        if (v.zb && h.done == 0) {
+            if (best_rr < 0 || h.rr < 0.5 * best_rr) {
+                best_rr = h.rr;
+                best_it = h.it;
+            } else if (h.it - best_it >= STALL) {
+                *iters = h.it;
+                *stop = 3;
+                return DG_OK;
+            }
+        }
         const bool claim = h.done == 1;
         const bool periodic = refresh > 0 && checks % refresh == 0;
         if (!b || (!claim && !periodic)) {
@@ -472,7 +487,7 @@ int dg_pcg_solve(dg_ctx* c, const double* b_host, double* x_host, double rtol, i
     if (rc) return rc;
     cudaEventRecord(e1, c->stream);
     rel = bb > 0 ? std::sqrt(rr / bb) : 0.0;
-    if (pc == DG_PC_LEARNED && (!(rel == rel) || stop == 2 || rel > rtol)) {
+    if (pc == DG_PC_LEARNED && (!(rel == rel) || stop >= 2 || rel > rtol)) {
         // block-Jacobi PCG is the fallback: solve again from the caller's x0
         cudaEventDestroy(e0);
         cudaEventDestroy(e1);

@@ -165,3 +165,30 @@ class PressureSolver:
         z = np.empty_like(r)
         _check(self.ctx.h, self.ctx.lib.dg_lpc_apply(self.ctx.h, L.dptr(r), L.dptr(z)))
         return z
+
+
+def train_learned_preconditioner(order, tau_coef=1.0, n_interior=2000, n_rhs=16, epochs=(10, 10), lr=(1e-3, 3e-4),
+                                 snapshots=(1, 2, 3, 5, 8, 13, 21, 34, 55, 89, 144, 233, 377), linear=False,
+                                 seed=11):
+    """Trains the learned preconditioner on a small seeded Delaunay mesh from
+    residuals of this solver's own block-Jacobi PCG (the network is local and
+    scale-free, so the weights transfer to larger meshes).  Returns
+    (W1, W2, info)."""
+    import time
+
+    from .mesh import delaunay_square
+
+    t0 = time.perf_counter()
+    mesh = delaunay_square(n_interior, seed=seed)
+    ps = PressureSolver(mesh, order, tau_coef=tau_coef)
+    ps.lpc_setup(hidden=128, seed=0, capacity=n_rhs * len(snapshots), linear=linear)
+    rhs = [poisson_rhs(mesh, order, seed=100 + i)[0] for i in range(n_rhs)]
+    n = ps.lpc_collect(rhs, snapshots=snapshots)
+    losses = []
+    for i, (ep, rate) in enumerate(zip(epochs, lr)):
+        losses.append(ps.lpc_train(epochs=ep, lr=rate, seed=i))
+    W1, W2 = ps.lpc_weights()
+    info = {"train_K": ps.K, "residuals": n, "loss": losses[-1][0], "loss_block_jacobi": losses[-1][1],
+            "seconds": time.perf_counter() - t0, "linear": bool(linear)}
+    ps.ctx.close()
+    return W1, W2, info

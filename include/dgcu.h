@@ -204,9 +204,11 @@ int dg_pcg_solve(dg_ctx* ctx, const double* b_host, double* x_host, double rtol,
  * block-Jacobi outputs of the element and its three neighbours (neighbours
  * rotated so the shared face is their face 0) and four scaled metrics, s
  * their RMS; W1 (hidden x F), W2 (Np x hidden), F = 4 Np + 4, BF16 for the
- * kernels, FP32 master copies.  The solve is flexible CG; when a learned
- * solve does not reach rtol, dg_pcg_solve repeats it with block Jacobi from
- * the same initial guess and reports negative iterations.
+ * kernels, FP32 master copies.  The solve is flexible CG; a learned solve
+ * whose best residual has not halved within 256 iterations stops early, and
+ * when a learned solve does not reach rtol dg_pcg_solve (DG_PC_LEARNED)
+ * repeats it with block Jacobi from the same initial guess and reports
+ * negative iterations.
  *   dg_lpc_setup: after dg_ipdg_setup; capacity = training residual vectors
  *     kept on the device; form DG_LPC_RELU (the network above) or
  *     DG_LPC_LINEAR (identity activation, no metric features: M is then a

@@ -452,9 +452,8 @@ def poisson_bench(with_cpu, n_interior=50000, order=4, tau_coef=1.0, rtol=1e-10)
     ps.solve(b, rtol=1e-4, precision=L.DG_PREC_SPLIT, raise_on_fail=False)  # warm-up
     x, st = ps.solve(b, rtol=rtol, precision=L.DG_PREC_SPLIT, raise_on_fail=False)
     out["bj_mixed"] = {"ms": st["ms"], "iterations": st["iterations"], "rel_residual": st["rel_residual"]}
-    x, st64 = ps.solve(b, rtol=rtol, precision=L.DG_PREC_FP64, maxit=4000, raise_on_fail=False)
-    out["bj_fp64"] = {"ms": st64["ms"], "iterations": st64["iterations"], "rel_residual": st64["rel_residual"],
-                      "note": "capped at 4000 iterations" if st64["status"] != L.DG_OK else ""}
+    x, st64 = ps.solve(b, rtol=rtol, precision=L.DG_PREC_FP64, maxit=20000, raise_on_fail=False)
+    out["bj_fp64"] = {"ms": st64["ms"], "iterations": st64["iterations"], "rel_residual": st64["rel_residual"]}
     # algorithmic bytes per iteration (FP64 vectors x 11 passes, FP32 block inverse)
     Np = ps.Np
     bytes_it = mesh.K * (8 * Np * 11 + 4 * Np * Np + 136)

@@ -488,11 +488,18 @@ int dg_pcg_solve(dg_ctx* c, const double* b_host, double* x_host, double rtol, i
     cudaEventRecord(e1, c->stream);
     rel = bb > 0 ? std::sqrt(rr / bb) : 0.0;
     if (pc == DG_PC_LEARNED && (!(rel == rel) || stop >= 2 || rel > rtol)) {
-        // block-Jacobi PCG is the fallback: solve again from the caller's x0
+        // block-Jacobi PCG is the fallback: solve again from the caller's x0;
+        // the reported time includes the learned attempt
+        IP_CUDA(c, cudaStreamSynchronize(c->stream));
+        float ms_learned = 0;
+        cudaEventElapsedTime(&ms_learned, e0, e1);
         cudaEventDestroy(e0);
         cudaEventDestroy(e1);
         int rc2 = dg_pcg_solve(c, b_host, x_host, rtol, maxit, DG_PC_BLOCK_JACOBI, precision, stats);
-        if (stats) stats->iterations = -stats->iterations;  // negative: the learned solve fell back
+        if (stats) {
+            stats->iterations = -stats->iterations;  // negative: the learned solve fell back
+            stats->ms += ms_learned;
+        }
         return rc2;
     }
     IP_CUDA(c, launch_permute(s->d_x, s->d_z, c->d_ring, c->K, c->Np, false, c->stream));

@@ -208,7 +208,7 @@ int dg_pcg_solve(dg_ctx* ctx, const double* b_host, double* x_host, double rtol,
  * whose best residual has not halved within 256 iterations stops early, and
  * when a learned solve does not reach rtol dg_pcg_solve (DG_PC_LEARNED)
  * repeats it with block Jacobi from the same initial guess and reports
- * negative iterations.
+ * negative iterations (the block-Jacobi count) and the time of both attempts.
  *   dg_lpc_setup: after dg_ipdg_setup; capacity = training residual vectors
  *     kept on the device; form DG_LPC_RELU (the network above) or
  *     DG_LPC_LINEAR (identity activation, no metric features: M is then a

@@ -254,6 +254,23 @@ def main():
     peak, peak_kind = peaks()
     qfin = ctx.download()
     finite = bool(np.isfinite(qfin).all())
+    # precision of the timed path: one LSERK4 step from the same state against the FP64
+    # path (itself equal to the oracle to 1e-12, tests/test_euler_gpu.py)
+    precision_check = None
+    if prec_name == "split":
+        ctx.upload(qfin)
+        ctx.lserk4(dt, 1, flux=L.DG_FLUX_LF, precision=L.DG_PREC_FP64)
+        q64 = ctx.download()
+        ctx.upload(qfin)
+        ctx.lserk4(dt, 1, flux=L.DG_FLUX_LF, precision=prec)
+        qsp = ctx.download()
+        d = (qsp - q64).reshape(4, -1)
+        r64 = q64.reshape(4, -1)
+        precision_check = {"against": "FP64 path, one LSERK4 step from the benchmark state",
+                           "rel_l2": float(np.linalg.norm(d) / np.linalg.norm(r64)),
+                           "rel_linf": float(np.abs(d).max() / np.abs(r64).max()),
+                           "rel_l2_per_variable": [float(np.linalg.norm(d[v]) / np.linalg.norm(r64[v]))
+                                                   for v in range(4)]}
 
     # end to end through the public API with pinned host buffers
     n = 4 * mesh.K * Np
@@ -296,6 +313,7 @@ def main():
         "gpu_launches": launches,
         "clocks": ck,
         "state_finite": finite,
+        "precision_check": precision_check,
     }
     if rank == 0 and not args.no_cpu_baseline:
         from oracle import oracle

@@ -106,7 +106,9 @@ __device__ __forceinline__ void roe_flux(T gamma, T nx, T ny, const T qO[4], con
 }
 
 // ---------------------------------------------------------------------------
-// Delta (product-rule) forms used by the split-precision path.  With a
+// Delta (product-rule) forms used by the split-precision path (FP32; the
+// divisions use the fast approximate form: their results carry FP32-level
+// relative error, inside the path's error budget).  With a
 // per-element reference state qb and q = qb + dq, the weak right-hand side
 // satisfies R(F) = R(F - F(qb)) exactly (the discrete divergence of a
 // constant flux cancels against its own surface term), so the kernels feed the
@@ -123,8 +125,9 @@ __device__ __forceinline__ RefState make_ref(float gamma, const float qb[4]) {
     b.m = qb[1];
     b.n = qb[2];
     b.E = qb[3];
-    b.u = b.m / b.rho;
-    b.v = b.n / b.rho;
+    const float ir = __fdividef(1.f, b.rho);
+    b.u = b.m * ir;
+    b.v = b.n * ir;
     b.p = (gamma - 1.f) * (b.E - 0.5f * (b.m * b.u + b.n * b.v));
     b.H = b.E + b.p;
     return b;
@@ -139,8 +142,9 @@ __device__ __forceinline__ DeltaPrim delta_prim(float gamma, const RefState& b, 
     DeltaPrim d;
     d.rho = b.rho + dq[0];
     const float m = b.m + dq[1], n = b.n + dq[2];
-    d.du = (dq[1] - b.u * dq[0]) / d.rho;
-    d.dv = (dq[2] - b.v * dq[0]) / d.rho;
+    const float ir = __fdividef(1.f, d.rho);
+    d.du = (dq[1] - b.u * dq[0]) * ir;
+    d.dv = (dq[2] - b.v * dq[0]) * ir;
     d.u = b.u + d.du;
     d.v = b.v + d.dv;
     const float dK = 0.5f * (dq[1] * b.u + m * d.du + dq[2] * b.v + n * d.dv);
@@ -165,7 +169,7 @@ __device__ __forceinline__ void flux_delta(const RefState& b, const float dq[4],
 
 __device__ __forceinline__ float wave_speed_delta(float gamma, float nx, float ny, const RefState& b, const DeltaPrim& d) {
     const float p = b.p + d.dp;
-    return fabsf(d.u * nx + d.v * ny) + sqrtf(fabsf(gamma * p / d.rho));
+    return fabsf(d.u * nx + d.v * ny) + sqrtf(fabsf(__fdividef(gamma * p, d.rho)));
 }
 
 // n.F*(q-, q+) - n.F(qb), Lax-Friedrichs

@@ -124,6 +124,7 @@ __global__ void __launch_bounds__(512, 1) euler_stage_split_kernel(SplitArgs sa)
     uint64_t* bar1 = reinterpret_cast<uint64_t*>(smem + D::OFF_BAR);
     uint64_t* bar2 = bar1 + 1;  // [NBUF]
     uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bar1 + 3);
+    volatile int* fail_flag = reinterpret_cast<volatile int*>(bar1 + 4);  // set by thread 0, read after a barrier
 
     const EulerArgs& a = sa.e;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -142,6 +143,7 @@ __global__ void __launch_bounds__(512, 1) euler_stage_split_kernel(SplitArgs sa)
         for (int i = tid; i < D::SZ_AF / 4; i += blockDim.x) sAF[i] = 0.f;
     }
     if (tid == 0) {
+        *fail_flag = 0;
         umma::mbar_init(bar1, 1);
         for (int b = 0; b < D::NBUF; b++) umma::mbar_init(bar2 + b, 1);
         umma::fence_mbar_init();
@@ -349,11 +351,18 @@ __global__ void __launch_bounds__(512, 1) euler_stage_split_kernel(SplitArgs sa)
                     for (int v = 0; v < 4; v++) fr[0][v] = fs[0][v] = 0.f;
                 }
             }
-            // the MMAs that last read this buffer must be complete
-            if (ch >= D::NBUF) {
-                ok = umma::mbar_wait(bar2 + buf, ph2[buf], kWaitLimit);
-                ph2[buf] ^= 1;
-                if (__syncthreads_or(!ok)) { failed = true; break; }
+            if constexpr (D::NBUF >= 2) {
+                // buffer reuse: thread 0 confirmed, before the previous chunk's
+                // barrier, that the MMAs which last read this buffer are complete
+                if (ch >= D::NBUF) ph2[buf] ^= 1;
+            } else {
+                // one buffer: the previous chunk's MMAs are issued after its barrier,
+                // so every thread waits for them here
+                if (ch >= D::NBUF) {
+                    ok = umma::mbar_wait(bar2 + buf, ph2[buf], kWaitLimit);
+                    ph2[buf] ^= 1;
+                    if (__syncthreads_or(!ok)) { failed = true; break; }
+                }
             }
             {
                 const int gl = sub * 4 + my_v;
@@ -373,8 +382,17 @@ __global__ void __launch_bounds__(512, 1) euler_stage_split_kernel(SplitArgs sa)
             }
             umma::fence_async_smem();
             umma::fence_before_sync();
+            if constexpr (D::NBUF >= 2) {
+                // chunk ch + 1 reuses the buffer of chunk ch + 1 - NBUF <= ch - 1, whose
+                // MMAs were issued before this point
+                if (tid == 0 && ch + 1 < D::NCH && ch + 1 >= D::NBUF) {
+                    const int nb = (ch + 1) % D::NBUF;
+                    if (!umma::mbar_wait(bar2 + nb, ph2[nb], kWaitLimit)) *fail_flag = 1;
+                }
+            }
             __syncthreads();
             umma::fence_after_sync();
+            if (*fail_flag) { failed = true; break; }
             if (tid == 0) {
                 constexpr uint32_t sboA = (KC / 4) * 128, sboB = (KP2 / 4) * 128;
                 const uint32_t aC = aAC + buf * STRIDE_AC;
@@ -409,6 +427,19 @@ __global__ void __launch_bounds__(512, 1) euler_stage_split_kernel(SplitArgs sa)
             }
         }
         if (failed) break;
+        // the epilogue's RK register values, loaded while the last MMAs run
+        constexpr int EPI = (E * 4 * Np + D::THREADS - 1) / D::THREADS;
+        const bool first = (a.rka == 0.0);
+        float resp[EPI];
+        {
+            const size_t base = (size_t)k0 * 4 * Np;
+            const bool need = a.mode == MODE_LSERK && !first;
+#pragma unroll
+            for (int j = 0; j < EPI; j++) {
+                const int i = tid + j * D::THREADS;
+                resp[j] = (need && i < ne * 4 * Np) ? __ldg(sa.res32 + base + i) : 0.f;
+            }
+        }
         // outstanding commits: the last NBUF chunks (one per buffer)
 #pragma unroll
         for (int b = 0; b < D::NBUF; b++) {
@@ -439,9 +470,11 @@ __global__ void __launch_bounds__(512, 1) euler_stage_split_kernel(SplitArgs sa)
         __syncthreads();
         {
             const size_t base = (size_t)k0 * 4 * Np;
-            const bool first = (a.rka == 0.0);
             const float rka = (float)a.rka, dtf0 = (float)a.dt, rkb = (float)a.rkb;
-            for (int i = tid; i < ne * 4 * Np; i += blockDim.x) {
+#pragma unroll
+            for (int j = 0; j < EPI; j++) {
+                const int i = tid + j * D::THREADS;
+                if (i >= ne * 4 * Np) break;
                 const float R = sRS[i];
                 const double q0 = sQ64[i];
                 const size_t idx = base + i;
@@ -449,7 +482,7 @@ __global__ void __launch_bounds__(512, 1) euler_stage_split_kernel(SplitArgs sa)
                 switch (a.mode) {
                     case MODE_RHS: a.rhs[idx] = (double)R; break;
                     case MODE_LSERK: {
-                        const float r = first ? dtf * R : fmaf(rka, sa.res32[idx], dtf * R);
+                        const float r = first ? dtf * R : fmaf(rka, resp[j], dtf * R);
                         sa.res32_out[idx] = r;
                         a.qout[idx] = q0 + (double)(rkb * r);
                     } break;

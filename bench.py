@@ -488,7 +488,7 @@ def poisson_bench(with_cpu, n_interior=50000, order=4, tau_coef=1.0, rtol=1e-10)
         from hopefoam_gb300.poisson import train_learned_preconditioner
 
         W1, W2, info = train_learned_preconditioner(order, tau_coef=tau_coef)
-        ps.lpc_setup(hidden=128, seed=0, capacity=0)
+        ps.lpc_setup(hidden=info["hidden"], seed=0, capacity=0, form=info["form"])
         ps.lpc_set_weights(W1, W2)
         _, stl = ps.solve(b, rtol=rtol, maxit=20000, pc=L.DG_PC_LEARNED_ONLY, precision=L.DG_PREC_SPLIT,
                           raise_on_fail=False)

@@ -424,11 +424,12 @@ __global__ void __launch_bounds__(RowDims<NP>::THREADS) pcg_init_kernel(PcgVecs 
             else {
                 v.z[idx] = z;
                 rz += ri * z;
-                if (i == 0) zs0[e] = z;
             }
+            if (i == 0) zs0[e] = z;
+            if (v.r32) v.r32[idx] = rs32[e][i];
             rr += ri * ri;
         }
-        if (v.dz && !v.zb) {
+        if (v.dz) {  // learned mode: the mirror of P r, completed by the learned kernel
             __syncthreads();
             if (act) v.dz[idx] = (float)(z - zs0[e]);
         }
@@ -489,14 +490,16 @@ __global__ void __launch_bounds__(RowDims<NP>::THREADS) pcg_update_kernel(PcgVec
             ri = v.r[idx] - alpha * v.Ap[idx];
             v.r[idx] = ri;
             if (v.P64) rs[e][i] = ri;
-            else rs32[e][i] = (float)ri;
+            if (!v.P64 || v.r32) rs32[e][i] = (float)ri;
         }
         __syncthreads();
         if (act) {
             z = v.P64 ? bj_rowg<NP>(v.P64, rs[e], grp) : bj_rowg<NP>(v.P32, rs32[e], grp);
             rr += ri * ri;
+            if (v.r32) v.r32[idx] = rs32[e][i];
             if (v.zb) {
                 v.zb[idx] = z;  // the learned kernel forms z and finishes the iteration
+                if (i == 0) zs0[e] = z;
             } else {
                 // block Jacobi is a fixed linear preconditioner: the standard
                 // (Fletcher-Reeves) beta needs no r.z_old, and skipping the
@@ -507,7 +510,7 @@ __global__ void __launch_bounds__(RowDims<NP>::THREADS) pcg_update_kernel(PcgVec
                 if (i == 0) zs0[e] = z;
             }
         }
-        if (v.dz && !v.zb) {
+        if (v.dz) {  // learned mode: the mirror of P r, completed by the learned kernel
             __syncthreads();
             if (act) v.dz[idx] = (float)(z - zs0[e]);
         }
@@ -686,8 +689,13 @@ static cudaError_t pcg_precondition(const IpdgArgs& a, const PcgVecs& v, const L
     ROWS_DISPATCH(a.Np, (pcg_init_kernel<NP><<<rows_grid<NP>(a), RowDims<NP>::THREADS, 0, s>>>(v, a.K, mode)));
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess || !v.zb) return e;
-    return launch_lpc_precond(*lpc, *fa, v.r, v.z, mode == 0 ? LPC_PCG_INIT : LPC_PCG_REFRESH, v.S, v.part, v.dz,
-                              s);
+    const int lmode = mode == 0 ? LPC_PCG_INIT : LPC_PCG_REFRESH;
+    if (lpc->sw) {
+        e = launch_schwarz_local(*lpc->sw, v.r, v.r32, lpc->U, nullptr, s);
+        if (e != cudaSuccess) return e;
+        return launch_schwarz_collect(*lpc->sw, v.zb, lpc->U, v.r, v.z, v.dz, lmode, v.S, v.part, s);
+    }
+    return launch_lpc_precond(*lpc, *fa, v.r, v.z, lmode, v.S, v.part, v.dz, s);
 }
 
 cudaError_t launch_pcg_init(const IpdgArgs& a, const PcgVecs& v, const LpcNet* lpc, const LpcFeatArgs* fa,
@@ -708,7 +716,15 @@ cudaError_t launch_pcg_iteration(const IpdgArgs& a, const PcgVecs& v, bool fp32,
     ROWS_DISPATCH(a.Np,
                   (pcg_update_kernel<NP><<<rows_grid<NP>(a), RowDims<NP>::THREADS, 0, s>>>(v, a.K, parity)));
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
-    if (v.zb) e = launch_lpc_precond(*lpc, *fa, v.r, v.z, LPC_PCG_ITERATION, v.S, v.part, v.dz, s);
+    if (v.zb) {
+        if (lpc->sw) {
+            e = launch_schwarz_local(*lpc->sw, v.r, v.r32, lpc->U, &v.S->done, s);
+            if (e == cudaSuccess)
+                e = launch_schwarz_collect(*lpc->sw, v.zb, lpc->U, v.r, v.z, v.dz, LPC_PCG_ITERATION, v.S, v.part, s);
+        } else {
+            e = launch_lpc_precond(*lpc, *fa, v.r, v.z, LPC_PCG_ITERATION, v.S, v.part, v.dz, s);
+        }
+    }
     return e;
 }
 

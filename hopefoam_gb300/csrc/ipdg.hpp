@@ -64,6 +64,7 @@ struct PcgVecs {
     // from the FP64 vectors
     float* dz;
     float* dp[2];
+    float* r32;                  // learned Schwarz mode: FP32 copy of r for the learned kernel (else null)
 };
 
 // largest grid of the PCG kernels (sizes the partials)

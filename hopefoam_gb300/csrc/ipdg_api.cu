@@ -31,6 +31,7 @@ struct IpdgState {
            *d_Ap = nullptr, *d_part = nullptr;
     double* d_ppart = nullptr;  // [3][nmax] partials of the PCG grid-wide sums
     float *d_dz = nullptr, *d_dp = nullptr, *d_dp2 = nullptr;  // FP32 offset mirrors of z and p
+    float* d_r32 = nullptr;      // FP32 copy of r (learned Schwarz mode)
     int nmax = 0;
     int sms = 1;
     PcgScalars* d_S = nullptr;
@@ -41,6 +42,13 @@ struct IpdgState {
     bool lpc_ready = false;
     int F = 0, H = 128;
     int lpc_linear = 0;
+    int lpc_form = DG_LPC_RELU;
+    SchwarzArgs sw{};                 // learned additive-Schwarz form
+    float* d_U = nullptr;             // its local outputs (K x F)
+    int* d_iperm = nullptr;
+    float *d_Xs = nullptr, *d_As = nullptr, *d_C = nullptr;  // training: gathered rows, F x F cross term
+    double* d_gvec = nullptr;         // training: output-gradient vector
+    int* d_tcstatus = nullptr;        // timeout flag of the tensor-core local stage
     float *d_W1 = nullptr, *d_W2 = nullptr, *d_m1 = nullptr, *d_v1 = nullptr, *d_m2 = nullptr, *d_v2 = nullptr;
     float *d_g1 = nullptr, *d_g2 = nullptr;
     __nv_bfloat16 *d_W1b = nullptr, *d_W2b = nullptr;
@@ -116,6 +124,10 @@ void lpc_descr(dg_ctx* c, LpcNet& net, LpcFeatArgs& fa) {
     net.W1 = s->d_W1b;
     net.W2 = s->d_W2b;
     net.perm = s->d_perm;
+    if (s->lpc_form == DG_LPC_SCHWARZ) {
+        net.sw = &s->sw;
+        net.U = s->d_U;
+    }
     fa.K = c->K;
     fa.Np = c->Np;
     fa.linear = s->lpc_linear;
@@ -362,6 +374,7 @@ int dg_ipdg_setup(dg_ctx* c, double tau_coef) {
     rc |= ialloc(c, s, &s->d_p, n);
     rc |= ialloc(c, s, &s->d_p2, n);
     rc |= ialloc(c, s, &s->d_dz, n);
+    rc |= ialloc(c, s, &s->d_r32, n);
     rc |= ialloc(c, s, &s->d_dp, n);
     rc |= ialloc(c, s, &s->d_dp2, n);
     int dev = 0, sms = 0;
@@ -454,6 +467,7 @@ int dg_pcg_solve(dg_ctx* c, const double* b_host, double* x_host, double rtol, i
     v.dz = mirrors ? s->d_dz : nullptr;
     v.dp[0] = mirrors ? s->d_dp : nullptr;
     v.dp[1] = mirrors ? s->d_dp2 : nullptr;
+    v.r32 = (learned && s->lpc_form == DG_LPC_SCHWARZ) ? s->d_r32 : nullptr;
     int total_it = 0, stop = 0;
     double rel = 0;
     if (bb == 0.0) {
@@ -487,6 +501,17 @@ int dg_pcg_solve(dg_ctx* c, const double* b_host, double* x_host, double rtol, i
     if (rc) return rc;
     cudaEventRecord(e1, c->stream);
     rel = bb > 0 ? std::sqrt(rr / bb) : 0.0;
+    if (learned && s->d_tcstatus) {
+        int tst = 0;
+        IP_CUDA(c, cudaMemcpyAsync(&tst, s->d_tcstatus, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+        IP_CUDA(c, cudaStreamSynchronize(c->stream));
+        if (tst) {
+            cudaMemsetAsync(s->d_tcstatus, 0, sizeof(int), c->stream);
+            cudaEventDestroy(e0);
+            cudaEventDestroy(e1);
+            return ifail(c, DG_ERR_TIMEOUT, "learned preconditioner: tensor-core completion wait timed out");
+        }
+    }
     if (pc == DG_PC_LEARNED && (!(rel == rel) || stop >= 2 || rel > rtol)) {
         // block-Jacobi PCG is the fallback: solve again from the caller's x0;
         // the reported time includes the learned attempt
@@ -571,9 +596,16 @@ int lpc_forward_vec(dg_ctx* c, const double* r, bool with_bj_loss) {
         IP_CUDA(c, launch_dot(r, s->d_zb, n, s->d_lpart + 2 * s->G, s->G, c->stream));
         IP_CUDA(c, launch_dot(s->d_zb, s->d_w, n, s->d_lpart + 3 * s->G, s->G, c->stream));
     }
-    IP_CUDA(c, launch_lpc_features(fa, s->d_X, s->d_sc, c->stream));
-    IP_CUDA(c, launch_lpc_forward(net, s->d_X, nullptr, K, s->d_Hs, s->d_y, s->d_lpart + 4 * s->G, s->G, c->stream));
-    IP_CUDA(c, launch_lpc_combine(s->d_zb, s->d_sc, s->d_y, K, Np, s->d_zt, c->stream));
+    if (s->lpc_form == DG_LPC_SCHWARZ) {
+        IP_CUDA(c, launch_schwarz_local(s->sw, r, nullptr, s->d_U, nullptr, c->stream));
+        IP_CUDA(c, launch_schwarz_collect(s->sw, s->d_zb, s->d_U, nullptr, s->d_zt, nullptr, LPC_APPLY, nullptr,
+                                          nullptr, c->stream));
+    } else {
+        IP_CUDA(c, launch_lpc_features(fa, s->d_X, s->d_sc, c->stream));
+        IP_CUDA(c, launch_lpc_forward(net, s->d_X, nullptr, K, s->d_Hs, s->d_y, s->d_lpart + 4 * s->G, s->G,
+                                      c->stream));
+        IP_CUDA(c, launch_lpc_combine(s->d_zb, s->d_sc, s->d_y, K, Np, s->d_zt, c->stream));
+    }
     IP_CUDA(c, launch_ipdg_apply(s->args, true, s->d_zt, s->d_w, c->stream));
     IP_CUDA(c, launch_dot(r, s->d_zt, n, s->d_lpart, s->G, c->stream));
     IP_CUDA(c, launch_dot(s->d_zt, s->d_w, n, s->d_lpart + s->G, s->G, c->stream));
@@ -583,6 +615,17 @@ int lpc_forward_vec(dg_ctx* c, const double* r, bool with_bj_loss) {
 // gradients of L(r) into s->d_g1 / d_g2
 int lpc_backward_vec(dg_ctx* c, const double* r) {
     IpdgState* s = c->ipdg;
+    if (s->lpc_form == DG_LPC_SCHWARZ) {
+        // dL/dW = (2a/b) W (X^T A + A^T X), X = G r, A = G g, g = (a/b) S z - r
+        const size_t n = (size_t)c->K * c->Np;
+        IP_CUDA(c, launch_schwarz_outgrad(r, s->d_w, s->d_lpart, s->d_lpart + s->G, s->G, n, s->d_gvec, c->stream));
+        IP_CUDA(c, launch_schwarz_gather_rows(s->sw, r, s->d_Xs, c->stream));
+        IP_CUDA(c, launch_schwarz_gather_rows(s->sw, s->d_gvec, s->d_As, c->stream));
+        IP_CUDA(c, launch_schwarz_cross(s->d_Xs, s->d_As, c->K, s->F, s->d_C, c->stream));
+        IP_CUDA(c, launch_schwarz_wgrad(s->d_W1, s->d_C, s->H, s->F, s->d_lpart, s->d_lpart + s->G, s->G, s->d_g1,
+                                        c->stream));
+        return DG_OK;
+    }
     LpcNet net;
     LpcFeatArgs fa;
     lpc_descr(c, net, fa);
@@ -620,12 +663,13 @@ int lpc_losses(dg_ctx* c, double* loss, double* loss_bj) {
 
 int lpc_adam_step(dg_ctx* c, double lr) {
     IpdgState* s = c->ipdg;
-    const int n1 = s->H * s->F, n2 = c->Np * s->H;
+    const int n1 = s->H * s->F, n2 = s->lpc_form == DG_LPC_SCHWARZ ? 0 : c->Np * s->H;
     s->adam_step++;
     IP_CUDA(c, launch_lpc_adam(s->d_W1, s->d_m1, s->d_v1, s->d_g1, s->d_W1b, n1, (float)lr, 0.9f, 0.999f, 1e-8f,
                                s->adam_step, 1.f, c->stream));
-    IP_CUDA(c, launch_lpc_adam(s->d_W2, s->d_m2, s->d_v2, s->d_g2, s->d_W2b, n2, (float)lr, 0.9f, 0.999f, 1e-8f,
-                               s->adam_step, 1.f, c->stream));
+    if (n2 > 0)
+        IP_CUDA(c, launch_lpc_adam(s->d_W2, s->d_m2, s->d_v2, s->d_g2, s->d_W2b, n2, (float)lr, 0.9f, 0.999f, 1e-8f,
+                                   s->adam_step, 1.f, c->stream));
     return DG_OK;
 }
 
@@ -633,13 +677,15 @@ int lpc_adam_step(dg_ctx* c, double lr) {
 // learning rate only converts)
 int lpc_refresh_bf16(dg_ctx* c) {
     IpdgState* s = c->ipdg;
-    const int n1 = s->H * s->F, n2 = c->Np * s->H;
+    const int n1 = s->H * s->F, n2 = s->lpc_form == DG_LPC_SCHWARZ ? 0 : c->Np * s->H;
     IP_CUDA(c, cudaMemsetAsync(s->d_g1, 0, n1 * sizeof(float), c->stream));
-    IP_CUDA(c, cudaMemsetAsync(s->d_g2, 0, n2 * sizeof(float), c->stream));
     IP_CUDA(c, launch_lpc_adam(s->d_W1, s->d_m1, s->d_v1, s->d_g1, s->d_W1b, n1, 0.f, 0.9f, 0.999f, 1e-8f, 1, 1.f,
                                c->stream));
-    IP_CUDA(c, launch_lpc_adam(s->d_W2, s->d_m2, s->d_v2, s->d_g2, s->d_W2b, n2, 0.f, 0.9f, 0.999f, 1e-8f, 1, 1.f,
-                               c->stream));
+    if (n2 > 0) {
+        IP_CUDA(c, cudaMemsetAsync(s->d_g2, 0, n2 * sizeof(float), c->stream));
+        IP_CUDA(c, launch_lpc_adam(s->d_W2, s->d_m2, s->d_v2, s->d_g2, s->d_W2b, n2, 0.f, 0.9f, 0.999f, 1e-8f, 1,
+                                   1.f, c->stream));
+    }
     return DG_OK;
 }
 
@@ -660,53 +706,86 @@ extern "C" {
 
 int dg_lpc_setup(dg_ctx* c, int hidden, unsigned long long seed, int capacity, int form) {
     if (!c || hidden < 8 || hidden > 256 || capacity < 0) return DG_ERR_ARG;
-    if (form != DG_LPC_RELU && form != DG_LPC_LINEAR) return DG_ERR_ARG;
+    if (form != DG_LPC_RELU && form != DG_LPC_LINEAR && form != DG_LPC_SCHWARZ) return DG_ERR_ARG;
     if (!c->ipdg || !c->ipdg->ready) return ifail(c, DG_ERR_ARG, "dg_ipdg_setup not called");
     IpdgState* s = c->ipdg;
     if (s->lpc_ready) return ifail(c, DG_ERR_ARG, "learned preconditioner already set up");
     const int Np = c->Np, K = c->K;
+    const bool schwarz = form == DG_LPC_SCHWARZ;
     if (Np > 36) return ifail(c, DG_ERR_UNSUPPORTED, "learned preconditioner supports N <= 7");
+    if (schwarz && (Np > 28 || (hidden != 32 && hidden != 64)))
+        return ifail(c, DG_ERR_UNSUPPORTED, "the Schwarz form supports N <= 6 and hidden width 32 or 64");
     s->H = hidden;
-    s->F = 4 * Np + 4;
+    s->F = schwarz ? 4 * Np : 4 * Np + 4;
+    s->lpc_form = form;
     s->lpc_linear = form == DG_LPC_LINEAR ? 1 : 0;
-    const int n1 = s->H * s->F, n2 = Np * s->H;
+    const int n1 = s->H * s->F, n2 = schwarz ? 0 : Np * s->H;
     std::mt19937_64 rng(seed);
     std::normal_distribution<float> nd(0.f, 1.f);
     std::vector<float> W1(n1), W2(n2);
-    for (auto& w : W1) w = nd(rng) * std::sqrt(2.0f / s->F);
+    // Schwarz form: a small start keeps M close to block Jacobi
+    for (auto& w : W1) w = nd(rng) * (schwarz ? 1e-3f : std::sqrt(2.0f / s->F));
     for (auto& w : W2) w = nd(rng) * 0.01f / std::sqrt((float)s->H);
     std::vector<int> perm = rotation_perms(c->ops);
     for (int v : perm)
         if (v < 0) return ifail(c, DG_ERR_ARG, "node set is not rotation symmetric");
+    std::vector<int> iperm(perm.size());
+    for (int f = 0; f < 3; f++)
+        for (int i = 0; i < Np; i++) iperm[f * Np + perm[f * Np + i]] = i;
     const size_t n = (size_t)K * Np;
     int rc = 0;
     rc |= iupload(c, s, &s->d_W1, W1);
-    rc |= iupload(c, s, &s->d_W2, W2);
     rc |= iupload(c, s, &s->d_perm, perm);
     rc |= ialloc(c, s, &s->d_m1, n1);
     rc |= ialloc(c, s, &s->d_v1, n1);
     rc |= ialloc(c, s, &s->d_g1, n1);
-    rc |= ialloc(c, s, &s->d_m2, n2);
-    rc |= ialloc(c, s, &s->d_v2, n2);
-    rc |= ialloc(c, s, &s->d_g2, n2);
     rc |= ialloc(c, s, &s->d_W1b, n1);
-    rc |= ialloc(c, s, &s->d_W2b, n2);
     rc |= ialloc(c, s, &s->d_zb, n);
-    rc |= ialloc(c, s, &s->d_sc, (size_t)K);
-    rc |= ialloc(c, s, &s->d_X, (size_t)K * s->F);
-    rc |= ialloc(c, s, &s->d_Hs, (size_t)2 * K * s->H);
-    rc |= ialloc(c, s, &s->d_y, n);
-    rc |= ialloc(c, s, &s->d_dY, n);
     rc |= ialloc(c, s, &s->d_zt, n);
     rc |= ialloc(c, s, &s->d_w, n);
     rc |= ialloc(c, s, &s->d_lpart, (size_t)5 * s->G);
+    if (schwarz) {
+        rc |= iupload(c, s, &s->d_iperm, iperm);
+        rc |= ialloc(c, s, &s->d_U, (size_t)K * s->F);
+        rc |= ialloc(c, s, &s->d_Xs, (size_t)K * s->F);
+        rc |= ialloc(c, s, &s->d_As, (size_t)K * s->F);
+        rc |= ialloc(c, s, &s->d_C, (size_t)s->F * s->F);
+        rc |= ialloc(c, s, &s->d_gvec, n);
+    } else {
+        rc |= iupload(c, s, &s->d_W2, W2);
+        rc |= ialloc(c, s, &s->d_m2, n2);
+        rc |= ialloc(c, s, &s->d_v2, n2);
+        rc |= ialloc(c, s, &s->d_g2, n2);
+        rc |= ialloc(c, s, &s->d_W2b, n2);
+        rc |= ialloc(c, s, &s->d_sc, (size_t)K);
+        rc |= ialloc(c, s, &s->d_X, (size_t)K * s->F);
+        rc |= ialloc(c, s, &s->d_Hs, (size_t)2 * K * s->H);
+        rc |= ialloc(c, s, &s->d_y, n);
+        rc |= ialloc(c, s, &s->d_dY, n);
+    }
     s->cap = (size_t)capacity;
     if (s->cap) rc |= ialloc(c, s, &s->d_R, s->cap * n);
     if (rc) return DG_ERR_NOMEM;
+    s->sw.K = K;
+    s->sw.Np = Np;
+    s->sw.H = s->H;
+    s->sw.sms = s->sms;
+    s->sw.W = s->d_W1b;
+    s->sw.conn = c->d_conn;
+    s->sw.perm = s->d_perm;
+    s->sw.iperm = s->d_iperm;
+    s->sw.tc_status = nullptr;
+    if (schwarz && s->H == 32) {
+        if (ialloc(c, s, &s->d_tcstatus, 1)) return DG_ERR_NOMEM;
+        IP_CUDA(c, cudaMemsetAsync(s->d_tcstatus, 0, sizeof(int), c->stream));
+        s->sw.tc_status = s->d_tcstatus;  // the tensor-core local stage
+    }
     IP_CUDA(c, cudaMemsetAsync(s->d_m1, 0, n1 * sizeof(float), c->stream));
     IP_CUDA(c, cudaMemsetAsync(s->d_v1, 0, n1 * sizeof(float), c->stream));
-    IP_CUDA(c, cudaMemsetAsync(s->d_m2, 0, n2 * sizeof(float), c->stream));
-    IP_CUDA(c, cudaMemsetAsync(s->d_v2, 0, n2 * sizeof(float), c->stream));
+    if (n2 > 0) {
+        IP_CUDA(c, cudaMemsetAsync(s->d_m2, 0, n2 * sizeof(float), c->stream));
+        IP_CUDA(c, cudaMemsetAsync(s->d_v2, 0, n2 * sizeof(float), c->stream));
+    }
     rc = lpc_refresh_bf16(c);
     if (rc) return rc;
     IP_CUDA(c, cudaStreamSynchronize(c->stream));
@@ -787,7 +866,8 @@ int dg_lpc_loss(dg_ctx* c, const double* r_host, double* loss, double* loss_bj) 
 }
 
 int dg_lpc_energy_gradients(dg_ctx* c, const double* r_host, float* gW1, float* gW2, double* loss) {
-    if (!c || !r_host || !gW1 || !gW2) return DG_ERR_ARG;
+    if (!c || !r_host || !gW1) return DG_ERR_ARG;
+    if (c->ipdg && c->ipdg->lpc_form != DG_LPC_SCHWARZ && !gW2) return DG_ERR_ARG;
     if (!lpc_ok(c)) return ifail(c, DG_ERR_ARG, "dg_lpc_setup not called");
     IpdgState* s = c->ipdg;
     int rc = lpc_upload_residual(c, r_host, s->d_r);
@@ -796,32 +876,42 @@ int dg_lpc_energy_gradients(dg_ctx* c, const double* r_host, float* gW1, float* 
     if (!rc) rc = lpc_losses(c, loss, nullptr);
     if (rc) return rc;
     IP_CUDA(c, cudaMemcpyAsync(gW1, s->d_g1, (size_t)s->H * s->F * sizeof(float), cudaMemcpyDeviceToHost, c->stream));
-    IP_CUDA(c, cudaMemcpyAsync(gW2, s->d_g2, (size_t)c->Np * s->H * sizeof(float), cudaMemcpyDeviceToHost, c->stream));
+    if (s->lpc_form != DG_LPC_SCHWARZ)
+        IP_CUDA(c, cudaMemcpyAsync(gW2, s->d_g2, (size_t)c->Np * s->H * sizeof(float), cudaMemcpyDeviceToHost,
+                                   c->stream));
     IP_CUDA(c, cudaStreamSynchronize(c->stream));
     return DG_OK;
 }
 
 int dg_lpc_get_weights(dg_ctx* c, float* W1, float* W2) {
-    if (!c || !W1 || !W2) return DG_ERR_ARG;
+    if (!c || !W1) return DG_ERR_ARG;
     if (!lpc_ok(c)) return ifail(c, DG_ERR_ARG, "dg_lpc_setup not called");
     IpdgState* s = c->ipdg;
+    const bool two = s->lpc_form != DG_LPC_SCHWARZ;
+    if (two && !W2) return DG_ERR_ARG;
     IP_CUDA(c, cudaMemcpyAsync(W1, s->d_W1, (size_t)s->H * s->F * sizeof(float), cudaMemcpyDeviceToHost, c->stream));
-    IP_CUDA(c, cudaMemcpyAsync(W2, s->d_W2, (size_t)c->Np * s->H * sizeof(float), cudaMemcpyDeviceToHost, c->stream));
+    if (two)
+        IP_CUDA(c, cudaMemcpyAsync(W2, s->d_W2, (size_t)c->Np * s->H * sizeof(float), cudaMemcpyDeviceToHost,
+                                   c->stream));
     IP_CUDA(c, cudaStreamSynchronize(c->stream));
     return DG_OK;
 }
 
 int dg_lpc_set_weights(dg_ctx* c, const float* W1, const float* W2) {
-    if (!c || !W1 || !W2) return DG_ERR_ARG;
+    if (!c || !W1) return DG_ERR_ARG;
     if (!lpc_ok(c)) return ifail(c, DG_ERR_ARG, "dg_lpc_setup not called");
     IpdgState* s = c->ipdg;
-    const int n1 = s->H * s->F, n2 = c->Np * s->H;
+    const bool two = s->lpc_form != DG_LPC_SCHWARZ;
+    if (two && !W2) return DG_ERR_ARG;
+    const int n1 = s->H * s->F, n2 = two ? c->Np * s->H : 0;
     IP_CUDA(c, cudaMemcpyAsync(s->d_W1, W1, n1 * sizeof(float), cudaMemcpyHostToDevice, c->stream));
-    IP_CUDA(c, cudaMemcpyAsync(s->d_W2, W2, n2 * sizeof(float), cudaMemcpyHostToDevice, c->stream));
     IP_CUDA(c, cudaMemsetAsync(s->d_m1, 0, n1 * sizeof(float), c->stream));
     IP_CUDA(c, cudaMemsetAsync(s->d_v1, 0, n1 * sizeof(float), c->stream));
-    IP_CUDA(c, cudaMemsetAsync(s->d_m2, 0, n2 * sizeof(float), c->stream));
-    IP_CUDA(c, cudaMemsetAsync(s->d_v2, 0, n2 * sizeof(float), c->stream));
+    if (two) {
+        IP_CUDA(c, cudaMemcpyAsync(s->d_W2, W2, n2 * sizeof(float), cudaMemcpyHostToDevice, c->stream));
+        IP_CUDA(c, cudaMemsetAsync(s->d_m2, 0, n2 * sizeof(float), c->stream));
+        IP_CUDA(c, cudaMemsetAsync(s->d_v2, 0, n2 * sizeof(float), c->stream));
+    }
     s->adam_step = 0;
     int rc = lpc_refresh_bf16(c);
     if (rc) return rc;
@@ -834,6 +924,8 @@ int dg_lpc_gradients(dg_ctx* c, const float* X_host, const float* T_host, int B,
     if (!c || !X_host || !T_host || B < 1 || !gW1 || !gW2) return DG_ERR_ARG;
     if (!lpc_ok(c)) return ifail(c, DG_ERR_ARG, "dg_lpc_setup not called");
     IpdgState* s = c->ipdg;
+    if (s->lpc_form == DG_LPC_SCHWARZ)
+        return ifail(c, DG_ERR_UNSUPPORTED, "batch gradients are defined for the two-layer forms");
     const int Np = c->Np;
     float *Xf = nullptr, *Td = nullptr, *Hs = nullptr, *dY = nullptr;
     __nv_bfloat16* Xb = nullptr;
@@ -884,7 +976,13 @@ int dg_lpc_apply(dg_ctx* c, const double* r_host, double* z_host) {
     LpcFeatArgs fa;
     lpc_descr(c, net, fa);
     IP_CUDA(c, cudaMemsetAsync(s->d_z, 0, n * sizeof(double), c->stream));
-    IP_CUDA(c, launch_lpc_precond(net, fa, s->d_r, s->d_z, LPC_APPLY, nullptr, nullptr, nullptr, c->stream));
+    if (s->lpc_form == DG_LPC_SCHWARZ) {
+        IP_CUDA(c, launch_schwarz_local(s->sw, s->d_r, nullptr, s->d_U, nullptr, c->stream));
+        IP_CUDA(c, launch_schwarz_collect(s->sw, s->d_zb, s->d_U, nullptr, s->d_z, nullptr, LPC_APPLY, nullptr,
+                                          nullptr, c->stream));
+    } else {
+        IP_CUDA(c, launch_lpc_precond(net, fa, s->d_r, s->d_z, LPC_APPLY, nullptr, nullptr, nullptr, c->stream));
+    }
     IP_CUDA(c, launch_permute(s->d_z, s->d_p, c->d_ring, K, Np, false, c->stream));
     IP_CUDA(c, cudaMemcpyAsync(z_host, s->d_p, n * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
     IP_CUDA(c, cudaStreamSynchronize(c->stream));

@@ -310,3 +310,320 @@ cudaError_t launch_lpc_precond(const LpcNet& n, const LpcFeatArgs& fa, const dou
 }
 
 }  // namespace dgk
+
+// ---------------------------------------------------------------------------
+// Learned additive-Schwarz form (SPD by construction):
+//   M r = P r + sum_m G_m^T W^T W G_m r
+// G_m gathers the residual on element m and its three face neighbours (each
+// neighbour rotated so that the shared face is its face 0; zero across a
+// boundary), F = 4 Np values; W (H x F) is stored in BF16, activations are
+// FP32, so M is exactly linear and symmetric positive definite and plain CG
+// applies.  The transpose is computed by the owner: element k collects its
+// own slot of U_k = W^T W G_k r and, through each face f with neighbour m
+// (m's face fn), the entries of m's slot fn + 1 at the node permutation of
+// face f.
+
+namespace dgk {
+
+namespace {
+
+// x = G_m v (FP32) for element m
+__device__ __forceinline__ void schwarz_gather(const SchwarzArgs& a, const double* __restrict__ v, int m, float* x) {
+    const int Np = a.Np;
+    const double* vm = v + (size_t)m * Np;
+    for (int i = 0; i < Np; i++) x[i] = (float)vm[i];
+    for (int f = 0; f < 3; f++) {
+        const int c = a.conn[(size_t)m * 3 + f];
+        float* xf = x + (f + 1) * Np;
+        if (c >= 0) {
+            const double* vn = v + (size_t)(c >> 3) * Np;
+            const int* pm = a.perm + (c & 3) * Np;
+            for (int i = 0; i < Np; i++) xf[i] = (float)vn[pm[i]];
+        } else {
+            for (int i = 0; i < Np; i++) xf[i] = 0.f;
+        }
+    }
+}
+
+}  // namespace
+
+// U[m] = W^T (W G_m r); W staged in shared memory (FP32 from the BF16 copy);
+// one thread per element, Np and H compile-time so x and h stay in registers
+template <int NP, int H>
+struct SchwarzLocalDims {
+    static constexpr int THREADS = H > 32 ? 64 : 128;  // static shared memory stays under 48 KB
+    static constexpr int MIN_BLOCKS = NP <= 15 ? (H > 32 ? 10 : 6) : (H > 32 ? 6 : 4);
+};
+
+template <int NP, int H>
+__global__ void __launch_bounds__(SchwarzLocalDims<NP, H>::THREADS, SchwarzLocalDims<NP, H>::MIN_BLOCKS)
+    schwarz_local_kernel(SchwarzArgs a, const double* __restrict__ r, const float* __restrict__ r32,
+                         float* __restrict__ U, const int* __restrict__ done) {
+    constexpr int F = 4 * NP;  // a multiple of 4: W rows are read as float4
+    constexpr int HP = H + 1;  // padded per-thread row of the hidden vector (no bank conflicts)
+    constexpr int T = SchwarzLocalDims<NP, H>::THREADS;
+    __shared__ __align__(16) float wsh[H * F];
+    __shared__ float hsh[T * HP];
+    if (done && *done) return;
+    for (int i = threadIdx.x; i < H * F; i += blockDim.x) wsh[i] = __bfloat162float(a.W[i]);
+    __syncthreads();
+    const float4* w4 = reinterpret_cast<const float4*>(wsh);
+    float* hrow = hsh + threadIdx.x * HP;
+    for (int m = blockIdx.x * blockDim.x + threadIdx.x; m < a.K; m += gridDim.x * blockDim.x) {
+        {
+            float x[F];
+            if (r32) {  // FP32 copy of the residual: no FP64 conversions here
+                const float* vm = r32 + (size_t)m * NP;
+#pragma unroll
+                for (int i = 0; i < NP; i++) x[i] = vm[i];
+#pragma unroll
+                for (int f = 0; f < 3; f++) {
+                    const int c = a.conn[(size_t)m * 3 + f];
+                    const float* vn = r32 + (size_t)(c >= 0 ? (c >> 3) : 0) * NP;
+                    const int* pm = a.perm + (c & 3) * NP;
+#pragma unroll
+                    for (int i = 0; i < NP; i++) x[(f + 1) * NP + i] = c >= 0 ? vn[pm[i]] : 0.f;
+                }
+            } else {
+                const double* vm = r + (size_t)m * NP;
+#pragma unroll
+                for (int i = 0; i < NP; i++) x[i] = (float)vm[i];
+#pragma unroll
+                for (int f = 0; f < 3; f++) {
+                    const int c = a.conn[(size_t)m * 3 + f];
+                    const double* vn = r + (size_t)(c >= 0 ? (c >> 3) : 0) * NP;
+                    const int* pm = a.perm + (c & 3) * NP;
+#pragma unroll
+                    for (int i = 0; i < NP; i++) x[(f + 1) * NP + i] = c >= 0 ? (float)vn[pm[i]] : 0.f;
+                }
+            }
+            // h = W x: four W entries per shared-memory load (broadcast)
+#pragma unroll 2
+            for (int j = 0; j < H; j++) {
+                float acc = 0.f;
+#pragma unroll
+                for (int i4 = 0; i4 < F / 4; i4++) {
+                    const float4 w = w4[j * (F / 4) + i4];
+                    acc = fmaf(w.x, x[4 * i4], acc);
+                    acc = fmaf(w.y, x[4 * i4 + 1], acc);
+                    acc = fmaf(w.z, x[4 * i4 + 2], acc);
+                    acc = fmaf(w.w, x[4 * i4 + 3], acc);
+                }
+                hrow[j] = acc;
+            }
+        }
+        // u = W^T h, accumulated row by row of W in registers, in two halves of
+        // the columns (fewer live registers: more resident warps)
+        float4* um = reinterpret_cast<float4*>(U + (size_t)m * F);
+        constexpr int Q = F / 4, Q0 = (Q + 1) / 2;
+#pragma unroll
+        for (int half = 0; half < 2; half++) {
+            constexpr int QH = Q0;
+            float u[4 * QH];
+#pragma unroll
+            for (int i = 0; i < 4 * QH; i++) u[i] = 0.f;
+            const int q0 = half * Q0;
+#pragma unroll 2
+            for (int j = 0; j < H; j++) {
+                const float hj = hrow[j];
+#pragma unroll
+                for (int i4 = 0; i4 < QH; i4++) {
+                    if (q0 + i4 < Q) {
+                        const float4 w = w4[j * Q + q0 + i4];
+                        u[4 * i4] = fmaf(w.x, hj, u[4 * i4]);
+                        u[4 * i4 + 1] = fmaf(w.y, hj, u[4 * i4 + 1]);
+                        u[4 * i4 + 2] = fmaf(w.z, hj, u[4 * i4 + 2]);
+                        u[4 * i4 + 3] = fmaf(w.w, hj, u[4 * i4 + 3]);
+                    }
+                }
+            }
+#pragma unroll
+            for (int i4 = 0; i4 < QH; i4++)
+                if (q0 + i4 < Q) um[q0 + i4] = make_float4(u[4 * i4], u[4 * i4 + 1], u[4 * i4 + 2], u[4 * i4 + 3]);
+        }
+    }
+}
+
+// z_k = zb_k + (G^T U)_k, one thread per element row in element-aligned
+// CTAs (EB = 256 / Np elements); the FP32 offset mirror of z is that of zb
+// (written by the PCG update) plus c - c0 in FP32; partial sums of r.z for the
+// CG scalars (M is linear SPD: the standard beta applies)
+__global__ void schwarz_collect_kernel(SchwarzArgs a, const double* __restrict__ zb, const float* __restrict__ U,
+                                       const double* __restrict__ r, double* __restrict__ z, float* __restrict__ dz,
+                                       int mode, PcgScalars* S, double* part) {
+    __shared__ float c0s[256];
+    if (mode == LPC_PCG_ITERATION && S->done) return;
+    const int Np = a.Np, F = 4 * Np, EB = 256 / Np;
+    const int e = threadIdx.x / Np, q = threadIdx.x - e * Np;
+    const int ngroups = (a.K + EB - 1) / EB;
+    double rz = 0;
+    for (int grp = blockIdx.x; grp < ngroups; grp += gridDim.x) {
+        const int k = grp * EB + e;
+        const bool act = e < EB && k < a.K;
+        float c = 0.f;
+        if (act) {
+            const size_t t = (size_t)k * Np + q;
+            c = U[(size_t)k * F + q];
+#pragma unroll
+            for (int f = 0; f < 3; f++) {
+                const int cn = a.conn[(size_t)k * 3 + f];
+                if (cn >= 0) c += U[(size_t)(cn >> 3) * F + ((cn & 3) + 1) * Np + a.iperm[f * Np + q]];
+            }
+            const double zv = zb[t] + (double)c;
+            z[t] = zv;
+            if (r) rz += r[t] * zv;
+            if (q == 0) c0s[e] = c;
+        }
+        if (dz) {
+            // dz enters as the offset mirror of zb: z - z0 = (zb - zb0) + (c - c0)
+            __syncthreads();
+            if (act) {
+                const size_t t = (size_t)k * Np + q;
+                dz[t] = dz[t] + (c - c0s[e]);
+            }
+            __syncthreads();
+        }
+    }
+    if (mode == LPC_APPLY) return;
+    double val[1] = {rz}, tot[1];
+    if (grid_sum<1>(val, part, gridDim.x, &S->counter, tot) && threadIdx.x == 0) {
+        if (mode == LPC_PCG_ITERATION) pcg_finish(S, tot[0], 0.0, S->rr);
+        else S->rz = tot[0];
+    }
+}
+
+// X[m] = G_m v as FP32 rows (training)
+__global__ void schwarz_gather_rows_kernel(SchwarzArgs a, const double* __restrict__ v, float* __restrict__ X) {
+    const int F = 4 * a.Np;
+    for (int m = blockIdx.x * blockDim.x + threadIdx.x; m < a.K; m += gridDim.x * blockDim.x) {
+        float x[kMaxF];
+        schwarz_gather(a, v, m, x);
+        for (int i = 0; i < F; i++) X[(size_t)m * F + i] = x[i];
+    }
+}
+
+// C = X^T A + A^T X (F x F), one thread per entry, fixed summation order
+__global__ void schwarz_cross_kernel(const float* __restrict__ X, const float* __restrict__ A, int K, int F,
+                                     float* __restrict__ C) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= F * F) return;
+    const int i = t / F, j = t - i * F;
+    float acc = 0.f;
+    for (int m = 0; m < K; m++) {
+        const float* xm = X + (size_t)m * F;
+        const float* am = A + (size_t)m * F;
+        acc = fmaf(xm[i], am[j], fmaf(am[i], xm[j], acc));
+    }
+    C[t] = acc;
+}
+
+// gW = scale W C (H x F)
+__global__ void schwarz_wgrad_kernel(const float* __restrict__ W, const float* __restrict__ C, int H, int F,
+                                     const double* __restrict__ part_a, const double* __restrict__ part_b, int G,
+                                     float* __restrict__ gW) {
+    __shared__ float s_scale;
+    if (threadIdx.x < 32) {
+        double aa = 0, bb = 0;
+        for (int i = threadIdx.x; i < G; i += 32) { aa += part_a[i]; bb += part_b[i]; }
+        for (int o = 16; o > 0; o >>= 1) {
+            aa += __shfl_xor_sync(0xffffffffu, aa, o);
+            bb += __shfl_xor_sync(0xffffffffu, bb, o);
+        }
+        if (threadIdx.x == 0) s_scale = bb > 0 ? (float)(2.0 * aa / bb) : 0.f;
+    }
+    __syncthreads();
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= H * F) return;
+    const int h = t / F, j = t - h * F;
+    float acc = 0.f;
+    for (int i = 0; i < F; i++) acc = fmaf(W[h * F + i], C[i * F + j], acc);
+    gW[t] = s_scale * acc;
+}
+
+// g = (a/b) w - r as FP64 (the energy-loss output gradient direction)
+__global__ void schwarz_outgrad_kernel(const double* __restrict__ r, const double* __restrict__ w,
+                                       const double* __restrict__ part_a, const double* __restrict__ part_b, int G,
+                                       size_t n, double* __restrict__ g) {
+    __shared__ double s_ab;
+    if (threadIdx.x < 32) {
+        double aa = 0, bb = 0;
+        for (int i = threadIdx.x; i < G; i += 32) { aa += part_a[i]; bb += part_b[i]; }
+        for (int o = 16; o > 0; o >>= 1) {
+            aa += __shfl_xor_sync(0xffffffffu, aa, o);
+            bb += __shfl_xor_sync(0xffffffffu, bb, o);
+        }
+        if (threadIdx.x == 0) s_ab = bb > 0 ? aa / bb : 0.0;
+    }
+    __syncthreads();
+    const double ab = s_ab;
+    for (size_t t = blockIdx.x * (size_t)blockDim.x + threadIdx.x; t < n; t += (size_t)gridDim.x * blockDim.x)
+        g[t] = ab * w[t] - r[t];
+}
+
+template <int NP, int H>
+static cudaError_t schwarz_local_nh(const SchwarzArgs& a, const double* r, const float* r32, float* U,
+                                    const int* done, cudaStream_t st) {
+    constexpr int T = SchwarzLocalDims<NP, H>::THREADS;
+    const int blocks = (a.K + T - 1) / T;
+    const int cap = (T == 128 ? 8 : 16) * a.sms;
+    schwarz_local_kernel<NP, H><<<blocks < cap ? blocks : cap, T, 0, st>>>(a, r, r32, U, done);
+    return cudaGetLastError();
+}
+
+template <int NP>
+static cudaError_t schwarz_local_np(const SchwarzArgs& a, const double* r, const float* r32, float* U,
+                                    const int* done, cudaStream_t st) {
+    switch (a.H) {
+        case 32: return schwarz_local_nh<NP, 32>(a, r, r32, U, done, st);
+        case 64: return schwarz_local_nh<NP, 64>(a, r, r32, U, done, st);
+        default: return cudaErrorInvalidValue;
+    }
+}
+
+cudaError_t launch_schwarz_local(const SchwarzArgs& a, const double* r, const float* r32, float* U, const int* done,
+                                 cudaStream_t st) {
+    if (a.tc_status && a.H == 32) return launch_schwarz_local_tc(a, r, r32, U, done, a.tc_status, st);
+    switch (a.Np) {
+        case 3: return schwarz_local_np<3>(a, r, r32, U, done, st);
+        case 6: return schwarz_local_np<6>(a, r, r32, U, done, st);
+        case 10: return schwarz_local_np<10>(a, r, r32, U, done, st);
+        case 15: return schwarz_local_np<15>(a, r, r32, U, done, st);
+        case 21: return schwarz_local_np<21>(a, r, r32, U, done, st);
+        case 28: return schwarz_local_np<28>(a, r, r32, U, done, st);
+        default: return cudaErrorInvalidValue;
+    }
+}
+
+cudaError_t launch_schwarz_collect(const SchwarzArgs& a, const double* zb, const float* U, const double* r,
+                                   double* z, float* dz, int mode, PcgScalars* S, double* part, cudaStream_t st) {
+    const int EB = 256 / a.Np;
+    const int threads = (EB * a.Np + 31) / 32 * 32;
+    const int ngroups = (a.K + EB - 1) / EB;
+    const int grid = ngroups < 8 * a.sms ? ngroups : 8 * a.sms;
+    schwarz_collect_kernel<<<grid, threads, 0, st>>>(a, zb, U, r, z, dz, mode, S, part);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_schwarz_gather_rows(const SchwarzArgs& a, const double* v, float* X, cudaStream_t st) {
+    schwarz_gather_rows_kernel<<<(a.K + 127) / 128, 128, 0, st>>>(a, v, X);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_schwarz_cross(const float* X, const float* A, int K, int F, float* C, cudaStream_t st) {
+    schwarz_cross_kernel<<<(F * F + 127) / 128, 128, 0, st>>>(X, A, K, F, C);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_schwarz_wgrad(const float* W, const float* C, int H, int F, const double* part_a,
+                                 const double* part_b, int G, float* gW, cudaStream_t st) {
+    schwarz_wgrad_kernel<<<(H * F + 127) / 128, 128, 0, st>>>(W, C, H, F, part_a, part_b, G, gW);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_schwarz_outgrad(const double* r, const double* w, const double* part_a, const double* part_b,
+                                   int G, size_t n, double* g, cudaStream_t st) {
+    schwarz_outgrad_kernel<<<608, 256, 0, st>>>(r, w, part_a, part_b, G, n, g);
+    return cudaGetLastError();
+}
+
+}  // namespace dgk

@@ -10,6 +10,8 @@
 
 namespace dgk {
 
+struct SchwarzArgs;
+
 // z_k = (P r)_k + s_k * W2 relu(W1 x_k / s_k)   with the feature vector
 // x_k = [(P r)_k, rotated (P r) of the 3 neighbours, 4 scaled metrics]
 struct LpcNet {
@@ -20,6 +22,8 @@ struct LpcNet {
     const __nv_bfloat16* W1 = nullptr;  // H x F (BF16 copy used by the kernels)
     const __nv_bfloat16* W2 = nullptr;  // Np x H
     const int* perm = nullptr;          // 3 x Np ring-order node permutation per neighbour face
+    const SchwarzArgs* sw = nullptr;  // learned additive-Schwarz form (then W1/W2 unused)
+    float* U = nullptr;                      // its per-element local outputs (K x 4 Np)
 };
 
 struct LpcFeatArgs {
@@ -54,5 +58,32 @@ enum { LPC_APPLY = 0, LPC_PCG_INIT = 1, LPC_PCG_REFRESH = 2, LPC_PCG_ITERATION =
 // dz (may be null): FP32 offset mirror of z (z minus the element's first-node value)
 cudaError_t launch_lpc_precond(const LpcNet& n, const LpcFeatArgs& fa, const double* r, double* z, int mode,
                                PcgScalars* S, double* part, float* dz, cudaStream_t st);
+
+// learned additive-Schwarz form: M r = P r + sum_m G_m^T W^T W G_m r
+constexpr int kSchwarzMaxH = 128;
+struct SchwarzArgs {
+    int K, Np, H, sms;
+    const __nv_bfloat16* W;  // H x 4 Np
+    const int* conn;         // packed neighbours
+    const int* perm;         // 3 x Np: node permutation that rotates a neighbour's face fn onto face 0
+    const int* iperm;        // 3 x Np: inverse of perm
+    int* tc_status;          // non-null: run the local stage on the tensor cores (H = 32); timeout flag
+};
+// tensor-core local stage (schwarz_tc.cu); cudaErrorNotSupported when H != 32 or N > 6
+cudaError_t launch_schwarz_local_tc(const SchwarzArgs& a, const double* r, const float* r32, float* U,
+                                    const int* done, int* status, cudaStream_t st);
+// r32 (may be null): FP32 copy of r, read instead of r
+cudaError_t launch_schwarz_local(const SchwarzArgs& a, const double* r, const float* r32, float* U, const int* done,
+                                 cudaStream_t st);
+// z = zb + G^T U; dz (may be null): on entry the FP32 offset mirror of zb, on
+// exit that of z; mode as for launch_lpc_precond
+cudaError_t launch_schwarz_collect(const SchwarzArgs& a, const double* zb, const float* U, const double* r,
+                                   double* z, float* dz, int mode, PcgScalars* S, double* part, cudaStream_t st);
+cudaError_t launch_schwarz_gather_rows(const SchwarzArgs& a, const double* v, float* X, cudaStream_t st);
+cudaError_t launch_schwarz_cross(const float* X, const float* A, int K, int F, float* C, cudaStream_t st);
+cudaError_t launch_schwarz_wgrad(const float* W, const float* C, int H, int F, const double* part_a,
+                                 const double* part_b, int G, float* gW, cudaStream_t st);
+cudaError_t launch_schwarz_outgrad(const double* r, const double* w, const double* part_a, const double* part_b,
+                                   int G, size_t n, double* g, cudaStream_t st);
 
 }  // namespace dgk

@@ -232,7 +232,7 @@ int dg_pcg_solve(dg_ctx* ctx, const double* b_host, double* x_host, double rtol,
  *     per output), a direct check of the backward kernels.
  *   dg_lpc_apply: z = M(r) once (host arrays of K*Np doubles, reference node
  *     order). */
-enum { DG_LPC_RELU = 0, DG_LPC_LINEAR = 1 };
+enum { DG_LPC_RELU = 0, DG_LPC_LINEAR = 1, DG_LPC_SCHWARZ = 2 };
 int dg_lpc_setup(dg_ctx* ctx, int hidden, unsigned long long seed, int capacity, int form);
 int dg_lpc_add_residual(dg_ctx* ctx, const double* r_host);
 int dg_lpc_train(dg_ctx* ctx, int epochs, double lr, unsigned long long seed, double* final_loss,

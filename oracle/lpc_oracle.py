@@ -180,3 +180,62 @@ def energy_gradients(W1, W2, r_ring, zb_ring, EToE, EToF, geo, perm, S_apply_rin
     dH = bf16(((dY @ W2b) * (1.0 if linear else (Hs > 0))).astype(np.float32)).astype(np.float64)
     K = X.shape[0]
     return dH.T @ Xb / K, dY.T @ Hs / K, -(a * a) / b
+
+
+# ---------------------------------------------------------------------------
+# Learned additive-Schwarz form: M r = P r + sum_m G_m^T W^T W G_m r, with
+# G_m the gather of element m and its three rotated neighbours (raw residual,
+# no scaling), W in BF16 and FP32 activations.
+
+
+def schwarz_gather(v_ring, EToE, EToF, perm):
+    """K x 4 Np rows G_m v (ring order)."""
+    K, Np = v_ring.shape
+    blocks = [v_ring]
+    for f in range(3):
+        nb = EToE[:, f]
+        bnd = nb < 0
+        nbc = np.where(bnd, 0, nb)
+        fn = np.where(bnd, 0, EToF[:, f])
+        vn = v_ring[nbc][np.arange(K)[:, None], perm[fn]]
+        vn[bnd] = 0.0
+        blocks.append(vn)
+    return np.concatenate(blocks, axis=1)
+
+
+def schwarz_scatter(U, EToE, EToF, perm):
+    """sum_m G_m^T U_m (K x Np): the element's own slot plus, through each face
+    f with neighbour m (m's face fn), m's slot fn + 1 at the node permutation
+    of face f."""
+    K = U.shape[0]
+    Np = U.shape[1] // 4
+    z = U[:, :Np].astype(np.float64).copy()
+    for f in range(3):
+        nb = EToE[:, f]
+        ok = nb >= 0
+        fn = EToF[:, f]
+        k = np.nonzero(ok)[0]
+        src = U[nb[k][:, None], (fn[k][:, None] + 1) * Np + np.arange(Np)[None, :]]
+        np.add.at(z, (k[:, None], perm[f][None, :].repeat(k.size, 0)), src)
+    return z
+
+
+def schwarz_apply(W, r_ring, zb_ring, EToE, EToF, perm):
+    Wb = bf16(W).astype(np.float64)
+    X = schwarz_gather(r_ring, EToE, EToF, perm).astype(np.float32).astype(np.float64)
+    U = ((X @ Wb.T) @ Wb)
+    return zb_ring + schwarz_scatter(U, EToE, EToF, perm)
+
+
+def schwarz_energy_gradients(W, r_ring, zb_ring, EToE, EToF, perm, S_apply_ring):
+    """dL/dW = (2a/b) W (X^T A + A^T X), X = G r, A = G g, g = (a/b) S z - r,
+    and the loss -(a^2)/b, for L(r) = -(r.z)|r.z| / (z.S z)."""
+    z = schwarz_apply(W, r_ring, zb_ring, EToE, EToF, perm)
+    w = S_apply_ring(z)
+    a = float((r_ring * z).sum())
+    b = float((z * w).sum())
+    g = (a / b) * w - r_ring
+    X = schwarz_gather(r_ring, EToE, EToF, perm)
+    A = schwarz_gather(g, EToE, EToF, perm)
+    C = X.T @ A + A.T @ X
+    return (2 * a / b) * (W.astype(np.float64) @ C), -(a * a) / b

@@ -72,3 +72,20 @@ def test_rotation_perms_against_library_nodes():
         for _ in range(3):
             p = p[perm[1]]
         assert np.array_equal(p, np.arange(ring.size))
+
+
+def test_schwarz_scatter_is_the_transpose_of_gather():
+    from hopefoam_gb300.euler import reference_operators
+    from hopefoam_gb300.mesh import delaunay_square, periodic_square
+
+    for N, mesh in ((3, delaunay_square(60, seed=4)), (2, periodic_square(3, 3, seed=2))):
+        ops = reference_operators(N)
+        ring = lo.ring_order(N)
+        perm = lo.rotation_perms(ops["r"], ops["s"], ring)
+        rng = np.random.default_rng(N)
+        Np = ring.size
+        v = rng.standard_normal((mesh.K, Np))
+        Y = rng.standard_normal((mesh.K, 4 * Np))
+        lhs = float((lo.schwarz_gather(v, mesh.EToE, mesh.EToF, perm) * Y).sum())
+        rhs = float((v * lo.schwarz_scatter(Y, mesh.EToE, mesh.EToF, perm)).sum())
+        assert abs(lhs - rhs) <= 1e-12 * max(1.0, abs(lhs))

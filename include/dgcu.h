@@ -210,10 +210,14 @@ int dg_pcg_solve(dg_ctx* ctx, const double* b_host, double* x_host, double rtol,
  * repeats it with block Jacobi from the same initial guess and reports
  * negative iterations (the block-Jacobi count) and the time of both attempts.
  *   dg_lpc_setup: after dg_ipdg_setup; capacity = training residual vectors
- *     kept on the device; form DG_LPC_RELU (the network above) or
- *     DG_LPC_LINEAR (identity activation, no metric features: M is then a
- *     learned linear coupling of the element's and its neighbours' block-Jacobi
- *     outputs, z = P r + W2 W1 x, which keeps CG's optimality).
+ *     kept on the device; form DG_LPC_SCHWARZ (recommended): the learned
+ *     additive-Schwarz preconditioner M r = P r + sum_m G_m^T W^T W G_m r, G_m
+ *     the residual on element m and its rotated neighbours, W (hidden x 4 Np,
+ *     hidden 32 or 64, N <= 6), SPD by construction (plain CG); the tensor
+ *     cores run its local stage at hidden 32.  DG_LPC_RELU (the network above)
+ *     or DG_LPC_LINEAR (identity activation, no metric features) correct the
+ *     block-Jacobi output instead; they are not SPD.  For DG_LPC_SCHWARZ the
+ *     weights are W1 = W only (W2 / gW2 arguments may be NULL).
  *   dg_lpc_add_residual: one residual r = b - S x of the method's own PCG
  *     (host array, reference node order), stored scaled to r.P r = 1.
  *   dg_lpc_train: Adam epochs, one step per stored residual, minimising the

@@ -187,6 +187,8 @@ def main():
     ap.add_argument("--no-batch", action="store_true")
     ap.add_argument("--no-configs", action="store_true")
     ap.add_argument("--kh-steps", type=int, default=2)
+    ap.add_argument("--c5-study", action="store_true", help="500-step shear-layer accuracy study (reduced size)")
+    ap.add_argument("--c5-study-n", type=int, default=128)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
@@ -334,6 +336,11 @@ def main():
                 line[key] = fn() if key == "c1" else fn(nsteps=args.kh_steps)
             except Exception as exc:
                 line[key] = {"error": str(exc)}
+    if rank == 0 and args.c5_study:
+        try:
+            line["c5_study"] = c5_study(n=args.c5_study_n)
+        except Exception as exc:
+            line["c5_study"] = {"error": str(exc)}
     if rank == 0 and not args.no_batch:
         try:
             line["batched"] = batch_bench(prec)
@@ -383,43 +390,113 @@ def c1_bench(nsteps=100, order=3):
             "value": mesh.K * ops["r"].size * 4 * 5 * nsteps / (ms * 1e-3), "unit": UNIT, "ms": ms}
 
 
-def c5_bench(nsteps=None, order=7, n=708):
-    """Large shear layer: periodic [0,1]^2, 708x708x2 = 1,002,528 triangles,
-    N = 7 (Np = 36), Kelvin-Helmholtz initial state, Roe flux, LSERK4 at CFL
-    0.5 on the FP64 path (the split path stops at N = 6); throughput over a few
-    steps (the 500-step run is a separate long job)."""
-    from hopefoam_gb300 import _lib as L
+def _kh_context(n, order):
     from hopefoam_gb300 import euler
     from hopefoam_gb300.mesh import periodic_square
 
-    import torch
-
-    nsteps = nsteps or 2
-    t0 = time.perf_counter()
     mesh = periodic_square(n, n, 1.0, 1.0)
     ops = euler.reference_operators(order)
     x, y = euler.node_coords(mesh, ops["r"], ops["s"])
     q0 = euler.kelvin_helmholtz(x, y, seed=0)
-    ctx = euler.EulerContext(mesh, order)
-    ctx.upload(q0)
-    del x, y, q0
-    dt = ctx.cfl_dt(0.5)
-    setup_s = time.perf_counter() - t0
-    ctx.lserk4(dt, 1, flux=L.DG_FLUX_ROE, precision=L.DG_PREC_FP64)
+    return mesh, q0
+
+
+def _timed_lserk4(ctx, dt, nsteps, flux, prec):
+    import torch
+
     stream = torch.cuda.ExternalStream(ctx.stream)
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record(stream)
-    ctx.lserk4(dt, nsteps, flux=L.DG_FLUX_ROE, precision=L.DG_PREC_FP64)
+    ctx.lserk4(dt, nsteps, flux=flux, precision=prec)
     e1.record(stream)
     e1.synchronize()
-    ms = e0.elapsed_time(e1)
-    q = ctx.download()
-    finite = bool(np.isfinite(q).all())
+    return e0.elapsed_time(e1)
+
+
+def c5_bench(nsteps=None, order=7, n=708):
+    """Large shear layer: periodic [0,1]^2, 708x708x2 = 1,002,528 triangles,
+    N = 7 (Np = 36), Kelvin-Helmholtz initial state, Roe flux, LSERK4 at CFL
+    0.5; the FP64 path and the split path (streamed-operator kernel) each
+    timed over a few steps from the initial state, and the split path's
+    one-step state error against the FP64 path from the same state.  The
+    500-step accuracy study is c5_study (--c5-study)."""
+    from hopefoam_gb300 import _lib as L
+    from hopefoam_gb300 import euler
+
+    nsteps = nsteps or 2
+    t0 = time.perf_counter()
+    mesh, q0 = _kh_context(n, order)
+    ctx = euler.EulerContext(mesh, order)
+    ctx.upload(q0)
+    dt = ctx.cfl_dt(0.5)
+    setup_s = time.perf_counter() - t0
     K, Np = mesh.K, ctx.Np
+    out = {"workload": "Kelvin-Helmholtz, periodic 708x708x2 (K=%d), N=7, Roe, LSERK4 CFL 0.5" % K,
+           "steps": nsteps, "setup_s": setup_s, "dt": dt, "unit": UNIT}
+    peak, peak_kind = peaks()
+    for name, prec in (("fp64", L.DG_PREC_FP64), ("split", L.DG_PREC_SPLIT)):
+        ctx.upload(q0)
+        ctx.lserk4(dt, 1, flux=L.DG_FLUX_ROE, precision=prec)  # warm-up
+        ctx.upload(q0)
+        ms = _timed_lserk4(ctx, dt, nsteps, L.DG_FLUX_ROE, prec)
+        bpe = alg_bytes_per_elem_stage(order, split=(name == "split"))
+        out[name] = {"ms_per_step": ms / nsteps, "value": K * Np * 4 * 5 * nsteps / (ms * 1e-3),
+                     "roofline": {"achieved": bpe * K * 5 * nsteps / (ms * 1e-3) / 1e9, "peak": peak,
+                                  "unit": "GB/s", "peak_kind": peak_kind, "bytes_per_elem_stage": bpe}}
+        out[name]["roofline"]["frac"] = out[name]["roofline"]["achieved"] / peak
+        out[name]["state_finite"] = bool(np.isfinite(ctx.download()).all())
+    out["split_speedup_vs_fp64"] = out["fp64"]["ms_per_step"] / out["split"]["ms_per_step"]
+    ctx.upload(q0)
+    ctx.lserk4(dt, 1, flux=L.DG_FLUX_ROE, precision=L.DG_PREC_FP64)
+    q64 = ctx.download()
+    ctx.upload(q0)
+    ctx.lserk4(dt, 1, flux=L.DG_FLUX_ROE, precision=L.DG_PREC_SPLIT)
+    qsp = ctx.download()
     ctx.close()
-    return {"workload": "Kelvin-Helmholtz, periodic 708x708x2 (K=%d), N=7, Roe, LSERK4 CFL 0.5, FP64 path" % K,
-            "steps": nsteps, "ms_per_step": ms / nsteps, "value": K * Np * 4 * 5 * nsteps / (ms * 1e-3),
-            "unit": UNIT, "state_finite": finite, "setup_s": setup_s, "dt": dt}
+    d = qsp - q64
+    out["split_step_error"] = {"against": "FP64 path, one LSERK4 step from the initial state",
+                               "rel_l2": float(np.linalg.norm(d) / np.linalg.norm(q64)),
+                               "rel_linf": float(np.abs(d).max() / np.abs(q64).max())}
+    out["value"] = out["split"]["value"]
+    out["ms_per_step"] = out["split"]["ms_per_step"]
+    return out
+
+
+def c5_study(order=7, n=128, checkpoints=(100, 250, 500), n_full=708):
+    """The shear layer's accuracy study at reduced size (n x n x 2 elements,
+    the full-size workload's setup otherwise) and at the full-size
+    workload's time step (its CFL-0.5 step on the n_full grid, so that 500
+    steps cover the same physical time; the unlimited scheme on the
+    discontinuous initial state does not survive 500 steps at the coarse
+    grid's own CFL step): the split path and the FP64 path advanced side by
+    side from the same initial state; density error of the split path
+    against the FP64 path (relative L2 and Linf) at each checkpoint, and
+    both paths' device time."""
+    from hopefoam_gb300 import _lib as L
+    from hopefoam_gb300 import euler
+
+    mesh, q0 = _kh_context(n, order)
+    c64 = euler.EulerContext(mesh, order)
+    csp = euler.EulerContext(mesh, order)
+    c64.upload(q0)
+    csp.upload(q0)
+    dt = c64.cfl_dt(0.5) * n / n_full  # min h scales with 1/n on this grid family
+    rows, done, ms64, mssp = [], 0, 0.0, 0.0
+    for cp in checkpoints:
+        ms64 += _timed_lserk4(c64, dt, cp - done, L.DG_FLUX_ROE, L.DG_PREC_FP64)
+        mssp += _timed_lserk4(csp, dt, cp - done, L.DG_FLUX_ROE, L.DG_PREC_SPLIT)
+        done = cp
+        r64, rsp = c64.download()[0], csp.download()[0]
+        d = rsp - r64
+        rows.append({"step": cp, "t": cp * dt, "rho_rel_l2": float(np.linalg.norm(d) / np.linalg.norm(r64)),
+                     "rho_rel_linf": float(np.abs(d).max() / np.abs(r64).max()),
+                     "finite_fp64": bool(np.isfinite(r64).all()), "finite_split": bool(np.isfinite(rsp).all())})
+    c64.close()
+    csp.close()
+    return {"workload": "Kelvin-Helmholtz, periodic %dx%dx2 (K=%d), N=7, Roe, LSERK4 at the %dx%dx2 grid's "
+                        "CFL-0.5 step, %d steps" % (n, n, mesh.K, n_full, n_full, checkpoints[-1]),
+            "dt": dt, "density_error_split_vs_fp64": rows, "ms_per_step_fp64": ms64 / checkpoints[-1],
+            "ms_per_step_split": mssp / checkpoints[-1]}
 
 
 def batch_bench(prec, n_cases=512, nsteps=100):

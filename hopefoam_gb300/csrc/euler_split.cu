@@ -58,20 +58,32 @@ struct SplitDims {
     static constexpr int CH = 16;                     // cubature points per chunk
     static constexpr int NCH = NG / CH;
     static constexpr int KC = 2 * CH;                 // chunk buffer K: [Fr 16 | Fs 16]
-    static constexpr int NBUF = (N <= 5) ? 2 : 1;     // chunk buffers
+    // N = 7: the volume operator [Sr|Ss] (110 KB as hi/lo) does not fit next to
+    // the other operands.  It is streamed per chunk by bulk copies into
+    // buffers that pair with the flux chunk buffers (only the lift part stays
+    // resident), the FP64 tile copy is dropped (q is re-read from L2 in the
+    // epilogue) and the FP32 deltas are recovered from the TF32 hi + lo
+    // operand, which holds them exactly.
+    static constexpr bool STREAM = (N == 7);
+    static constexpr int NBUF = (N <= 5 || STREAM) ? 2 : 1;  // chunk buffers
+    static constexpr int FG = (Nfq <= 8) ? 8 : 16;    // lanes per face group
     // shared-memory layout (bytes, operand buffers 1024-aligned)
     static constexpr int SZ_B1 = 2 * NG * KP1 * 4;    // Vg hi/lo
-    static constexpr int SZ_B2 = 2 * NP2 * KP2 * 4;   // [Sr|Ss|Lift] hi/lo
+    static constexpr int SZ_BC = 2 * NP2 * KC * 4;    // one streamed [Sr|Ss] chunk hi/lo
+    static constexpr int SZ_B2 = STREAM ? 2 * NP2 * NF * 4    // Lift hi/lo
+                                        : 2 * NP2 * KP2 * 4;  // [Sr|Ss|Lift] hi/lo
     static constexpr int SZ_A1 = 2 * ROWS * KP1 * 4;  // dQ hi/lo
     static constexpr int SZ_AC = 2 * ROWS * KC * 4;   // one flux chunk hi/lo
     static constexpr int SZ_AF = 2 * ROWS * NF * 4;   // face flux hi/lo
-    static constexpr int SZ_QF = E * 4 * Np * 4;      // FP32 deltas of the tile state
-    static constexpr int SZ_Q64 = E * 4 * Np * 8;     // FP64 tile state
+    static constexpr int SZ_QF = STREAM ? 0 : E * 4 * Np * 4;   // FP32 deltas of the tile state
+    static constexpr int SZ_Q64 = STREAM ? 0 : E * 4 * Np * 8;  // FP64 tile state
     static constexpr int SZ_QB = ROWS * 4 + ROWS * 8 + E * 4 * 4;  // reference state FP32 + FP64, FP32 metrics
     static constexpr int al(int x) { return (x + 1023) / 1024 * 1024; }
     static constexpr int OFF_B1 = 0;
     static constexpr int OFF_B2 = OFF_B1 + al(SZ_B1);
-    static constexpr int OFF_A1 = OFF_B2 + al(SZ_B2);
+    static constexpr int AL_BC = al(SZ_BC);           // stride between streamed operand buffers
+    static constexpr int OFF_BC = OFF_B2 + al(SZ_B2);
+    static constexpr int OFF_A1 = OFF_BC + (STREAM ? NBUF * AL_BC : 0);
     static constexpr int OFF_AC = OFF_A1 + al(SZ_A1);
     static constexpr int AL_AC = al(SZ_AC);           // stride between chunk buffers
     static constexpr int OFF_AF = OFF_AC + NBUF * AL_AC;
@@ -81,9 +93,12 @@ struct SplitDims {
     static constexpr int OFF_BAR = OFF_QB + al(SZ_QB);
     static constexpr int SMEM = OFF_BAR + 64;
     static constexpr int RS_FLOATS = E * 4 * Np;      // epilogue staging (aliases chunk buffer 0)
+    static constexpr int TILE_VALS = E * 4 * Np;
+    static constexpr int EPI = (TILE_VALS + THREADS - 1) / THREADS;  // tile values per thread
     static_assert(RS_FLOATS * 4 <= SZ_AC, "epilogue staging does not fit");
     static_assert(SMEM <= 232448, "shared memory budget");
-    static_assert(Nfq <= 8, "face groups are 8 lanes");
+    static_assert(Nfq <= FG && Nfp <= FG, "face group width");
+    static_assert(!STREAM || NBUF == 2, "streamed operand buffers pair with two chunk buffers");
     static constexpr int TMEM_COLS = 256;
     static constexpr int D2_COL = 128;
     static_assert(NG <= 128 && NP2 <= 128, "tensor memory layout");
@@ -125,11 +140,21 @@ __global__ void __launch_bounds__(512, 1) euler_stage_split_kernel(SplitArgs sa)
     uint64_t* bar2 = bar1 + 1;  // [NBUF]
     uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bar1 + 3);
     volatile int* fail_flag = reinterpret_cast<volatile int*>(bar1 + 4);  // set by thread 0, read after a barrier
+    uint64_t* bfull = bar1 + 5;  // [NBUF] streamed operand buffer filled (N = 7)
 
     const EulerArgs& a = sa.e;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int ntiles = (a.K + E - 1) / E;
     const float gamma = (float)a.gamma;
+    // streamed [Sr|Ss] chunks (N = 7): thread 0 issues the bulk copies and
+    // tracks the buffers' phases and copies in flight
+    const float* bsrc = sa.b2 + D::SZ_B2 / 4;
+    uint32_t pb = 0, pend = 0;  // bit b: buffer b's phase parity / a copy in flight
+    auto issue_chunk = [&](int c, int b) {
+        umma::mbar_arrive_expect_tx(bfull + b, D::SZ_BC);
+        umma::bulk_g2s(smem + D::OFF_BC + b * D::AL_BC, bsrc + (size_t)c * (D::SZ_BC / 4), D::SZ_BC, bfull + b);
+        pend |= 1u << b;
+    };
 
     // constant operands and zero padding, once per CTA
     {
@@ -146,7 +171,15 @@ __global__ void __launch_bounds__(512, 1) euler_stage_split_kernel(SplitArgs sa)
         *fail_flag = 0;
         umma::mbar_init(bar1, 1);
         for (int b = 0; b < D::NBUF; b++) umma::mbar_init(bar2 + b, 1);
+        if constexpr (D::STREAM)
+            for (int b = 0; b < D::NBUF; b++) umma::mbar_init(bfull + b, 1);
         umma::fence_mbar_init();
+        if constexpr (D::STREAM) {
+            if ((int)blockIdx.x < ntiles) {
+                issue_chunk(0, 0);
+                issue_chunk(1, 1);
+            }
+        }
     }
     if (warp == 0) {
         umma::tmem_alloc(tmem_slot, D::TMEM_COLS);
@@ -163,10 +196,11 @@ __global__ void __launch_bounds__(512, 1) euler_stage_split_kernel(SplitArgs sa)
     const uint32_t aB1 = umma::smem_u32(sB1), aB2 = umma::smem_u32(sB2);
     const uint32_t aA1 = umma::smem_u32(sA1), aAF = umma::smem_u32(sAF);
     const uint32_t aAC = umma::smem_u32(smem + D::OFF_AC);
-    constexpr uint32_t LO_B1 = NG * KP1 * 4, LO_B2 = NP2 * KP2 * 4, LO_A1 = 128 * KP1 * 4, LO_AC = 128 * KC * 4,
-                       LO_AF = 128 * NF * 4, STRIDE_AC = D::AL_AC;
+    constexpr uint32_t LO_B1 = NG * KP1 * 4, LO_B2 = D::SZ_B2 / 2, LO_A1 = 128 * KP1 * 4, LO_AC = 128 * KC * 4,
+                       LO_AF = 128 * NF * 4, STRIDE_AC = D::AL_AC, LO_BC = D::SZ_BC / 2;
+    const uint32_t aBC = umma::smem_u32(smem + D::OFF_BC);
     uint32_t ph1 = 0;
-    uint32_t ph2[2] = {0, 0};
+    uint32_t ph2 = 0;  // bit b: phase parity of chunk buffer b's MMA barrier
     bool failed = false;
 
     // this thread's rows in the element-major TMEM layout r = 4 e + v; the
@@ -183,35 +217,72 @@ __global__ void __launch_bounds__(512, 1) euler_stage_split_kernel(SplitArgs sa)
         //      deltas.  FP64 work is one subtraction and one conversion per
         //      value: GB300 retires 2 FP64 operations per clock per SM, and
         //      conversions there are the kernel's scarcest resource.
-        {
-            const double* qin = a.qin + (size_t)k0 * 4 * Np;
-            for (int i = tid; i < ne * 4 * Np; i += blockDim.x) sQ64[i] = qin[i];
-        }
-        __syncthreads();
-        if (tid < D::ROWS) {
-            const int e = tid >> 2, v = tid & 3;
-            float qb = 1.f;
-            if (e < ne) {
-                const double* row = sQ64 + e * 4 * Np + v * Np;  // ring order: vertices at 0, N, 2N
-                qb = (float)((row[0] + row[N] + row[2 * N]) * (1.0 / 3.0));
+        const double* qtile = a.qin + (size_t)k0 * 4 * Np;
+        if constexpr (D::STREAM) {
+            // no FP64 tile copy: the values stay in registers between the two
+            // barriers, the reference state reads its vertex values from L2
+            double qv[D::EPI];
+#pragma unroll
+            for (int j = 0; j < D::EPI; j++) {
+                const int i = tid + j * D::THREADS;
+                qv[j] = i < ne * 4 * Np ? __ldg(qtile + i) : 0.0;
             }
-            sQB[tid] = qb;
-            sQBd[tid] = (double)qb;
-        } else if (tid < D::ROWS + 4 * E) {
-            const int e = (tid - D::ROWS) >> 2, c = (tid - D::ROWS) & 3;
-            sGeo[tid - D::ROWS] = e < ne ? (float)a.geo[(size_t)(k0 + e) * 4 + c] : 0.f;
-        }
-        __syncthreads();
-        for (int i = tid; i < ne * 4 * Np; i += blockDim.x) {
-            const int e = i / (4 * Np), rem = i - e * 4 * Np, v = rem / Np, p = rem - v * Np;
-            const int r = 4 * e + v;
-            const float d = (float)(sQ64[i] - sQBd[r]);
-            sQF[i] = d;
-            float hi, lo;
-            umma::split_tf32(d, hi, lo);
-            const uint32_t off = umma::kmajor_offset(r, p, KP1) >> 2;
-            sA1[off] = hi;
-            sA1[off + LO_A1 / 4] = lo;
+            if (tid < D::ROWS) {
+                const int e = tid >> 2, v = tid & 3;
+                float qb = 1.f;
+                if (e < ne) {
+                    const double* row = qtile + e * 4 * Np + v * Np;  // ring order: vertices at 0, N, 2N
+                    qb = (float)((__ldg(row) + __ldg(row + N) + __ldg(row + 2 * N)) * (1.0 / 3.0));
+                }
+                sQB[tid] = qb;
+                sQBd[tid] = (double)qb;
+            } else if (tid < D::ROWS + 4 * E) {
+                const int e = (tid - D::ROWS) >> 2, c = (tid - D::ROWS) & 3;
+                sGeo[tid - D::ROWS] = e < ne ? (float)a.geo[(size_t)(k0 + e) * 4 + c] : 0.f;
+            }
+            __syncthreads();
+#pragma unroll
+            for (int j = 0; j < D::EPI; j++) {
+                const int i = tid + j * D::THREADS;
+                if (i < ne * 4 * Np) {
+                    const int e = i / (4 * Np), rem = i - e * 4 * Np, v = rem / Np, p = rem - v * Np;
+                    const int r = 4 * e + v;
+                    const float d = (float)(qv[j] - sQBd[r]);
+                    float hi, lo;
+                    umma::split_tf32(d, hi, lo);
+                    const uint32_t off = umma::kmajor_offset(r, p, KP1) >> 2;
+                    sA1[off] = hi;
+                    sA1[off + LO_A1 / 4] = lo;
+                }
+            }
+        } else {
+            for (int i = tid; i < ne * 4 * Np; i += blockDim.x) sQ64[i] = qtile[i];
+            __syncthreads();
+            if (tid < D::ROWS) {
+                const int e = tid >> 2, v = tid & 3;
+                float qb = 1.f;
+                if (e < ne) {
+                    const double* row = sQ64 + e * 4 * Np + v * Np;  // ring order: vertices at 0, N, 2N
+                    qb = (float)((row[0] + row[N] + row[2 * N]) * (1.0 / 3.0));
+                }
+                sQB[tid] = qb;
+                sQBd[tid] = (double)qb;
+            } else if (tid < D::ROWS + 4 * E) {
+                const int e = (tid - D::ROWS) >> 2, c = (tid - D::ROWS) & 3;
+                sGeo[tid - D::ROWS] = e < ne ? (float)a.geo[(size_t)(k0 + e) * 4 + c] : 0.f;
+            }
+            __syncthreads();
+            for (int i = tid; i < ne * 4 * Np; i += blockDim.x) {
+                const int e = i / (4 * Np), rem = i - e * 4 * Np, v = rem / Np, p = rem - v * Np;
+                const int r = 4 * e + v;
+                const float d = (float)(sQ64[i] - sQBd[r]);
+                sQF[i] = d;
+                float hi, lo;
+                umma::split_tf32(d, hi, lo);
+                const uint32_t off = umma::kmajor_offset(r, p, KP1) >> 2;
+                sA1[off] = hi;
+                sA1[off + LO_A1 / 4] = lo;
+            }
         }
         umma::fence_async_smem();
         umma::fence_before_sync();
@@ -231,14 +302,16 @@ __global__ void __launch_bounds__(512, 1) euler_stage_split_kernel(SplitArgs sa)
             }
             umma::commit(bar1);
         }
-        // ---- (B) face fluxes while GEMM1 runs: 8-lane groups per (element, face),
+        // ---- (B) face fluxes while GEMM1 runs: FG-lane groups per (element, face),
         //      lane i = face node i (gather) and face Gauss point i (flux)
         {
-            const int i = lane & 7;
-            // 96 groups of 8 lanes over 512 threads: warps 0-7 take two groups, 8-15 one
-            // (the bound is warp-uniform, so the shuffles below see full warps)
+            constexpr int FG = D::FG;
+            const int i = lane & (FG - 1);
+            // 96 groups over 512 threads: with 8 lanes warps 0-7 take two groups and
+            // 8-15 one, with 16 lanes every warp takes three (the bound is
+            // warp-uniform, so the shuffles below see full warps)
 #pragma unroll 1
-            for (int G = tid >> 3; G < 3 * E; G += D::THREADS / 8) {
+            for (int G = tid / FG; G < 3 * E; G += D::THREADS / FG) {
                 const int e = G / 3, f = G - 3 * e;
                 const bool valid = e < ne;
                 const int k = k0 + (valid ? e : 0);
@@ -252,8 +325,16 @@ __global__ void __launch_bounds__(512, 1) euler_stage_split_kernel(SplitArgs sa)
                 }
                 if (valid && i < Nfp) {
                     const int pos = (f * N + i) % NB;
+                    if constexpr (D::STREAM) {
 #pragma unroll
-                    for (int v = 0; v < 4; v++) own[v] = sQF[e * 4 * Np + v * Np + pos];
+                        for (int v = 0; v < 4; v++) {
+                            const uint32_t off = umma::kmajor_offset(4 * e + v, pos, KP1) >> 2;
+                            own[v] = sA1[off] + sA1[off + LO_A1 / 4];  // exact: lo = d - hi
+                        }
+                    } else {
+#pragma unroll
+                        for (int v = 0; v < 4; v++) own[v] = sQF[e * 4 * Np + v * Np + pos];
+                    }
                     const int c = __ldg(a.conn + (size_t)k * 3 + f);
                     if (c >= 0) {
                         const int nb = c >> 3, fn = c & 3, rot = (c >> 2) & 1;
@@ -268,7 +349,7 @@ __global__ void __launch_bounds__(512, 1) euler_stage_split_kernel(SplitArgs sa)
                         for (int v = 0; v < 4; v++) nbr[v] = (float)(__ldg(bt + v * Nfp) - qbd[v]);
                     }
                 }
-                // interpolate both traces to Gauss point i (shuffles within the 8-lane group)
+                // interpolate both traces to Gauss point i (shuffles within the group)
                 float dm[4] = {0.f, 0.f, 0.f, 0.f}, dp[4] = {0.f, 0.f, 0.f, 0.f};
                 const int gi = i < Nfq ? i : 0;
 #pragma unroll
@@ -276,8 +357,8 @@ __global__ void __launch_bounds__(512, 1) euler_stage_split_kernel(SplitArgs sa)
                     const float w = (float)__ldg(a.ops.If + gi * Nfp + jn);
 #pragma unroll
                     for (int v = 0; v < 4; v++) {
-                        dm[v] = fmaf(w, __shfl_sync(0xffffffffu, own[v], jn, 8), dm[v]);
-                        dp[v] = fmaf(w, __shfl_sync(0xffffffffu, nbr[v], jn, 8), dp[v]);
+                        dm[v] = fmaf(w, __shfl_sync(0xffffffffu, own[v], jn, FG), dm[v]);
+                        dp[v] = fmaf(w, __shfl_sync(0xffffffffu, nbr[v], jn, FG), dp[v]);
                     }
                 }
                 const float* gk = sGeo + 4 * (valid ? e : 0);
@@ -293,7 +374,7 @@ __global__ void __launch_bounds__(512, 1) euler_stage_split_kernel(SplitArgs sa)
                                                   wave_speed_delta(gamma, nx, ny, b, pp))
                                           : 0.f;
 #pragma unroll
-                    for (int o = 1; o < 8; o <<= 1) lam = fmaxf(lam, __shfl_xor_sync(0xffffffffu, lam, o, 8));
+                    for (int o = 1; o < FG; o <<= 1) lam = fmaxf(lam, __shfl_xor_sync(0xffffffffu, lam, o, FG));
                     lf_flux_delta(nx, ny, lam, b, dm, pm, dp, pp, F);
                 }
                 if (valid && i < Nfq) {
@@ -329,13 +410,15 @@ __global__ void __launch_bounds__(512, 1) euler_stage_split_kernel(SplitArgs sa)
             float fr[1][4], fs[1][4];
             {
                 // gather the 4 variables at point (sub*4 + my_v) from the element's 4 lanes
-                float dq[4];
+                float got[4], dq[4];
 #pragma unroll
                 for (int s = 0; s < 4; s++) {
                     const float send = pick4(x, (my_v + s) & 3);
-                    const float got = __shfl_sync(0xffffffffu, send, (lane & ~3) | ((my_v - s) & 3));
-                    dq[(my_v - s) & 3] = got;
+                    got[s] = __shfl_sync(0xffffffffu, send, (lane & ~3) | ((my_v - s) & 3));
                 }
+                // variable t arrived in round s = (my_v - t) mod 4 (selects, no local memory)
+#pragma unroll
+                for (int t = 0; t < 4; t++) dq[t] = pick4(got, (my_v - t) & 3);
                 const int g = ch * CH + sub * 4 + my_v;
                 if (g < Ng && my_e < ne) {
                     const DeltaPrim d = delta_prim(gamma, bref, dq);
@@ -354,13 +437,13 @@ __global__ void __launch_bounds__(512, 1) euler_stage_split_kernel(SplitArgs sa)
             if constexpr (D::NBUF >= 2) {
                 // buffer reuse: thread 0 confirmed, before the previous chunk's
                 // barrier, that the MMAs which last read this buffer are complete
-                if (ch >= D::NBUF) ph2[buf] ^= 1;
+                if (ch >= D::NBUF) ph2 ^= 1u << buf;
             } else {
                 // one buffer: the previous chunk's MMAs are issued after its barrier,
                 // so every thread waits for them here
                 if (ch >= D::NBUF) {
-                    ok = umma::mbar_wait(bar2 + buf, ph2[buf], kWaitLimit);
-                    ph2[buf] ^= 1;
+                    ok = umma::mbar_wait(bar2 + buf, (ph2 >> buf) & 1u, kWaitLimit);
+                    ph2 ^= 1u << buf;
                     if (__syncthreads_or(!ok)) { failed = true; break; }
                 }
             }
@@ -387,7 +470,19 @@ __global__ void __launch_bounds__(512, 1) euler_stage_split_kernel(SplitArgs sa)
                 // MMAs were issued before this point
                 if (tid == 0 && ch + 1 < D::NCH && ch + 1 >= D::NBUF) {
                     const int nb = (ch + 1) % D::NBUF;
-                    if (!umma::mbar_wait(bar2 + nb, ph2[nb], kWaitLimit)) *fail_flag = 1;
+                    if (!umma::mbar_wait(bar2 + nb, (ph2 >> nb) & 1u, kWaitLimit)) *fail_flag = 1;
+                    else if constexpr (D::STREAM) issue_chunk(ch + 1, nb);  // its buffer is free now
+                }
+            }
+            if constexpr (D::STREAM) {
+                // this chunk's [Sr|Ss] slice has landed (issued one chunk earlier)
+                if (tid == 0) {
+                    if (!umma::mbar_wait(bfull + buf, (pb >> buf) & 1u, kWaitLimit)) {
+                        *fail_flag = 1;
+                    } else {
+                        pend &= ~(1u << buf);
+                        pb ^= 1u << buf;
+                    }
                 }
             }
             __syncthreads();
@@ -398,12 +493,20 @@ __global__ void __launch_bounds__(512, 1) euler_stage_split_kernel(SplitArgs sa)
                 const uint32_t aC = aAC + buf * STRIDE_AC;
 #pragma unroll
                 for (int s = 0; s < KC / 8; s++) {
-                    // chunk K step s: Fr part (s < 2) at B2 k = ch*CH + 8s, Fs part at NG + ch*CH + 8(s-2)
-                    const int kb = (s < CH / 8) ? (ch * CH + 8 * s) : (NG + ch * CH + 8 * (s - CH / 8));
                     const uint64_t ah = umma::smem_desc(aC + s * 256, 128, sboA);
                     const uint64_t al = umma::smem_desc(aC + LO_AC + s * 256, 128, sboA);
-                    const uint64_t bh = umma::smem_desc(aB2 + kb * 32, 128, sboB);
-                    const uint64_t bl = umma::smem_desc(aB2 + LO_B2 + kb * 32, 128, sboB);
+                    uint64_t bh, bl;
+                    if constexpr (D::STREAM) {
+                        // the streamed slice has the chunk's own K layout [Sr 16 | Ss 16]
+                        const uint32_t bC = aBC + buf * D::AL_BC;
+                        bh = umma::smem_desc(bC + s * 256, 128, sboA);
+                        bl = umma::smem_desc(bC + LO_BC + s * 256, 128, sboA);
+                    } else {
+                        // chunk K step s: Fr part (s < 2) at B2 k = ch*CH + 8s, Fs part at NG + ch*CH + 8(s-2)
+                        const int kb = (s < CH / 8) ? (ch * CH + 8 * s) : (NG + ch * CH + 8 * (s - CH / 8));
+                        bh = umma::smem_desc(aB2 + kb * 32, 128, sboB);
+                        bl = umma::smem_desc(aB2 + LO_B2 + kb * 32, 128, sboB);
+                    }
                     const uint32_t acc = (ch > 0 || s > 0) ? 1u : 0u;
                     umma::mma_tf32(tD2, ah, bh, idesc2, acc);
                     umma::mma_tf32(tD2, al, bh, idesc2, 1);
@@ -413,11 +516,13 @@ __global__ void __launch_bounds__(512, 1) euler_stage_split_kernel(SplitArgs sa)
                     constexpr uint32_t sboF = (NF / 4) * 128;
 #pragma unroll
                     for (int s = 0; s < NF / 8; s++) {
-                        const int kb = 2 * NG + 8 * s;
+                        // lift part: B2 k = 2 NG + 8s (resident image), or k = 8s of the lift-only image
+                        const int kb = D::STREAM ? 8 * s : 2 * NG + 8 * s;
+                        constexpr uint32_t sbo = D::STREAM ? sboF : sboB;
                         const uint64_t ah = umma::smem_desc(aAF + s * 256, 128, sboF);
                         const uint64_t al = umma::smem_desc(aAF + LO_AF + s * 256, 128, sboF);
-                        const uint64_t bh = umma::smem_desc(aB2 + kb * 32, 128, sboB);
-                        const uint64_t bl = umma::smem_desc(aB2 + LO_B2 + kb * 32, 128, sboB);
+                        const uint64_t bh = umma::smem_desc(aB2 + kb * 32, 128, sbo);
+                        const uint64_t bl = umma::smem_desc(aB2 + LO_B2 + kb * 32, 128, sbo);
                         umma::mma_tf32(tD2, ah, bh, idesc2, 1);
                         umma::mma_tf32(tD2, al, bh, idesc2, 1);
                         umma::mma_tf32(tD2, ah, bl, idesc2, 1);
@@ -428,9 +533,10 @@ __global__ void __launch_bounds__(512, 1) euler_stage_split_kernel(SplitArgs sa)
         }
         if (failed) break;
         // the epilogue's RK register values, loaded while the last MMAs run
-        constexpr int EPI = (E * 4 * Np + D::THREADS - 1) / D::THREADS;
+        constexpr int EPI = D::EPI;
         const bool first = (a.rka == 0.0);
         float resp[EPI];
+        double q0v[D::STREAM ? EPI : 1];  // N = 7: the stage input again (L2)
         {
             const size_t base = (size_t)k0 * 4 * Np;
             const bool need = a.mode == MODE_LSERK && !first;
@@ -438,6 +544,7 @@ __global__ void __launch_bounds__(512, 1) euler_stage_split_kernel(SplitArgs sa)
             for (int j = 0; j < EPI; j++) {
                 const int i = tid + j * D::THREADS;
                 resp[j] = (need && i < ne * 4 * Np) ? __ldg(sa.res32 + base + i) : 0.f;
+                if constexpr (D::STREAM) q0v[j] = (a.mode != MODE_RHS && i < ne * 4 * Np) ? __ldg(qtile + i) : 0.0;
             }
         }
         // outstanding commits: the last NBUF chunks (one per buffer)
@@ -446,12 +553,19 @@ __global__ void __launch_bounds__(512, 1) euler_stage_split_kernel(SplitArgs sa)
             const int chb = D::NCH - D::NBUF + b;
             if (chb < 0) continue;
             const int buf = (D::NBUF == 2) ? (chb & 1) : 0;
-            ok = umma::mbar_wait(bar2 + buf, ph2[buf], kWaitLimit);
-            ph2[buf] ^= 1;
+            ok = umma::mbar_wait(bar2 + buf, (ph2 >> buf) & 1u, kWaitLimit);
+            ph2 ^= 1u << buf;
             if (__syncthreads_or(!ok)) { failed = true; break; }
         }
         if (failed) break;
         umma::fence_after_sync();
+        if constexpr (D::STREAM) {
+            // every MMA of this tile is complete: prefetch the next tile's first two slices
+            if (tid == 0 && tile + (int)gridDim.x < ntiles) {
+                issue_chunk(0, 0);
+                issue_chunk(1, 1);
+            }
+        }
         // ---- (D) epilogue: R (tensor memory) -> staging -> coalesced stage update
         {
 #pragma unroll
@@ -476,7 +590,9 @@ __global__ void __launch_bounds__(512, 1) euler_stage_split_kernel(SplitArgs sa)
                 const int i = tid + j * D::THREADS;
                 if (i >= ne * 4 * Np) break;
                 const float R = sRS[i];
-                const double q0 = sQ64[i];
+                double q0;
+                if constexpr (D::STREAM) q0 = q0v[j];
+                else q0 = sQ64[i];
                 const size_t idx = base + i;
                 const float dtf = a.dtk ? (float)(a.dt * a.dtk[k0 + i / (4 * Np)]) : dtf0;
                 switch (a.mode) {
@@ -494,6 +610,12 @@ __global__ void __launch_bounds__(512, 1) euler_stage_split_kernel(SplitArgs sa)
         __syncthreads();  // staging buffers are rewritten by the next tile
     }
     if (failed && tid == 0) atomicExch(sa.status, 1);
+    if constexpr (D::STREAM) {
+        // after a timeout: let this CTA's bulk copies in flight land before it exits
+        if (tid == 0)
+            for (int b = 0; b < D::NBUF; b++)
+                if ((pend >> b) & 1u) umma::mbar_wait(bfull + b, (pb >> b) & 1u, kWaitLimit);
+    }
     umma::fence_before_sync();
     __syncthreads();
     if (warp == 0) umma::tmem_dealloc(tmem, D::TMEM_COLS);
@@ -537,13 +659,29 @@ static int setup_n(dg_ctx* c) {
     std::vector<float> b1 = operand_image(D::NG, D::KP1, [&](int g, int p) {
         return (g < Ng && p < Np) ? o.dVg[(size_t)g * Np + p] : 0.0;
     });
-    std::vector<float> b2 = operand_image(D::NP2, D::KP2, [&](int p, int k) {
-        if (p >= Np) return 0.0;
-        if (k < NG) return k < Ng ? o.dSr[(size_t)p * Ng + k] : 0.0;
-        if (k < 2 * NG) return (k - NG) < Ng ? o.dSs[(size_t)p * Ng + (k - NG)] : 0.0;
-        const int cc = k - 2 * NG;
-        return cc < 3 * Nfq ? o.dLift[(size_t)p * 3 * Nfq + cc] : 0.0;
-    });
+    std::vector<float> b2;
+    if (D::STREAM) {
+        // lift image (resident), then one [Sr 16 | Ss 16] image per chunk (streamed)
+        b2 = operand_image(D::NP2, D::NF, [&](int p, int cc) {
+            return (p < Np && cc < 3 * Nfq) ? o.dLift[(size_t)p * 3 * Nfq + cc] : 0.0;
+        });
+        for (int ch = 0; ch < D::NCH; ch++) {
+            std::vector<float> bc = operand_image(D::NP2, D::KC, [&](int p, int k) {
+                const int g = ch * D::CH + (k < D::CH ? k : k - D::CH);
+                if (p >= Np || g >= Ng) return 0.0;
+                return k < D::CH ? o.dSr[(size_t)p * Ng + g] : o.dSs[(size_t)p * Ng + g];
+            });
+            b2.insert(b2.end(), bc.begin(), bc.end());
+        }
+    } else {
+        b2 = operand_image(D::NP2, D::KP2, [&](int p, int k) {
+            if (p >= Np) return 0.0;
+            if (k < NG) return k < Ng ? o.dSr[(size_t)p * Ng + k] : 0.0;
+            if (k < 2 * NG) return (k - NG) < Ng ? o.dSs[(size_t)p * Ng + (k - NG)] : 0.0;
+            const int cc = k - 2 * NG;
+            return cc < 3 * Nfq ? o.dLift[(size_t)p * 3 * Nfq + cc] : 0.0;
+        });
+    }
     size_t bytes = (b1.size() + b2.size()) * sizeof(float);
     float* d = nullptr;
     if (cudaMalloc(&d, bytes) != cudaSuccess) return DG_ERR_NOMEM;
@@ -595,6 +733,7 @@ cudaError_t launch_euler_split(int N, const EulerArgs& a, const SplitPlan& plan,
         case 4: return launch_split_n<4>(a, plan, s);
         case 5: return launch_split_n<5>(a, plan, s);
         case 6: return launch_split_n<6>(a, plan, s);
+        case 7: return launch_split_n<7>(a, plan, s);
         default: return cudaErrorNotSupported;
     }
 }
@@ -610,7 +749,8 @@ int split_setup(dg_ctx* c) {
         case 4: return dgk::setup_n<4>(c);
         case 5: return dgk::setup_n<5>(c);
         case 6: return dgk::setup_n<6>(c);
-        default: return DG_ERR_UNSUPPORTED;  // N = 7 needs a streamed operator (does not fit shared memory)
+        case 7: return dgk::setup_n<7>(c);
+        default: return DG_ERR_UNSUPPORTED;
     }
 }
 

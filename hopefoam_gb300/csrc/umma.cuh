@@ -90,6 +90,22 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* mbar, uint32_t phase, uint32
     return false;
 }
 
+// arrive once on an mbarrier and add `bytes` to the transaction count its
+// current phase waits for
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* mbar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(mbar)), "r"(bytes)
+                 : "memory");
+}
+
+// untiled bulk copy global -> shared (both 16-byte aligned, bytes a multiple
+// of 16); completion is signalled as transactions on `mbar`
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* mbar) {
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(smem_u32(dst)),
+        "l"(src), "r"(bytes), "r"(smem_u32(mbar))
+        : "memory");
+}
+
 // make generic-proxy shared-memory writes visible to the tensor core (async proxy)
 __device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
 

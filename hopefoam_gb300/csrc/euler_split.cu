@@ -27,14 +27,16 @@
 // Per tile: stage q (FP64 tile in shared memory, reference state, FP32 deltas,
 // TF32 hi/lo in the canonical no-swizzle K-major layout, see umma.cuh) ->
 // GEMM1 (issued by one thread, completion on an mbarrier) -> face fluxes in
-// 8-lane groups (gather, Gauss interpolation and wave-speed max by shuffles)
-// while GEMM1 runs -> per chunk of 16 cubature points: tensor memory ->
+// 8-lane groups, 16 at N = 7 (gather, Gauss interpolation and wave-speed max
+// by shuffles) while GEMM1 runs -> per chunk of 16 cubature points: tensor memory ->
 // registers, the 4 variables of a point exchanged by warp shuffles within
 // the element's 4 lanes -> FP32 delta flux -> TF32 split into a
 // double-buffered chunk operand -> GEMM2 MMAs for that K chunk -> epilogue:
-// tensor memory -> shared -> coalesced LSERK update.  All mbarrier waits are
-// bounded; a timeout sets the status word, the CTA frees tensor memory and
-// returns.
+// tensor memory -> shared -> coalesced LSERK update.  At N = 7 the volume
+// operator is streamed from L2 per chunk and the tile is not copied to shared
+// memory (SplitDims::STREAM).  All mbarrier waits are bounded; a timeout sets
+// the status word, the CTA waits for its bulk copies in flight, frees tensor
+// memory and returns.
 #include <cstdio>
 #include <cstring>
 #include <vector>

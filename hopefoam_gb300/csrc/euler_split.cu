@@ -19,9 +19,11 @@
 // Because the weak divergence of a constant flux cancels against its own
 // surface term, R is unchanged by the shift, but the FP32 round-off now
 // scales with the variation inside an element instead of with |F| N^2 / h.
-// The state q stays FP64 in HBM (dQ = q - qb is formed in FP64); the
-// low-storage RK register is FP32 (it carries dt*R, whose own precision is
-// FP32); q += b*res is the only FP64 arithmetic per value in the update.
+// The state q stays FP64 in HBM; dQ = q - qb (and the neighbour traces' deltas)
+// is one FP64 subtraction and conversion per value (at N = 7 it is formed from
+// q's bits with integer and FP32 operations, f64split.cuh); the low-storage RK
+// register is FP32 (it carries dt*R, whose own precision is FP32); q += b*res
+// is the only other FP64 arithmetic per value.
 //
 // Structure: persistent CTAs (one per SM, 512 threads), 32 elements per tile.
 // Per tile: stage q (FP64 tile in shared memory, reference state, FP32 deltas,
@@ -44,6 +46,7 @@
 #include "../../include/dgcu.h"
 #include "dg_ctx.hpp"
 #include "euler_flux.cuh"
+#include "f64split.cuh"
 #include "umma.cuh"
 
 namespace dgk {
@@ -64,8 +67,8 @@ struct SplitDims {
     // the other operands.  It is streamed per chunk by bulk copies into
     // buffers that pair with the flux chunk buffers (only the lift part stays
     // resident), the FP64 tile copy is dropped (q is re-read from L2 in the
-    // epilogue) and the FP32 deltas are recovered from the TF32 hi + lo
-    // operand, which holds them exactly.
+    // epilogue) and the face phase reads the FP32 deltas back from the TF32
+    // hi + lo operand, which holds them exactly.
     static constexpr bool STREAM = (N == 7);
     static constexpr int NBUF = (N <= 5 || STREAM) ? 2 : 1;  // chunk buffers
     static constexpr int FG = (Nfq <= 8) ? 8 : 16;    // lanes per face group
@@ -79,7 +82,9 @@ struct SplitDims {
     static constexpr int SZ_AF = 2 * ROWS * NF * 4;   // face flux hi/lo
     static constexpr int SZ_QF = STREAM ? 0 : E * 4 * Np * 4;   // FP32 deltas of the tile state
     static constexpr int SZ_Q64 = STREAM ? 0 : E * 4 * Np * 8;  // FP64 tile state
-    static constexpr int SZ_QB = ROWS * 4 + ROWS * 8 + E * 4 * 4;  // reference state FP32 + FP64, FP32 metrics
+    // reference state FP32 (+ FP64 copy on the resident path), FP32 metrics
+    static constexpr int OFF_GEO_IN_QB = ROWS * 4 + (STREAM ? 0 : ROWS * 8);
+    static constexpr int SZ_QB = OFF_GEO_IN_QB + E * 4 * 4;
     static constexpr int al(int x) { return (x + 1023) / 1024 * 1024; }
     static constexpr int OFF_B1 = 0;
     static constexpr int OFF_B2 = OFF_B1 + al(SZ_B1);
@@ -135,8 +140,8 @@ __global__ void __launch_bounds__(512, 1) euler_stage_split_kernel(SplitArgs sa)
     float* sQF = reinterpret_cast<float*>(smem + D::OFF_QF);
     double* sQ64 = reinterpret_cast<double*>(smem + D::OFF_Q64);
     float* sQB = reinterpret_cast<float*>(smem + D::OFF_QB);                      // [ROWS]
-    double* sQBd = reinterpret_cast<double*>(smem + D::OFF_QB + D::ROWS * 4);    // the same values in FP64
-    float* sGeo = reinterpret_cast<float*>(smem + D::OFF_QB + D::ROWS * 12);     // [E][rx, sx, ry, sy]
+    double* sQBd = reinterpret_cast<double*>(smem + D::OFF_QB + D::ROWS * 4);    // FP64 copy (resident path)
+    float* sGeo = reinterpret_cast<float*>(smem + D::OFF_QB + D::OFF_GEO_IN_QB);  // [E][rx, sx, ry, sy]
     float* sRS = reinterpret_cast<float*>(smem + D::OFF_AC);  // after GEMM2 completed
     uint64_t* bar1 = reinterpret_cast<uint64_t*>(smem + D::OFF_BAR);
     uint64_t* bar2 = bar1 + 1;  // [NBUF]
@@ -213,51 +218,62 @@ __global__ void __launch_bounds__(512, 1) euler_stage_split_kernel(SplitArgs sa)
     for (int tile = blockIdx.x; tile < ntiles && !failed; tile += gridDim.x) {
         const int k0 = tile * E;
         const int ne = min(E, a.K - k0);
-        // ---- (A) stage the tile: FP64 copy, per-(element, variable) reference
-        //      state (mean of the three vertex values, rounded to FP32 and kept
-        //      in both precisions), FP32 metrics, FP32 deltas, TF32 hi/lo of the
-        //      deltas.  FP64 work is one subtraction and one conversion per
-        //      value: GB300 retires 2 FP64 operations per clock per SM, and
-        //      conversions there are the kernel's scarcest resource.
+        // ---- (A) stage the tile: per-(element, variable) reference state (the
+        //      mean of the three vertex values, in FP32), FP32 metrics, FP32
+        //      deltas, TF32 hi/lo of the deltas.
         const double* qtile = a.qin + (size_t)k0 * 4 * Np;
         if constexpr (D::STREAM) {
-            // no FP64 tile copy: the values stay in registers between the two
-            // barriers, the reference state reads its vertex values from L2
-            double qv[D::EPI];
+            // N = 7: no FP64 tile copy (the values stay in registers across the
+            // reference-state barrier; the vertex values come from L2), and the
+            // deltas are formed with integer and FP32 operations (f64split.cuh):
+            // at this order the FP64 pipe (2 operations per clock per SM) is the
+            // scarcest resource.  Each warp instruction writes one 8-row x
+            // 4-column core matrix of the K-major operand (lane = (row & 7) * 4 +
+            // (k & 3), 128 contiguous bytes: no bank conflicts); padding rows and
+            // columns are written as zeros.
+            constexpr int NCM = (D::ROWS / 8) * (KP1 / 4);    // core matrices of the dQ operand
+            constexpr int CMW = (NCM + 15) / 16;              // per warp (16 warps)
+            auto cm_val = [&](int cm, int& r, int& k) -> bool {
+                r = (cm / (KP1 / 4)) * 8 + (lane >> 2);
+                k = (cm % (KP1 / 4)) * 4 + (lane & 3);
+                return cm < NCM && (r >> 2) < ne && k < Np;
+            };
+            double qv[CMW];
 #pragma unroll
-            for (int j = 0; j < D::EPI; j++) {
-                const int i = tid + j * D::THREADS;
-                qv[j] = i < ne * 4 * Np ? __ldg(qtile + i) : 0.0;
+            for (int j = 0; j < CMW; j++) {
+                int r, k;
+                qv[j] = cm_val(warp + 16 * j, r, k) ? __ldg(qtile + (size_t)r * Np + k) : 0.0;
             }
             if (tid < D::ROWS) {
                 const int e = tid >> 2, v = tid & 3;
                 float qb = 1.f;
                 if (e < ne) {
                     const double* row = qtile + e * 4 * Np + v * Np;  // ring order: vertices at 0, N, 2N
-                    qb = (float)((__ldg(row) + __ldg(row + N) + __ldg(row + 2 * N)) * (1.0 / 3.0));
+                    qb = (f64s::trunc_f32(__ldg(row)) + f64s::trunc_f32(__ldg(row + N)) +
+                          f64s::trunc_f32(__ldg(row + 2 * N))) * (1.f / 3.f);
                 }
                 sQB[tid] = qb;
-                sQBd[tid] = (double)qb;
             } else if (tid < D::ROWS + 4 * E) {
                 const int e = (tid - D::ROWS) >> 2, c = (tid - D::ROWS) & 3;
                 sGeo[tid - D::ROWS] = e < ne ? (float)a.geo[(size_t)(k0 + e) * 4 + c] : 0.f;
             }
             __syncthreads();
 #pragma unroll
-            for (int j = 0; j < D::EPI; j++) {
-                const int i = tid + j * D::THREADS;
-                if (i < ne * 4 * Np) {
-                    const int e = i / (4 * Np), rem = i - e * 4 * Np, v = rem / Np, p = rem - v * Np;
-                    const int r = 4 * e + v;
-                    const float d = (float)(qv[j] - sQBd[r]);
+            for (int j = 0; j < CMW; j++) {
+                const int cm = warp + 16 * j;
+                int r, k;
+                const bool in = cm_val(cm, r, k);
+                if (cm < NCM) {
                     float hi, lo;
-                    umma::split_tf32(d, hi, lo);
-                    const uint32_t off = umma::kmajor_offset(r, p, KP1) >> 2;
-                    sA1[off] = hi;
-                    sA1[off + LO_A1 / 4] = lo;
+                    umma::split_tf32(in ? f64s::minus_f32(qv[j], sQB[r]) : 0.f, hi, lo);
+                    sA1[cm * 32 + lane] = hi;
+                    sA1[cm * 32 + lane + LO_A1 / 4] = lo;
                 }
             }
         } else {
+            // N <= 6: FP64 tile copy, FP64 reference state copy; one FP64
+            // subtraction and one conversion per value (at these orders the
+            // kernel is issue-bound and the FP64 form takes fewer instructions)
             for (int i = tid; i < ne * 4 * Np; i += blockDim.x) sQ64[i] = qtile[i];
             __syncthreads();
             if (tid < D::ROWS) {
@@ -323,15 +339,16 @@ __global__ void __launch_bounds__(512, 1) euler_stage_split_kernel(SplitArgs sa)
 #pragma unroll
                 for (int v = 0; v < 4; v++) {
                     qbv[v] = sQB[4 * (valid ? e : 0) + v];
-                    qbd[v] = sQBd[4 * (valid ? e : 0) + v];
+                    if constexpr (!D::STREAM) qbd[v] = sQBd[4 * (valid ? e : 0) + v];
                 }
                 if (valid && i < Nfp) {
                     const int pos = (f * N + i) % NB;
                     if constexpr (D::STREAM) {
 #pragma unroll
                         for (int v = 0; v < 4; v++) {
+                            // the FP32 delta, read back from the TF32 operand: hi + lo is exact
                             const uint32_t off = umma::kmajor_offset(4 * e + v, pos, KP1) >> 2;
-                            own[v] = sA1[off] + sA1[off + LO_A1 / 4];  // exact: lo = d - hi
+                            own[v] = sA1[off] + sA1[off + LO_A1 / 4];
                         }
                     } else {
 #pragma unroll
@@ -344,11 +361,15 @@ __global__ void __launch_bounds__(512, 1) euler_stage_split_kernel(SplitArgs sa)
                         const int npos = (fn * N + jj) % NB;
                         const double* qn = a.qin + (size_t)nb * 4 * Np + npos;
 #pragma unroll
-                        for (int v = 0; v < 4; v++) nbr[v] = (float)(__ldg(qn + v * Np) - qbd[v]);
+                        for (int v = 0; v < 4; v++)
+                            nbr[v] = D::STREAM ? f64s::minus_f32(__ldg(qn + v * Np), qbv[v])
+                                               : (float)(__ldg(qn + v * Np) - qbd[v]);
                     } else {
                         const double* bt = a.btrace + (size_t)(-1 - c) * 4 * Nfp + i;
 #pragma unroll
-                        for (int v = 0; v < 4; v++) nbr[v] = (float)(__ldg(bt + v * Nfp) - qbd[v]);
+                        for (int v = 0; v < 4; v++)
+                            nbr[v] = D::STREAM ? f64s::minus_f32(__ldg(bt + v * Nfp), qbv[v])
+                                               : (float)(__ldg(bt + v * Nfp) - qbd[v]);
                     }
                 }
                 // interpolate both traces to Gauss point i (shuffles within the group)
@@ -450,6 +471,8 @@ __global__ void __launch_bounds__(512, 1) euler_stage_split_kernel(SplitArgs sa)
                 }
             }
             {
+                // (4-way bank conflicts: a rotation of the variable order per element
+                // pair removes them but costs more issue slots than it saves)
                 const int gl = sub * 4 + my_v;
 #pragma unroll
                 for (int v = 0; v < 4; v++) {

@@ -29,8 +29,9 @@
 // Per tile: stage q (FP64 tile in shared memory, reference state, FP32 deltas,
 // TF32 hi/lo in the canonical no-swizzle K-major layout, see umma.cuh) ->
 // GEMM1 (issued by one thread, completion on an mbarrier) -> face fluxes in
-// 8-lane groups, 16 at N = 7 (gather, Gauss interpolation and wave-speed max
-// by shuffles) while GEMM1 runs -> per chunk of 16 cubature points: tensor memory ->
+// lane segments, one per (element, face) (gather, Gauss interpolation and
+// wave-speed max by shuffles) while GEMM1 runs -> per chunk of 16 cubature
+// points: tensor memory ->
 // registers, the 4 variables of a point exchanged by warp shuffles within
 // the element's 4 lanes -> FP32 delta flux -> TF32 split into a
 // double-buffered chunk operand -> GEMM2 MMAs for that K chunk -> epilogue:
@@ -71,7 +72,13 @@ struct SplitDims {
     // hi + lo operand, which holds them exactly.
     static constexpr bool STREAM = (N == 7);
     static constexpr int NBUF = (N <= 5 || STREAM) ? 2 : 1;  // chunk buffers
-    static constexpr int FG = (Nfq <= 8) ? 8 : 16;    // lanes per face group
+    // face phase: one (element, face) per segment of SW lanes, SPW segments per
+    // warp.  Power-of-two groups (SW = 8) where packing would not save a pass
+    // over the tile's 96 faces, packed segments (SW = Nfq) otherwise: at N = 7
+    // two passes instead of three, at N <= 3 one instead of two.
+    static constexpr bool PACKED = (N == 7) || (N <= 3);
+    static constexpr int SW = PACKED ? Nfq : 8;
+    static constexpr int SPW = 32 / SW;
     // shared-memory layout (bytes, operand buffers 1024-aligned)
     static constexpr int SZ_B1 = 2 * NG * KP1 * 4;    // Vg hi/lo
     static constexpr int SZ_BC = 2 * NP2 * KC * 4;    // one streamed [Sr|Ss] chunk hi/lo
@@ -104,7 +111,7 @@ struct SplitDims {
     static constexpr int EPI = (TILE_VALS + THREADS - 1) / THREADS;  // tile values per thread
     static_assert(RS_FLOATS * 4 <= SZ_AC, "epilogue staging does not fit");
     static_assert(SMEM <= 232448, "shared memory budget");
-    static_assert(Nfq <= FG && Nfp <= FG, "face group width");
+    static_assert(Nfq <= SW && Nfp <= SW, "face segment width");
     static_assert(!STREAM || NBUF == 2, "streamed operand buffers pair with two chunk buffers");
     static constexpr int TMEM_COLS = 256;
     static constexpr int D2_COL = 128;
@@ -320,18 +327,20 @@ __global__ void __launch_bounds__(512, 1) euler_stage_split_kernel(SplitArgs sa)
             }
             umma::commit(bar1);
         }
-        // ---- (B) face fluxes while GEMM1 runs: FG-lane groups per (element, face),
-        //      lane i = face node i (gather) and face Gauss point i (flux)
+        // ---- (B) face fluxes while GEMM1 runs: one (element, face) per segment of
+        //      SW lanes, lane i = face node i (gather) and face Gauss point i (flux)
         {
-            constexpr int FG = D::FG;
-            const int i = lane & (FG - 1);
-            // 96 groups over 512 threads: with 8 lanes warps 0-7 take two groups and
-            // 8-15 one, with 16 lanes every warp takes three (the bound is
-            // warp-uniform, so the shuffles below see full warps)
+            constexpr int SW = D::SW, SPW = D::SPW;
+            const int seg = lane / SW, i = lane - seg * SW;  // lanes with seg >= SPW idle
+            const int sbase = (seg < SPW ? seg : 0) * SW;     // first lane of this segment
+            // the loop bound is warp-uniform, so the shuffles below see full warps
 #pragma unroll 1
-            for (int G = tid / FG; G < 3 * E; G += D::THREADS / FG) {
-                const int e = G / 3, f = G - 3 * e;
-                const bool valid = e < ne;
+            for (int gbase = warp * SPW; gbase < 3 * E; gbase += (D::THREADS / 32) * SPW) {
+                const int G = gbase + seg;
+                const bool gok = seg < SPW && G < 3 * E;
+                const int Gc = gok ? G : gbase;
+                const int e = Gc / 3, f = Gc - 3 * e;
+                const bool valid = gok && e < ne;
                 const int k = k0 + (valid ? e : 0);
                 float own[4] = {0.f, 0.f, 0.f, 0.f}, nbr[4] = {0.f, 0.f, 0.f, 0.f};
                 float qbv[4];
@@ -380,8 +389,13 @@ __global__ void __launch_bounds__(512, 1) euler_stage_split_kernel(SplitArgs sa)
                     const float w = (float)__ldg(a.ops.If + gi * Nfp + jn);
 #pragma unroll
                     for (int v = 0; v < 4; v++) {
-                        dm[v] = fmaf(w, __shfl_sync(0xffffffffu, own[v], jn, FG), dm[v]);
-                        dp[v] = fmaf(w, __shfl_sync(0xffffffffu, nbr[v], jn, FG), dp[v]);
+                        if constexpr (D::PACKED) {
+                            dm[v] = fmaf(w, __shfl_sync(0xffffffffu, own[v], sbase + jn), dm[v]);
+                            dp[v] = fmaf(w, __shfl_sync(0xffffffffu, nbr[v], sbase + jn), dp[v]);
+                        } else {
+                            dm[v] = fmaf(w, __shfl_sync(0xffffffffu, own[v], jn, SW), dm[v]);
+                            dp[v] = fmaf(w, __shfl_sync(0xffffffffu, nbr[v], jn, SW), dp[v]);
+                        }
                     }
                 }
                 const float* gk = sGeo + 4 * (valid ? e : 0);
@@ -396,8 +410,15 @@ __global__ void __launch_bounds__(512, 1) euler_stage_split_kernel(SplitArgs sa)
                     float lam = (i < Nfq) ? fmaxf(wave_speed_delta(gamma, nx, ny, b, pm),
                                                   wave_speed_delta(gamma, nx, ny, b, pp))
                                           : 0.f;
+                    if constexpr (D::PACKED) {
+                        float m = lam;
 #pragma unroll
-                    for (int o = 1; o < FG; o <<= 1) lam = fmaxf(lam, __shfl_xor_sync(0xffffffffu, lam, o, FG));
+                        for (int j = 0; j < Nfq; j++) m = fmaxf(m, __shfl_sync(0xffffffffu, lam, sbase + j));
+                        lam = m;
+                    } else {
+#pragma unroll
+                        for (int o = 1; o < SW; o <<= 1) lam = fmaxf(lam, __shfl_xor_sync(0xffffffffu, lam, o, SW));
+                    }
                     lf_flux_delta(nx, ny, lam, b, dm, pm, dp, pp, F);
                 }
                 if (valid && i < Nfq) {

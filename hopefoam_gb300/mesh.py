@@ -29,6 +29,10 @@ class Mesh:
     ROT: np.ndarray
     BC: np.ndarray
     name: str = ""
+    # boundary patches (from mesh files): patch[k, f] = index into patch_names
+    # for a boundary face, -1 for an interior face; None when not read from a file
+    patch: np.ndarray = None
+    patch_names: tuple = ()
 
     @property
     def K(self):

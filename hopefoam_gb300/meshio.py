@@ -4,9 +4,10 @@ tutorials/DG/2D/isentropicVortex/vortex0256.msh).
 
 Sections used: ``(10 ...)`` nodes (x y per line), ``(13 (zone first last
 bc type)( ... ))`` faces (``[2] n0 n1 c0 c1`` in hex, c1 = 0 on a boundary),
-``(12 ...)`` cell count.  Triangles are rebuilt from their three edges and made
-counter-clockwise; boundary faces are tagged Dirichlet (the tutorial's exact
-fixed-value boundary).
+``(12 ...)`` cell count, ``(45 (zone type name)())`` zone names.  Triangles are
+rebuilt from their three edges and made counter-clockwise; boundary faces are
+tagged Dirichlet (the tutorial's exact fixed-value boundary) and carry the name
+of their face zone as their patch (``Mesh.patch`` / ``Mesh.patch_names``).
 """
 import re
 
@@ -48,13 +49,14 @@ def read_fluent_msh(path):
                     n = 2
                 ids = [int(t, 16) for t in toks[i:i + n + 2]]
                 i += n + 2
-                faces.append(ids)
+                faces.append(ids + [int(hdr[0], 16)])
+    zone_names = {int(z): name for z, name in re.findall(r"\(45\s*\(\s*(\d+)\s+\S+\s+(\S+?)\)", text)}
     nodes.sort()
     P = np.concatenate([v for _, v in nodes])
-    faces = np.array(faces, dtype=np.int64)  # n0 n1 c0 c1 (1-based, c=0 none)
+    faces = np.array(faces, dtype=np.int64)  # n0 n1 c0 c1 zone (1-based, c=0 none)
     ncell = int(max(faces[:, 2].max(), faces[:, 3].max()))
     edges = [[] for _ in range(ncell)]
-    for n0, n1, c0, c1 in faces:
+    for n0, n1, c0, c1, _ in faces:
         for c in (c0, c1):
             if c > 0:
                 edges[c - 1].append((n0 - 1, n1 - 1))
@@ -69,4 +71,12 @@ def read_fluent_msh(path):
     VXY = P[EToV]
     EToV, VXY = make_ccw(EToV, VXY)
     EToE, EToF, ROT, BC = connect(EToV)
-    return Mesh(EToV, VXY, EToE, EToF, ROT, BC, name=path.split("/")[-1])
+    # patches: the zone of each boundary face, matched on its vertex pair
+    bzones = sorted({int(z) for n0, n1, c0, c1, z in faces if c0 == 0 or c1 == 0})
+    names = tuple(zone_names.get(z, "zone%d" % z) for z in bzones)
+    edge_zone = {(min(n0, n1) - 1, max(n0, n1) - 1): bzones.index(int(z)) for n0, n1, c0, c1, z in faces if c0 == 0 or c1 == 0}
+    patch = -np.ones((ncell, 3), np.int32)
+    for k, f in zip(*np.nonzero(EToE < 0)):
+        a, b = int(EToV[k, f]), int(EToV[k, (f + 1) % 3])
+        patch[k, f] = edge_zone[(min(a, b), max(a, b))]
+    return Mesh(EToV, VXY, EToE, EToF, ROT, BC, name=path.split("/")[-1], patch=patch, patch_names=names)

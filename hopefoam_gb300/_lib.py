@@ -45,6 +45,16 @@ class SolveStats(ctypes.Structure):
     _fields_ = [("iterations", ctypes.c_int32), ("rel_residual", ctypes.c_double), ("ms", ctypes.c_double)]
 
 
+class InsBdata(ctypes.Structure):
+    _fields_ = [("u_value", _dp), ("u_gradient", _dp), ("p_value", _dp), ("p_neumann_extra", _dp),
+                ("p_data_scale", ctypes.c_double), ("u_data_scale", ctypes.c_double)]
+
+
+class InsStats(ctypes.Structure):
+    _fields_ = [("iterations_p", ctypes.c_int32), ("iterations_u", ctypes.c_int32 * 2),
+                ("rel_residual_p", ctypes.c_double), ("rel_residual_u", ctypes.c_double), ("ms", ctypes.c_double)]
+
+
 # name -> (restype, argtypes); every symbol declared in include/dgcu.h
 SIGNATURES = {
     "dg_ctx_create": (ctypes.c_int, [ctypes.POINTER(MeshDesc), ctypes.POINTER(Opts), ctypes.POINTER(_vp)]),
@@ -63,6 +73,17 @@ SIGNATURES = {
     "dg_reference_operators": (ctypes.c_int, [ctypes.c_int, _dp, ctypes.c_int, _dp, _dp, _dp, _dp, _dp, _dp, _dp]),
     "dg_ipdg_setup": (ctypes.c_int, [_vp, ctypes.c_double]),
     "dg_ipdg_apply": (ctypes.c_int, [_vp, _dp, _dp]),
+    "dg_ipdg_set_boundary_types": (ctypes.c_int, [_vp, _ip]),
+    "dg_ipdg_set_mass": (ctypes.c_int, [_vp, ctypes.c_double]),
+    "dg_ins_create": (ctypes.c_int, [ctypes.POINTER(MeshDesc), ctypes.POINTER(Opts), _ip, _ip, ctypes.c_double,
+                                     ctypes.c_double, ctypes.c_double, ctypes.POINTER(_vp)]),
+    "dg_ins_destroy": (ctypes.c_int, [_vp]),
+    "dg_ins_last_error": (ctypes.c_char_p, [_vp]),
+    "dg_ins_set_state": (ctypes.c_int, [_vp, _dp, _dp]),
+    "dg_ins_get_state": (ctypes.c_int, [_vp, _dp, _dp]),
+    "dg_ins_step": (ctypes.c_int, [_vp, ctypes.POINTER(InsBdata), ctypes.c_double, ctypes.c_int,
+                                   ctypes.POINTER(InsStats)]),
+    "dg_ins_operator": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.POINTER(InsBdata), _dp, _dp]),
     "dg_pcg_solve": (ctypes.c_int, [_vp, _dp, _dp, ctypes.c_double, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                     ctypes.POINTER(SolveStats)]),
     "dg_euler_rhs_noalloc": (ctypes.c_int, [_vp, _vp, _vp, ctypes.c_int]),

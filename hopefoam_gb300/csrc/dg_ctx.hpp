@@ -70,5 +70,17 @@ int check_run_args(dg_ctx* c, int flux, int precision);
 int check_split_status(dg_ctx* c, int precision);
 
 // SIPG / PCG state (ipdg_api.cu)
+namespace dgk {
+struct IpdgArgs;
+}
 struct IpdgState;
 void ipdg_teardown(dg_ctx* c);
+// FP64 block-Jacobi PCG with the context's SIPG operator on ring-order device
+// vectors (x: initial guess in, solution out)
+int ipdg_solve_device(dg_ctx* c, const double* b_dev, double* x_dev, double rtol, int maxit, int* iters,
+                      double* rel);
+// the operator's device tables (null before dg_ipdg_setup), the boundary
+// types per slot and the host copy of the face coefficients as built
+const dgk::IpdgArgs* ipdg_args(dg_ctx* c);
+const std::vector<int>* ipdg_btypes(dg_ctx* c);
+const std::vector<double>* ipdg_face_coefs(dg_ctx* c);

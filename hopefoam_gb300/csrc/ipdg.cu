@@ -236,6 +236,13 @@ __global__ void __launch_bounds__(256, 4) ipdg_apply_kernel(IpdgArgs a, const do
             C += o.Sss[p * Np + i] * up;
         }
         T v = o.vc[(size_t)k * 3] * A + o.vc[(size_t)k * 3 + 1] * B + o.vc[(size_t)k * 3 + 2] * C;
+        if (a.mass_coef != 0.0) {
+            // Helmholtz term mass_coef J M u, u = offsets + the element's first-node value
+            T m = o.mrow[i] * ub0[e];
+#pragma unroll
+            for (int p = 0; p < Np; p++) m += o.Mr[p * Np + i] * us[e][p];
+            v += (T)(a.mass_coef * a.J[k]) * m;
+        }
 #pragma unroll
         for (int fg = 0; fg < NF; fg++) v += c2r[e][fg] * o.Drf[fg * Np + i] + c2s[e][fg] * o.Dsf[fg * Np + i];
         if (i < NB) {
@@ -276,8 +283,9 @@ __global__ void ipdg_diag_kernel(IpdgArgs a, double* __restrict__ blocks) {
     if (k >= a.K || j >= Np) return;
     const double vrr = o.vc[(size_t)k * 3], vrs = o.vc[(size_t)k * 3 + 1], vss = o.vc[(size_t)k * 3 + 2];
     double col[Np];
+    const double mc = a.mass_coef * a.J[k];
     for (int i = 0; i < Np; i++)
-        col[i] = vrr * o.Srr[i * Np + j] + vrs * o.Srs2[i * Np + j] + vss * o.Sss[i * Np + j];
+        col[i] = vrr * o.Srr[i * Np + j] + vrs * o.Srs2[i * Np + j] + vss * o.Sss[i * Np + j] + mc * o.Mr[i * Np + j];
     for (int f = 0; f < 3; f++) {
         const double* fc = o.fc + ((size_t)k * 3 + f) * kFaceCoef;
         const double arr = fc[0], ass = fc[1];

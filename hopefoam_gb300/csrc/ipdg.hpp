@@ -20,6 +20,8 @@ struct IpdgOps {
     const T* fc;    // K x 3 x 6 per element face:
                     //   [n.grad r, n.grad s, n.grad r of the neighbour, n.grad s of the neighbour, tau/2, sJ]
     const T* vc;    // K x 3 volume coefficients J (rx^2+ry^2), J (rx sx+ry sy), J (sx^2+sy^2)
+    const T* Mr;    // Np x Np reference mass matrix (J = 1, symmetric)
+    const T* mrow;  // Np row sums of Mr (the mass term acts on offsets plus a constant)
 };
 
 struct IpdgArgs {
@@ -29,6 +31,7 @@ struct IpdgArgs {
     const double* geo;   // K x 4 metrics
     const double* J;     // K Jacobians
     const int* conn;     // K x 3 packed neighbours
+    double mass_coef;    // S + mass_coef M (Helmholtz form); 0: the Laplacian alone
     IpdgOps<double> o64;
     IpdgOps<float> o32;
 };

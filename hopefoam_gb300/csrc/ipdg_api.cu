@@ -23,6 +23,8 @@ struct IpdgState {
     double* d_J = nullptr;
     IpdgOps<double> o64h{};  // device pointers of the operator tables
     IpdgOps<float> o32h{};
+    std::vector<double> fc_host;  // face coefficients as built (boundary types reset sJ from it)
+    std::vector<int> btype;       // per boundary slot: 0 fixesValue, 1 fixesGradient, 2 neither
     double* d_blocks = nullptr;  // FP64 inverse diagonal blocks (row-major per element)
     double* d_P64 = nullptr;     // the same, grouped layout of the element-aligned kernels
     float* d_P32 = nullptr;      // FP32 copy, grouped
@@ -256,6 +258,21 @@ void ipdg_teardown(dg_ctx* c) {
 
 extern "C" {
 
+// block-Jacobi inverse blocks of the current operator
+static int build_blocks(dg_ctx* c) {
+    IpdgState* s = c->ipdg;
+    const IpdgArgs& a = s->args;
+    IP_CUDA(c, cudaMemsetAsync(s->d_status, 0, sizeof(int), c->stream));
+    IP_CUDA(c, launch_ipdg_diag(a, s->d_blocks, c->stream));
+    IP_CUDA(c, launch_invert_blocks(s->d_blocks, nullptr, a.K, a.Np, s->d_status, c->stream));
+    IP_CUDA(c, launch_group_blocks(a, s->d_blocks, s->d_P64, s->d_P32, c->stream));
+    int st = 0;
+    IP_CUDA(c, cudaMemcpyAsync(&st, s->d_status, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+    IP_CUDA(c, cudaStreamSynchronize(c->stream));
+    if (st) return ifail(c, DG_ERR_NONFINITE, "singular diagonal block in the SIPG operator");
+    return DG_OK;
+}
+
 int dg_ipdg_setup(dg_ctx* c, double tau_coef) {
     if (!c || !(tau_coef > 0)) return DG_ERR_ARG;
     ipdg_teardown(c);
@@ -335,6 +352,15 @@ int dg_ipdg_setup(dg_ctx* c, double tau_coef) {
         }
     }
     std::vector<double> Ifh(o.If.begin(), o.If.end());
+    // reference mass matrix in ring order and its row sums
+    std::vector<double> Mr((size_t)Np * Np), mrow(Np, 0.0);
+    for (int i = 0; i < Np; i++)
+        for (int j = 0; j < Np; j++) {
+            Mr[(size_t)i * Np + j] = o.Mref[(size_t)o.ring[i] * Np + o.ring[j]];
+            mrow[i] += Mr[(size_t)i * Np + j];
+        }
+    s->fc_host = fc;
+    s->btype.assign(c->nb, 0);
     auto f32 = [](const std::vector<double>& v) { return std::vector<float>(v.begin(), v.end()); };
     int rc = 0;
     IpdgOps<double>& o64 = s->o64h;
@@ -351,6 +377,10 @@ int dg_ipdg_setup(dg_ctx* c, double tau_coef) {
     rc |= iupload(c, s, (double**)&o64.fw, o.fw);
     rc |= iupload(c, s, (double**)&o64.fc, fc);
     rc |= iupload(c, s, (double**)&o64.vc, vc);
+    rc |= iupload(c, s, (double**)&o64.Mr, Mr);
+    rc |= iupload(c, s, (double**)&o64.mrow, mrow);
+    rc |= iupload(c, s, (float**)&o32.Mr, f32(Mr));
+    rc |= iupload(c, s, (float**)&o32.mrow, f32(mrow));
     rc |= iupload(c, s, (float**)&o32.Srr, f32(Srr));
     rc |= iupload(c, s, (float**)&o32.Srs2, f32(Srs2));
     rc |= iupload(c, s, (float**)&o32.Sss, f32(Sss));
@@ -400,18 +430,43 @@ int dg_ipdg_setup(dg_ctx* c, double tau_coef) {
     a.J = s->d_J;
     a.conn = c->d_conn;
     a.sms = s->sms;
+    a.mass_coef = 0.0;
     a.o64 = o64;
     a.o32 = o32;
-    IP_CUDA(c, cudaMemsetAsync(s->d_status, 0, sizeof(int), c->stream));
-    IP_CUDA(c, launch_ipdg_diag(a, s->d_blocks, c->stream));
-    IP_CUDA(c, launch_invert_blocks(s->d_blocks, nullptr, K, Np, s->d_status, c->stream));
-    IP_CUDA(c, launch_group_blocks(a, s->d_blocks, s->d_P64, s->d_P32, c->stream));
-    int st = 0;
-    IP_CUDA(c, cudaMemcpyAsync(&st, s->d_status, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
-    IP_CUDA(c, cudaStreamSynchronize(c->stream));
-    if (st) return ifail(c, DG_ERR_NONFINITE, "singular diagonal block in the SIPG operator");
+    rc = build_blocks(c);
+    if (rc) return rc;
     s->ready = true;
     return DG_OK;
+}
+
+int dg_ipdg_set_mass(dg_ctx* c, double alpha) {
+    if (!c || !(alpha >= 0)) return DG_ERR_ARG;
+    if (!c->ipdg || !c->ipdg->ready) return ifail(c, DG_ERR_ARG, "dg_ipdg_setup not called");
+    c->ipdg->args.mass_coef = alpha;
+    return build_blocks(c);
+}
+
+int dg_ipdg_set_boundary_types(dg_ctx* c, const int* btype) {
+    if (!c || (!btype && c->nb > 0)) return DG_ERR_ARG;
+    if (!c->ipdg || !c->ipdg->ready) return ifail(c, DG_ERR_ARG, "dg_ipdg_setup not called");
+    IpdgState* s = c->ipdg;
+    for (int i = 0; i < c->nb; i++)
+        if (btype[i] < 0 || btype[i] > 2) return ifail(c, DG_ERR_ARG, "boundary type must be 0, 1 or 2");
+    std::vector<double> fc = s->fc_host;
+    for (int k = 0; k < c->K; k++)
+        for (int f = 0; f < 3; f++) {
+            const int cn = c->conn_host[(size_t)k * 3 + f];
+            if (cn >= 0) continue;
+            s->btype[-1 - cn] = btype[-1 - cn];
+            // no operator terms on faces without a fixed value: their face weight is zero
+            if (btype[-1 - cn] != 0) fc[((size_t)k * 3 + f) * kFaceCoef + 5] = 0.0;
+        }
+    const size_t nfc = fc.size();
+    std::vector<float> fc32(fc.begin(), fc.end());
+    IP_CUDA(c, cudaMemcpyAsync((void*)s->o64h.fc, fc.data(), nfc * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+    IP_CUDA(c, cudaMemcpyAsync((void*)s->o32h.fc, fc32.data(), nfc * sizeof(float), cudaMemcpyHostToDevice, c->stream));
+    IP_CUDA(c, cudaStreamSynchronize(c->stream));
+    return build_blocks(c);
 }
 
 int dg_ipdg_apply(dg_ctx* c, const double* x_host, double* y_host) {
@@ -546,6 +601,63 @@ int dg_pcg_solve(dg_ctx* c, const double* b_host, double* x_host, double rtol, i
 }
 
 }  // extern "C"
+
+// FP64 block-Jacobi PCG on ring-order device vectors (x holds the initial
+// guess and receives the solution); used by the incompressible step
+int ipdg_solve_device(dg_ctx* c, const double* b_dev, double* x_dev, double rtol, int maxit, int* iters,
+                      double* rel_out) {
+    if (!c->ipdg || !c->ipdg->ready) return ifail(c, DG_ERR_ARG, "dg_ipdg_setup not called");
+    IpdgState* s = c->ipdg;
+    const size_t n = (size_t)c->K * c->Np;
+    IP_CUDA(c, cudaMemcpyAsync(s->d_b, b_dev, n * sizeof(double), cudaMemcpyDeviceToDevice, c->stream));
+    IP_CUDA(c, cudaMemcpyAsync(s->d_x, x_dev, n * sizeof(double), cudaMemcpyDeviceToDevice, c->stream));
+    double bb = 0;
+    int rc = dot_host(c, s->d_b, s->d_b, &bb);
+    if (rc) return rc;
+    int total_it = 0, stop = 0;
+    double rr = 0;
+    if (bb == 0.0) {
+        IP_CUDA(c, cudaMemsetAsync(s->d_x, 0, n * sizeof(double), c->stream));
+    } else {
+        PcgVecs v{};
+        v.r = s->d_r;
+        v.z = s->d_z;
+        v.p[0] = s->d_p;
+        v.p[1] = s->d_p2;
+        v.Ap = s->d_Ap;
+        v.part = s->d_ppart;
+        v.nmax = s->nmax;
+        v.P32 = s->d_P32;
+        v.P64 = s->d_P64;
+        v.zb = nullptr;
+        v.S = s->d_S;
+        v.dz = nullptr;
+        v.dp[0] = v.dp[1] = nullptr;
+        v.r32 = nullptr;
+        v.x = s->d_x;
+        rc = apply64(c, s->d_x, s->d_Ap);
+        if (rc) return rc;
+        IP_CUDA(c, launch_xmy(s->d_r, s->d_b, s->d_Ap, n, c->stream));
+        rc = run_cg(c, v, false, rtol * rtol * bb, maxit, s->d_b, 0, &total_it, &stop);
+        if (rc) return rc;
+        rc = apply64(c, s->d_x, s->d_Ap);
+        if (rc) return rc;
+        IP_CUDA(c, launch_xmy(s->d_r, s->d_b, s->d_Ap, n, c->stream));
+        rc = dot_host(c, s->d_r, s->d_r, &rr);
+        if (rc) return rc;
+    }
+    IP_CUDA(c, cudaMemcpyAsync(x_dev, s->d_x, n * sizeof(double), cudaMemcpyDeviceToDevice, c->stream));
+    const double rel = bb > 0 ? std::sqrt(rr / bb) : 0.0;
+    if (iters) *iters = total_it;
+    if (rel_out) *rel_out = rel;
+    if (!(rel == rel) || stop == 2) return ifail(c, DG_ERR_NONFINITE, "PCG breakdown or non-finite residual");
+    if (rel > rtol) return ifail(c, DG_ERR_NOT_CONVERGED, "PCG reached the iteration limit");
+    return DG_OK;
+}
+
+const dgk::IpdgArgs* ipdg_args(dg_ctx* c) { return (c->ipdg && c->ipdg->ready) ? &c->ipdg->args : nullptr; }
+const std::vector<int>* ipdg_btypes(dg_ctx* c) { return c->ipdg ? &c->ipdg->btype : nullptr; }
+const std::vector<double>* ipdg_face_coefs(dg_ctx* c) { return c->ipdg ? &c->ipdg->fc_host : nullptr; }
 
 // ---------------------------------------------------------------------------
 // learned preconditioner

@@ -178,6 +178,19 @@ int dg_batch_run(dg_batch* batch, double dt, int nsteps, int flux, int precision
  * dgMatrix::assembleMatrix (dgMatrices/dgMatrix/dgMatrix.C:383-438). */
 int dg_ipdg_setup(dg_ctx* ctx, double tau_coef);
 
+/* Boundary types of the operator per boundary slot (the context's boundary
+ * faces in element, face order): 0 fixesValue (the SIPG penalty and
+ * consistency terms, defaultLaplacianScheme.C:157-209), 1 fixesGradient and
+ * 2 neither (no operator terms on the face; data enter the right-hand side,
+ * :210-220).  Default after dg_ipdg_setup: all 0.  Rebuilds the block-Jacobi
+ * inverse. */
+int dg_ipdg_set_boundary_types(dg_ctx* ctx, const int* btype);
+
+/* S <- S + alpha M (Helmholtz form of the viscous step, dgChorinFoam.C:92-96:
+ * dgm::Sp(U) * g0/(dt nu) == laplacian(U) + ...); alpha = 0 restores the
+ * Laplacian.  Rebuilds the block-Jacobi inverse. */
+int dg_ipdg_set_mass(dg_ctx* ctx, double alpha);
+
 /* y = S x with S = -A (SPD sign of the reference operator A), matrix-free,
  * FP64; x, y host arrays of K*Np doubles in the reference node order. */
 int dg_ipdg_apply(dg_ctx* ctx, const double* x_host, double* y_host);
@@ -266,6 +279,56 @@ int dg_lpc_apply(dg_ctx* ctx, const double* r_host, double* z_host);
  * in time (other streams, other contexts on the same device) race on it. */
 #define DG_NOALLOC_MAX_VALUES 524288
 int dg_euler_rhs_noalloc(dg_ctx* ctx, const double* q_dev, double* rhs_dev, int flux);
+
+/* ---------------------------------------------------------------------------
+ * Incompressible Navier-Stokes: the velocity-correction (Chorin) step of
+ * tutorials/DG/2D/pearsonVortex/dgChorinFoam/dgChorinFoam.C:63-109, FP64 on
+ * the device (one step = convection, pressure Poisson solve, velocity
+ * correction, Helmholtz solve per velocity component; BDF1/EXT1 on the first
+ * step after dg_ins_set_state, BDF2/EXT2 after).
+ *
+ * Boundary slots are the mesh's boundary faces in element, face order.  Per
+ * slot u_kind: 0 fixedValue, 1 fixedGradient; p_kind: 0 fixedValue,
+ * 2 zeroGradient.  The pressure Neumann data of pEqnCorrect.H apply on the
+ * u_kind 0 slots.  State arrays: U as 2 x K x Np (x then y component), p as
+ * K x Np, reference node order. */
+typedef struct dg_ins dg_ins;
+
+/* Boundary data of one step, host arrays per slot in face-node order
+ * (the order of dg_set_boundary_traces): u_value [nb][2][Nfp] (read on u_kind
+ * 0 slots), u_gradient [nb][2][Nfp] (n.grad U, u_kind 1), p_value [nb][Nfp]
+ * (p_kind 0), p_neumann_extra [nb][Nfp] (added to n.(N + nu curl curl U) in
+ * the pressure Neumann data, u_kind 0: the reference case's n.dU/dt term);
+ * p_data_scale / u_data_scale multiply the Laplacians' boundary-data terms
+ * (the reference case's paraT3 / paraT4 of bCorrectEquation.H). */
+typedef struct {
+    const double* u_value;
+    const double* u_gradient;
+    const double* p_value;
+    const double* p_neumann_extra;
+    double p_data_scale;
+    double u_data_scale;
+} dg_ins_bdata;
+
+typedef struct {
+    int iterations_p;
+    int iterations_u[2];
+    double rel_residual_p;
+    double rel_residual_u;
+    double ms;  /* device time of the step */
+} dg_ins_stats;
+
+int dg_ins_create(const dg_mesh_desc* mesh, const dg_opts* opts, const int* u_kind, const int* p_kind, double nu,
+                  double dt, double tau_coef, dg_ins** out);
+int dg_ins_destroy(dg_ins* ins);
+const char* dg_ins_last_error(const dg_ins* ins);
+int dg_ins_set_state(dg_ins* ins, const double* U_host, const double* p_host);
+int dg_ins_get_state(dg_ins* ins, double* U_host, double* p_host);
+/* one step; the linear solves stop at rtol (relative residual) */
+int dg_ins_step(dg_ins* ins, const dg_ins_bdata* bd, double rtol, int maxit, dg_ins_stats* stats);
+/* one operator of the step alone (parity tests): op 0 div(U (x) U) with the
+ * u_value of bd on u_kind 0 slots, 1 div U, 2 grad p, 3 curl curl U */
+int dg_ins_operator(dg_ins* ins, int op, const dg_ins_bdata* bd, const double* in_host, double* out_host);
 
 /* Host-only (no GPU needed): the reference-element operators this library
  * builds for order N from a cubature rule, in the reference node order.

@@ -944,7 +944,13 @@ static Mat AtDB(const Mat& A, const double* x, const Mat& Bm) {
 // Assembles the reference-sign SIPG operator A (negative semi-definite) and
 // the Dirichlet part of b for boundary data gD (values at boundary face
 // nodes, indexed [face id][Nfp], ignored where NULL -> 0).
-static void ipdg_assemble(const Oracle& O, double tau_coef, Ipdg& L, const double* gD, vec& b) {
+// btype (optional, per element face k*3+f, read on boundary faces):
+// 0 fixesValue (Dirichlet, data gD), 1 fixesGradient (data gN: b -= I^T W I gN,
+// no matrix terms, defaultLaplacianScheme.C:210-220), 2 neither (zeroGradient:
+// nothing).  With kf_data the data arrays are indexed [(k*3+f)*Nfp + i] in the
+// element's own face-node order, else [face id * Nfp + i].
+static void ipdg_assemble(const Oracle& O, double tau_coef, Ipdg& L, const double* gD, vec& b,
+                          const int* btype = nullptr, const double* gN = nullptr, bool kf_data = false) {
     const TriBase& B = O.B;
     int K = O.K, Np = B.Np, Ng = B.Ng, Nfp = B.Nfp, Nfq = B.Nfq, N = B.N;
     L.diag.assign(K, Mat());
@@ -966,15 +972,31 @@ static void ipdg_assemble(const Oracle& O, double tau_coef, Ipdg& L, const doubl
             bool own = (F.owner == k) && (F.fo == f);
             const double* fwJ = F.wJ.data();
             if (F.nbr < 0) {
-                // Dirichlet (fixesValue) boundary face
+                const int bt = btype ? btype[k * 3 + f] : 0;
+                const size_t didx = kf_data ? (size_t)(k * 3 + f) * Nfp : (size_t)O.cellFace[k][f] * Nfp;
                 const Mat& I1 = B.faceInterp;
-                const Mat& Dn1 = F.DnO;
                 const int* m1 = B.fci[F.fo][0];
+                if (bt == 1) {
+                    // fixesGradient: data only
+                    if (gN) {
+                        Mat t = AtDB(I1, fwJ, I1);
+                        const double* g = gN + didx;
+                        for (int i = 0; i < Nfp; i++) {
+                            double s = 0;
+                            for (int j = 0; j < Nfp; j++) s += t(j, i) * g[j];
+                            b[(size_t)k * Np + m1[i]] -= s;
+                        }
+                    }
+                    continue;
+                }
+                if (bt == 2) continue;
+                // Dirichlet (fixesValue) boundary face
+                const Mat& Dn1 = F.DnO;
                 Mat t = AtDB(I1, fwJ, I1);
                 for (auto& e : t.a) e *= gtau;
                 for (int i = 0; i < Nfp; i++)
                     for (int j = 0; j < Nfp; j++) diag(m1[i], m1[j]) -= t(i, j);
-                const double* g = gD ? gD + (size_t)O.cellFace[k][f] * Nfp : nullptr;
+                const double* g = gD ? gD + didx : nullptr;
                 if (g) {
                     for (int i = 0; i < Nfp; i++) {
                         double s = 0;
@@ -1032,6 +1054,202 @@ static void ipdg_assemble(const Oracle& O, double tau_coef, Ipdg& L, const doubl
         }
         L.diag[k] = diag;
     }
+}
+
+// ---------------------------------------------------------------------------
+// Operators of the Chorin (velocity-correction) step of
+// tutorials/DG/2D/pearsonVortex/dgChorinFoam/dgChorinFoam.C:70-96.
+// Vector fields are component-major: u[c * K*Np + k*Np + p], c = 0 (x), 1 (y).
+
+// nodal derivatives of phi_j at node i of element k: d/dx = Dr rx + Ds sx, d/dy = Dr ry + Ds sy
+// (defaultGrad.C:44-78 / defaultDivScheme.C:40-75: drdx at the element's nodes)
+static void node_metrics(const Oracle& O, int k, int i, double& rx, double& sx, double& ry, double& sy) {
+    const std::array<double, 4>& d = O.dxdr[(size_t)k * O.B.Np + i];  // xr, yr, xs, ys
+    double J = d[0] * d[3] - d[1] * d[2];
+    rx = d[3] / J;
+    sx = -d[1] / J;
+    ry = -d[2] / J;
+    sy = d[0] / J;
+}
+
+// out = -(dgc::div(U) source) = strong nodal divergence (defaultDivScheme.C:40-75)
+static void ins_div_nodal(const Oracle& O, const double* u, double* out) {
+    const TriBase& B = O.B;
+    int K = O.K, Np = B.Np;
+    size_t KN = (size_t)K * Np;
+#pragma omp parallel for schedule(static)
+    for (int k = 0; k < K; k++)
+        for (int i = 0; i < Np; i++) {
+            double rx, sx, ry, sy;
+            node_metrics(O, k, i, rx, sx, ry, sy);
+            double s = 0;
+            for (int j = 0; j < Np; j++) {
+                double dx = B.Dr(i, j) * rx + B.Ds(i, j) * sx, dy = B.Dr(i, j) * ry + B.Ds(i, j) * sy;
+                s += dx * u[(size_t)k * Np + j] + dy * u[KN + (size_t)k * Np + j];
+            }
+            out[(size_t)k * Np + i] = s;
+        }
+}
+
+// strong nodal gradient (defaultGrad.C:44-78, without its minus sign)
+static void ins_grad_nodal(const Oracle& O, const double* p, double* out) {
+    const TriBase& B = O.B;
+    int K = O.K, Np = B.Np;
+    size_t KN = (size_t)K * Np;
+#pragma omp parallel for schedule(static)
+    for (int k = 0; k < K; k++)
+        for (int i = 0; i < Np; i++) {
+            double rx, sx, ry, sy;
+            node_metrics(O, k, i, rx, sx, ry, sy);
+            double gx = 0, gy = 0;
+            for (int j = 0; j < Np; j++) {
+                double pj = p[(size_t)k * Np + j];
+                gx += (B.Dr(i, j) * rx + B.Ds(i, j) * sx) * pj;
+                gy += (B.Dr(i, j) * ry + B.Ds(i, j) * sy) * pj;
+            }
+            out[(size_t)k * Np + i] = gx;
+            out[KN + (size_t)k * Np + i] = gy;
+        }
+}
+
+// curl(curl U) at nodes: w = dv/dx - du/dy, then (dw/dy, -dw/dx)
+// (pEqnCorrect.H:28-46, element-local)
+static void ins_curlcurl(const Oracle& O, const double* u, double* out) {
+    const TriBase& B = O.B;
+    int K = O.K, Np = B.Np;
+    size_t KN = (size_t)K * Np;
+#pragma omp parallel for schedule(static)
+    for (int k = 0; k < K; k++) {
+        double w[64];
+        for (int i = 0; i < Np; i++) {
+            double rx, sx, ry, sy;
+            node_metrics(O, k, i, rx, sx, ry, sy);
+            double s = 0;
+            for (int j = 0; j < Np; j++) {
+                double dx = B.Dr(i, j) * rx + B.Ds(i, j) * sx, dy = B.Dr(i, j) * ry + B.Ds(i, j) * sy;
+                s += -dy * u[(size_t)k * Np + j] + dx * u[KN + (size_t)k * Np + j];
+            }
+            w[i] = s;
+        }
+        for (int i = 0; i < Np; i++) {
+            double rx, sx, ry, sy;
+            node_metrics(O, k, i, rx, sx, ry, sy);
+            double cx = 0, cy = 0;
+            for (int j = 0; j < Np; j++) {
+                double dx = B.Dr(i, j) * rx + B.Ds(i, j) * sx, dy = B.Dr(i, j) * ry + B.Ds(i, j) * sy;
+                cx += dy * w[j];
+                cy -= dx * w[j];
+            }
+            out[(size_t)k * Np + i] = cx;
+            out[KN + (size_t)k * Np + i] = cy;
+        }
+    }
+}
+
+// dgc::div(U, U) with the LF flux on dof fields, solved against the mass
+// matrix (dgm::Sp(convecU) == dgc::div(U, U)): returns div(U (x) U).
+// Face flux at the face nodes (LFFlux.C:103-211): v = n.U on both sides,
+// lambda = max |v| over the face's nodes and sides, F = (vO UO + vN UN)/2 +
+// lambda (UO - UN)/2, interpolated to the face gauss points; boundary faces
+// take ubnd (per element face, [(k*3+f)*2*Nfp + c*Nfp + i], owner face-node
+// order).  Volume: products at the nodes, interpolated to the cubature points
+// (defaultConvectionScheme.C:216-263); lift as :265-300.
+static void ins_convection(const Oracle& O, const double* u, const double* ubnd, double* out) {
+    const TriBase& B = O.B;
+    int K = O.K, Np = B.Np, Ng = B.Ng, Nfp = B.Nfp, Nfq = B.Nfq;
+    size_t KN = (size_t)K * Np;
+    vec flux((size_t)2 * O.nFaceGauss);
+    int nF = (int)O.faces.size();
+#pragma omp parallel for schedule(static)
+    for (int fi = 0; fi < nF; fi++) {
+        const Face& F = O.faces[fi];
+        double UO[2][16], UN[2][16], vO[16], vN[16], t[2][16];
+        for (int i = 0; i < Nfp; i++) {
+            size_t no = (size_t)F.owner * Np + B.fci[F.fo][0][i];
+            UO[0][i] = u[no];
+            UO[1][i] = u[KN + no];
+            if (F.nbr >= 0) {
+                size_t nn = (size_t)F.nbr * Np + B.fci[F.fn][F.rot][i];
+                UN[0][i] = u[nn];
+                UN[1][i] = u[KN + nn];
+            } else {
+                const double* g = ubnd + (size_t)(F.owner * 3 + F.fo) * 2 * Nfp;
+                UN[0][i] = g[i];
+                UN[1][i] = g[Nfp + i];
+            }
+        }
+        double maxV = 0;
+        for (int i = 0; i < Nfp; i++) {
+            vO[i] = F.nx[i] * UO[0][i] + F.ny[i] * UO[1][i];
+            vN[i] = F.nx[i] * UN[0][i] + F.ny[i] * UN[1][i];
+            maxV = std::max(maxV, std::max(std::fabs(vO[i]), std::fabs(vN[i])));
+        }
+        for (int c = 0; c < 2; c++)
+            for (int i = 0; i < Nfp; i++) t[c][i] = (vO[i] * UO[c][i] + vN[i] * UN[c][i]) * 0.5 + maxV * (UO[c][i] - UN[c][i]) * 0.5;
+        for (int c = 0; c < 2; c++)
+            for (int g = 0; g < Nfq; g++) {
+                double s = 0;
+                for (int i = 0; i < Nfp; i++) s += B.faceInterp(g, i) * t[c][i];
+                flux[(size_t)c * O.nFaceGauss + F.start + g] = s;
+            }
+    }
+#pragma omp parallel for schedule(static)
+    for (int k = 0; k < K; k++) {
+        double b[2][64], tx[64], gt[128];
+        for (int c = 0; c < 2; c++)
+            for (int j = 0; j < Np; j++) b[c][j] = 0;
+        const double* wJ = &O.wJ[(size_t)k * Ng];
+        const double* D1[2] = {&O.D1x[(size_t)k * Ng * Np], &O.D1y[(size_t)k * Ng * Np]};
+        for (int d = 0; d < 2; d++)        // flux direction (the z direction contributes zero)
+            for (int c = 0; c < 2; c++) {  // transported component
+                for (int i = 0; i < Np; i++) tx[i] = u[d * KN + (size_t)k * Np + i] * u[c * KN + (size_t)k * Np + i];
+                for (int g = 0; g < Ng; g++) {
+                    double s = 0;
+                    for (int j = 0; j < Np; j++) s += B.cellV(g, j) * tx[j];
+                    gt[g] = s * wJ[g];
+                }
+                for (int g = 0; g < Ng; g++)
+                    for (int j = 0; j < Np; j++) b[c][j] += D1[d][(size_t)g * Np + j] * gt[g];
+            }
+        for (int f = 0; f < 3; f++) {
+            const Face& F = O.faces[O.cellFace[k][f]];
+            bool own = (F.owner == k) && (F.fo == f);
+            const int* map = own ? B.fci[F.fo][0] : B.fci[F.fn][F.rot];
+            double sgn = own ? -1.0 : 1.0;
+            for (int c = 0; c < 2; c++)
+                for (int g = 0; g < Nfq; g++) {
+                    double tt = F.wJ[g] * flux[(size_t)c * O.nFaceGauss + F.start + g];
+                    for (int j = 0; j < Nfp; j++) b[c][map[j]] += sgn * tt * B.faceInterp(g, j);
+                }
+        }
+        // Sp(convecU) == div: M convecU = -b
+        for (int c = 0; c < 2; c++)
+            for (int i = 0; i < Np; i++) {
+                double s = 0;
+                for (int j = 0; j < Np; j++) s -= O.Minv[k](i, j) * b[c][j];
+                out[c * KN + (size_t)k * Np + i] = s;
+            }
+    }
+}
+
+// b[k][fci[f][0][i]] += (I^T W I g)[i] on the element faces with mask[k*3+f]
+// (the face mass matrix of pCorrectEquation.H:90-110 and of the Neumann data)
+static void face_mass_lift(const Oracle& O, const int* mask, const double* g, double* b) {
+    const TriBase& B = O.B;
+    int K = O.K, Np = B.Np, Nfp = B.Nfp;
+    for (int k = 0; k < K; k++)
+        for (int f = 0; f < 3; f++) {
+            if (!mask[k * 3 + f]) continue;
+            const Face& F = O.faces[O.cellFace[k][f]];
+            if (!(F.owner == k && F.fo == f)) continue;
+            Mat t = AtDB(B.faceInterp, F.wJ.data(), B.faceInterp);
+            const double* gg = g + (size_t)(k * 3 + f) * Nfp;
+            for (int i = 0; i < Nfp; i++) {
+                double s = 0;
+                for (int j = 0; j < Nfp; j++) s += t(i, j) * gg[j];
+                b[(size_t)k * Np + B.fci[f][0][i]] += s;
+            }
+        }
 }
 
 }  // namespace orc
@@ -1273,6 +1491,36 @@ int orc_pcg_bj(void* h, const double* diag, const double* off, const double* rhs
     }
     *relres = rn / bnorm;
     return it;
+}
+
+// SIPG blocks with boundary types and data per element face (see ipdg_assemble)
+void orc_ipdg_blocks_bc(void* h, double tau_coef, const int* btype, const double* gD, const double* gN, double* diag,
+                        double* off, double* b) {
+    Oracle& O = *(Oracle*)h;
+    build_face_dn(O);
+    Ipdg L;
+    vec bb;
+    ipdg_assemble(O, tau_coef, L, gD, bb, btype, gN, true);
+    int Np = O.B.Np;
+    size_t NN = (size_t)Np * Np;
+    for (int k = 0; k < O.K; k++) {
+        std::copy(L.diag[k].a.begin(), L.diag[k].a.end(), diag + k * NN);
+        for (int f = 0; f < 3; f++) {
+            if (L.off[k][f].r) std::copy(L.off[k][f].a.begin(), L.off[k][f].a.end(), off + (k * 3 + f) * NN);
+            else std::fill(off + (k * 3 + f) * NN, off + (k * 3 + f + 1) * NN, 0.0);
+        }
+    }
+    if (b) std::copy(bb.begin(), bb.end(), b);
+}
+
+void orc_ins_div_nodal(void* h, const double* u, double* out) { ins_div_nodal(*(Oracle*)h, u, out); }
+void orc_ins_grad_nodal(void* h, const double* p, double* out) { ins_grad_nodal(*(Oracle*)h, p, out); }
+void orc_ins_curlcurl(void* h, const double* u, double* out) { ins_curlcurl(*(Oracle*)h, u, out); }
+void orc_ins_convection(void* h, const double* u, const double* ubnd, double* out) {
+    ins_convection(*(Oracle*)h, u, ubnd, out);
+}
+void orc_face_mass_lift(void* h, const int* mask, const double* g, double* b) {
+    face_mass_lift(*(Oracle*)h, mask, g, b);
 }
 
 void orc_set_threads(int n) {

@@ -44,6 +44,12 @@ def lib():
         L.orc_blk_apply.argtypes = [ctypes.c_void_p, _dp, _dp, _dp, _dp]
         L.orc_pcg_bj.restype = ctypes.c_int
         L.orc_pcg_bj.argtypes = [ctypes.c_void_p, _dp, _dp, _dp, _dp, ctypes.c_double, ctypes.c_int, _dp]
+        L.orc_ipdg_blocks_bc.argtypes = [ctypes.c_void_p, ctypes.c_double, _ip, _dp, _dp, _dp, _dp, _dp]
+        L.orc_ins_div_nodal.argtypes = [ctypes.c_void_p, _dp, _dp]
+        L.orc_ins_grad_nodal.argtypes = [ctypes.c_void_p, _dp, _dp]
+        L.orc_ins_curlcurl.argtypes = [ctypes.c_void_p, _dp, _dp]
+        L.orc_ins_convection.argtypes = [ctypes.c_void_p, _dp, _dp, _dp]
+        L.orc_face_mass_lift.argtypes = [ctypes.c_void_p, _ip, _dp, _dp]
         L.orc_set_threads.argtypes = [ctypes.c_int]
         L.orc_max_threads.restype = ctypes.c_int
         _lib = L
@@ -158,6 +164,54 @@ class Oracle:
         g = None if gD is None else np.ascontiguousarray(gD, np.float64)
         self.L.orc_ipdg_blocks(self.h, tau_coef, _d(g) if g is not None else None, _d(diag), _d(off), _d(b))
         return diag, off, b
+
+    def ipdg_blocks_bc(self, btype, gD=None, gN=None, tau_coef=20.0):
+        """SIPG blocks with a boundary type per element face (0 Dirichlet with
+        data gD, 1 Neumann with data gN, 2 natural), data per element face in
+        the element's face-node order: arrays (K, 3, Nfp)."""
+        Np, K, Nfp = self.Np, self.K, self.Nfp
+        diag = np.zeros((K, Np, Np))
+        off = np.zeros((K, 3, Np, Np))
+        b = np.zeros(K * Np)
+        bt = np.ascontiguousarray(btype, np.int32).reshape(K * 3)
+        gd = None if gD is None else np.ascontiguousarray(gD, np.float64).reshape(K * 3 * Nfp)
+        gn = None if gN is None else np.ascontiguousarray(gN, np.float64).reshape(K * 3 * Nfp)
+        self.L.orc_ipdg_blocks_bc(self.h, tau_coef, _i(bt), _d(gd) if gd is not None else None,
+                                  _d(gn) if gn is not None else None, _d(diag), _d(off), _d(b))
+        return diag, off, b
+
+    def _vec_op(self, fn, x, ncomp_out):
+        x = np.ascontiguousarray(x, np.float64)
+        out = np.zeros(ncomp_out * self.K * self.Np)
+        fn(self.h, _d(x), _d(out))
+        return out
+
+    def div_nodal(self, u):
+        """Strong nodal divergence of u (2, K, Np) -> (K, Np)."""
+        return self._vec_op(self.L.orc_ins_div_nodal, u, 1).reshape(self.K, self.Np)
+
+    def grad_nodal(self, p):
+        return self._vec_op(self.L.orc_ins_grad_nodal, p, 2).reshape(2, self.K, self.Np)
+
+    def curlcurl(self, u):
+        return self._vec_op(self.L.orc_ins_curlcurl, u, 2).reshape(2, self.K, self.Np)
+
+    def convection(self, u, ubnd):
+        """div(U (x) U) of the LF-flux DG convection operator; ubnd (K, 3, 2, Nfp)
+        boundary values (read on boundary faces)."""
+        u = np.ascontiguousarray(u, np.float64)
+        g = np.ascontiguousarray(ubnd, np.float64)
+        out = np.zeros(2 * self.K * self.Np)
+        self.L.orc_ins_convection(self.h, _d(u), _d(g), _d(out))
+        return out.reshape(2, self.K, self.Np)
+
+    def face_mass_lift(self, mask, g):
+        """b[k, face nodes of f] += (I^T W I) g[k, f] where mask[k, f]."""
+        m = np.ascontiguousarray(mask, np.int32).reshape(-1)
+        g = np.ascontiguousarray(g, np.float64)
+        b = np.zeros(self.K * self.Np)
+        self.L.orc_face_mass_lift(self.h, _i(m), _d(g), _d(b))
+        return b.reshape(self.K, self.Np)
 
     def blk_apply(self, diag, off, x):
         x = np.ascontiguousarray(x, np.float64)

@@ -21,7 +21,11 @@ def golden_mesh(name):
     d = np.load(os.path.join(GOLDEN, name + ".npz"))
     EToV, VXY = d["EToV"], d["VXY"]
     EToE, EToF, ROT, BC = connect(EToV)
-    return Mesh(EToV, VXY, EToE, EToF, ROT, BC, name=name)
+    m = Mesh(EToV, VXY, EToE, EToF, ROT, BC, name=name)
+    if "patch" in d:
+        m.patch = d["patch"]
+        m.patch_names = tuple(str(x) for x in d["patch_names"])
+    return m
 
 
 def rel_l2(a, b):

@@ -4,6 +4,9 @@
   meshes (HopeFOAM-0.1/tutorials/DG/2D/isentropicVortex/vortex0256.msh,
   vortex1024.msh) converted by hopefoam_gb300.meshio to (EToV, VXY) arrays, so
   the known-answer tests run where the reference tree is absent.
+* ``pearson_h.npz`` / ``pearson_0.5h.npz`` / ``pearson_0.25h.npz``: the
+  Pearson-vortex tutorial meshes (tutorials/DG/2D/pearsonVortex/vortexh.msh,
+  vortex0.5h.msh, vortex0.25h.msh) with their inlet / outlet boundary patches.
 * ``vortex_kat.json``: the reference's published accuracy table for that case
   ("2017-07-24-OpenFOAM workshop.pptx", slide 18: Roe flux, SSP-RK2, exact
   fixed-value boundary, t = 2; mean absolute nodal error of rho and |rhoU|),
@@ -39,6 +42,11 @@ def main():
     for name in ["vortex0256", "vortex1024"]:
         m = read_fluent_msh(os.path.join(tut, name + ".msh"))
         np.savez_compressed(os.path.join(HERE, name + ".npz"), EToV=m.EToV, VXY=m.VXY)
+    pv = os.path.join(root, "HopeFOAM-0.1", "tutorials", "DG", "2D", "pearsonVortex")
+    for src, name in (("vortexh", "pearson_h"), ("vortex0.5h", "pearson_0.5h"), ("vortex0.25h", "pearson_0.25h")):
+        m = read_fluent_msh(os.path.join(pv, src + ".msh"))
+        np.savez_compressed(os.path.join(HERE, name + ".npz"), EToV=m.EToV, VXY=m.VXY, patch=m.patch,
+                            patch_names=np.array(m.patch_names))
     kat = {
         "source": "2017-07-24-OpenFOAM workshop.pptx, slide 18",
         "case": "isentropic vortex beta=5 centre (5,0) u_inf=1, gamma=1.4, Roe flux, SSP-RK2, exact fixed-value "

@@ -187,6 +187,7 @@ def main():
     ap.add_argument("--no-batch", action="store_true")
     ap.add_argument("--no-configs", action="store_true")
     ap.add_argument("--kh-steps", type=int, default=2)
+    ap.add_argument("--no-ins", action="store_true", help="skip the incompressible (Chorin) step benchmark")
     ap.add_argument("--c5-study", action="store_true", help="500-step shear-layer accuracy study (reduced size)")
     ap.add_argument("--c5-study-n", type=int, default=128)
     args = ap.parse_args()
@@ -336,6 +337,11 @@ def main():
                 line[key] = fn() if key == "c1" else fn(nsteps=args.kh_steps)
             except Exception as exc:
                 line[key] = {"error": str(exc)}
+    if rank == 0 and not args.no_ins:
+        try:
+            line["ins"] = ins_bench(with_cpu=not args.no_cpu_baseline)
+        except Exception as exc:
+            line["ins"] = {"error": str(exc)}
     if rank == 0 and args.c5_study:
         try:
             line["c5_study"] = c5_study(n=args.c5_study_n)
@@ -497,6 +503,66 @@ def c5_study(order=7, n=128, checkpoints=(100, 250, 500), n_full=708):
                         "CFL-0.5 step, %d steps" % (n, n, mesh.K, n_full, n_full, checkpoints[-1]),
             "dt": dt, "density_error_split_vs_fp64": rows, "ms_per_step_fp64": ms64 / checkpoints[-1],
             "ms_per_step_split": mssp / checkpoints[-1]}
+
+
+def ins_bench(n=128, order=2, steps=4, warmup=2, with_cpu=True, cpu_steps=2):
+    """Incompressible Chorin step (dg_ins_step) on the Pearson-vortex case of
+    the reference's dgChorinFoam tutorial, refined: [-0.5, 0.5]^2 as n x n x 2
+    triangles (K = 2 n^2) with the tutorial's inlet / outlet pattern, N = 2
+    (its baseOrder), nu = 0.01, dt = 1e-3, tau = 20 (N+1)^2 fscale; solves to a
+    relative residual of 1e-10.  Device time per step from CUDA events on the
+    solver's stream; the CPU baseline is the oracle's step (C++ operators,
+    scipy sparse LU factorised once) on the same mesh."""
+    from hopefoam_gb300.ins import ChorinSolver, PearsonVortex, pearson_mesh
+
+    mesh = pearson_mesh(n)
+    g = ChorinSolver(mesh, order, nu=0.01, dt=1e-3)
+    pv = PearsonVortex(g)
+    g.set_state(*pv.initial_state())
+    t = 0.0
+    for _ in range(warmup):
+        g.step(pv.bdata(t), rtol=1e-10)
+        t += g.dt
+    sts = []
+    for _ in range(steps):
+        sts.append(g.step(pv.bdata(t), rtol=1e-10))
+        t += g.dt
+    _, p = g.get_state()
+    err = pv.pressure_error(p, t)
+    ms = float(np.mean([s["ms"] for s in sts]))
+    Np = g.Np
+    # PCG iteration bytes (FP64 vectors x 11 passes, FP64 block inverse, geometry)
+    bytes_it = mesh.K * (8 * Np * 11 + 8 * Np * Np + 136)
+    its = float(np.mean([s["iterations_p"] + sum(s["iterations_u"]) for s in sts]))
+    peak, peak_kind = peaks()
+    out = {"workload": "Pearson vortex (dgChorinFoam tutorial case refined), %dx%dx2 (K=%d), N=%d, dt=1e-3, "
+                       "nu=0.01, rtol 1e-10" % (n, n, mesh.K, order),
+           "ms_per_step": ms, "steps": steps, "iterations_p": [s["iterations_p"] for s in sts],
+           "iterations_u": [list(s["iterations_u"]) for s in sts], "pressure_error_avg_max": err,
+           "value": mesh.K * Np * 3 / (ms * 1e-3), "unit": "DOF-steps/s (3 fields)",
+           "roofline": {"bound": "hbm", "achieved": bytes_it * its / (ms * 1e-3) / 1e9, "peak": peak, "unit": "GB/s",
+                        "frac": bytes_it * its / (ms * 1e-3) / 1e9 / peak, "peak_kind": peak_kind,
+                        "bytes_per_pcg_iteration": bytes_it,
+                        "note": "PCG iteration bytes x iterations of the step's three solves / step time"}}
+    g.close()
+    if with_cpu:
+        from hopefoam_gb300.mesh import load_cubature
+        from oracle import oracle
+        from oracle.ins_oracle import ChorinOracle
+
+        threads = oracle.max_threads()
+        t0 = time.perf_counter()
+        o = ChorinOracle(mesh, order, load_cubature(3 * (order + 1)), nu=0.01, dt=1e-3)
+        setup = time.perf_counter() - t0
+        o.step()  # first step (BDF1) factorises its Helmholtz operator
+        t0 = time.perf_counter()
+        for _ in range(cpu_steps):
+            o.step()
+        el = (time.perf_counter() - t0) / cpu_steps
+        out["cpu_baseline"] = {"value": mesh.K * Np * 3 / el, "unit": out["unit"], "cores": threads, "kind": "port",
+                               "ms_per_step": el * 1e3, "setup_s": setup,
+                               "sample": "%d oracle steps on the same mesh (sparse LU factorised at setup)" % cpu_steps}
+    return out
 
 
 def batch_bench(prec, n_cases=512, nsteps=100):

@@ -318,6 +318,15 @@ __global__ void ins_ut_kernel(size_t n, double a0, double a1, double b0, double 
     if (i < n) UT[i] = (a0 * U[i] + a1 * Uo[i] - dt * (b0 * Nn[i] + b1 * No[i])) / g0;
 }
 
+// initial guess of a solve from the previous solutions, polynomial
+// extrapolation in time: x = c0 x0 + c1 x1 + c2 x2
+__global__ void ins_extrap_kernel(size_t n, double c0, double c1, double c2, const double* __restrict__ x0,
+                                  const double* __restrict__ x1, const double* __restrict__ x2,
+                                  double* __restrict__ out) {
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) out[i] = c0 * x0[i] + (c1 != 0.0 ? c1 * x1[i] : 0.0) + (c2 != 0.0 ? c2 * x2[i] : 0.0);
+}
+
 __global__ void ins_axpy_kernel(size_t n, double a, const double* __restrict__ x, double* __restrict__ y) {
     const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) y[i] += a * x[i];
@@ -341,6 +350,9 @@ struct dg_ins {
     std::vector<void*> allocs;
     double *U = nullptr, *Uo = nullptr, *Nn = nullptr, *No = nullptr, *UT = nullptr, *P = nullptr, *w1 = nullptr,
            *w2 = nullptr, *rhs = nullptr, *sol = nullptr;
+    double *Ph1 = nullptr, *Ph2 = nullptr;  // the two pressure solutions before P
+    double* Pg = nullptr;                   // scratch: the extrapolated initial guess
+    int nhist = 0;                          // valid solutions among P, Ph1, Ph2
     double *nbp_prev = nullptr, *nbp_old = nullptr, *ubnd = nullptr, *ugrad = nullptr, *pval = nullptr,
            *pext = nullptr;
     int *ukind = nullptr, *pkind = nullptr;
@@ -458,6 +470,23 @@ int ins_step_n(dg_ins* s, const dg_ins_bdata* bd, double rtol, int maxit, dg_ins
     INS_CUDA(s, launch_bdata<N>(s, s->ukind, 0, 1, s->nbp_old, Nfp, 0, 1.0, s->rhs, st));
     int itp = 0, itu[2] = {0, 0};
     double relp = 0, relu[2] = {0, 0};
+    // initial guess: the pressure extrapolated in time from the last solutions
+    // (quadratic from three, linear from two); the solution changes only by the
+    // solver tolerance, the iteration count drops
+    {
+        double c0 = 1, c1 = 0, c2 = 0;
+        if (s->nhist >= 3) { c0 = 3; c1 = -3; c2 = 1; }
+        else if (s->nhist == 2) { c0 = 2; c1 = -1; }
+        dgk::ins_extrap_kernel<<<blocks_for(KN, 256), 256, 0, st>>>(KN, c0, c1, c2, s->P, s->Ph1, s->Ph2, s->Pg);
+        INS_CUDA(s, cudaGetLastError());
+        // history rotation: Ph2 <- Ph1 <- P, the guess becomes the solve's vector
+        double* freed = s->Ph2;
+        s->Ph2 = s->Ph1;
+        s->Ph1 = s->P;
+        s->P = s->Pg;
+        s->Pg = freed;
+        s->nhist = std::min(s->nhist + 1, 3);
+    }
     int rc = ipdg_solve_device(s->cp, s->rhs, s->P, rtol, maxit, &itp, &relp);
     if (rc) return insfail(s, rc, std::string("pressure solve: ") + s->cp->err);
     // 5: velocity correction
@@ -476,7 +505,11 @@ int ins_step_n(dg_ins* s, const dg_ins_bdata* bd, double rtol, int maxit, dg_ins
         // - q4 b_LU: Dirichlet terms on fixed-value slots, -F^T W F h on fixed-gradient slots
         INS_CUDA(s, launch_bdata<N>(s, s->ukind, 0, 0, s->ubnd, 2 * Nfp, c * Nfp, -bd->u_data_scale, s->rhs, st));
         INS_CUDA(s, launch_bdata<N>(s, s->ukind, 1, 1, s->ugrad, 2 * Nfp, c * Nfp, -bd->u_data_scale, s->rhs, st));
-        INS_CUDA(s, cudaMemcpyAsync(s->sol + c * KN, s->U + c * KN, KN * sizeof(double), cudaMemcpyDeviceToDevice, st));
+        // initial guess: U extrapolated linearly in time (U itself on the first step)
+        dgk::ins_extrap_kernel<<<blocks_for(KN, 256), 256, 0, st>>>(KN, s->nstep > 0 ? 2.0 : 1.0,
+                                                                    s->nstep > 0 ? -1.0 : 0.0, 0.0, s->U + c * KN,
+                                                                    s->Uo + c * KN, nullptr, s->sol + c * KN);
+        INS_CUDA(s, cudaGetLastError());
         rc = ipdg_solve_device(s->cu, s->rhs, s->sol + c * KN, rtol, maxit, &itu[c], &relu[c]);
         if (rc) return insfail(s, rc, std::string("velocity solve: ") + s->cu->err);
     }
@@ -598,13 +631,13 @@ int dg_ins_create(const dg_mesh_desc* mesh, const dg_opts* opts, const int* u_ki
     rc |= ins_upload(s, &s->pkind, s->pkind_h);
     const size_t KN = (size_t)s->K * Np;
     for (double** p : {&s->U, &s->Uo, &s->Nn, &s->No, &s->UT, &s->w2, &s->sol}) rc |= ins_alloc(s, p, 2 * KN);
-    for (double** p : {&s->P, &s->w1, &s->rhs}) rc |= ins_alloc(s, p, KN);
+    for (double** p : {&s->P, &s->w1, &s->rhs, &s->Ph1, &s->Ph2, &s->Pg}) rc |= ins_alloc(s, p, KN);
     const size_t nbf = (size_t)std::max(s->nb, 1) * s->Nfp;
     for (double** p : {&s->nbp_prev, &s->nbp_old, &s->pval, &s->pext}) rc |= ins_alloc(s, p, nbf);
     for (double** p : {&s->ubnd, &s->ugrad}) rc |= ins_alloc(s, p, 2 * nbf);
     if (rc) { dg_ins_destroy(s); return DG_ERR_NOMEM; }
     for (double* p : {s->U, s->Uo, s->Nn, s->No, s->UT, s->w2, s->sol}) cudaMemset(p, 0, 2 * KN * sizeof(double));
-    for (double* p : {s->P, s->w1, s->rhs}) cudaMemset(p, 0, KN * sizeof(double));
+    for (double* p : {s->P, s->w1, s->rhs, s->Ph1, s->Ph2, s->Pg}) cudaMemset(p, 0, KN * sizeof(double));
     for (double* p : {s->nbp_prev, s->nbp_old, s->pval, s->pext}) cudaMemset(p, 0, nbf * sizeof(double));
     for (double* p : {s->ubnd, s->ugrad}) cudaMemset(p, 0, 2 * nbf * sizeof(double));
     if (cudaDeviceSynchronize() != cudaSuccess) { dg_ins_destroy(s); return DG_ERR_CUDA; }
@@ -640,6 +673,7 @@ int dg_ins_set_state(dg_ins* s, const double* U_host, const double* p_host) {
     INS_CUDA(s, launch_permute(s->w1, s->P, s->cu->d_ring, s->K, s->Np, true, st));
     INS_CUDA(s, cudaStreamSynchronize(st));
     s->nstep = 0;
+    s->nhist = 1;
     return DG_OK;
 }
 

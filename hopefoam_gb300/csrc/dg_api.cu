@@ -224,6 +224,7 @@ int dg_ctx_create(const dg_mesh_desc* m, const dg_opts* o, dg_ctx** out) {
     }
     c->geo_host = geo;
     c->conn_host = conn;
+    if (m->EToV) c->etov_host.assign(m->EToV, m->EToV + 3 * (size_t)K);
     if (split_setup(c) != DG_OK) c->split.ready = false;
     if (cudaDeviceSynchronize() != cudaSuccess) { dg_ctx_destroy(c); return DG_ERR_CUDA; }
     *out = c;

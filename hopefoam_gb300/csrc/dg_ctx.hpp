@@ -38,6 +38,7 @@ struct dg_ctx {
     dgb::RefOps ops;
     std::vector<double> geo_host;
     std::vector<int> conn_host;
+    std::vector<int> etov_host;  // [K][3] vertex ids (empty when the mesh descriptor has none)
     // device buffers
     double* d_q[2] = {nullptr, nullptr};
     double* d_res = nullptr;
@@ -78,7 +79,7 @@ void ipdg_teardown(dg_ctx* c);
 // FP64 block-Jacobi PCG with the context's SIPG operator on ring-order device
 // vectors (x: initial guess in, solution out)
 int ipdg_solve_device(dg_ctx* c, const double* b_dev, double* x_dev, double rtol, int maxit, int* iters,
-                      double* rel);
+                      double* rel, int pc);
 // the operator's device tables (null before dg_ipdg_setup), the boundary
 // types per slot and the host copy of the face coefficients as built
 const dgk::IpdgArgs* ipdg_args(dg_ctx* c);

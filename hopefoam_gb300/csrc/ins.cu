@@ -345,6 +345,7 @@ struct dg_ins {
     int K = 0, N = 0, Np = 0, Nfp = 0, nb = 0;
     double nu = 0, dt = 0, mass_coef = -1;
     int nstep = 0;
+    int pc = DG_PC_MULTILEVEL;  // block Jacobi when the multilevel preconditioner cannot be built
     InsTables t{};
     InsSlots sl{};
     std::vector<void*> allocs;
@@ -487,7 +488,11 @@ int ins_step_n(dg_ins* s, const dg_ins_bdata* bd, double rtol, int maxit, dg_ins
         s->Pg = freed;
         s->nhist = std::min(s->nhist + 1, 3);
     }
-    int rc = ipdg_solve_device(s->cp, s->rhs, s->P, rtol, maxit, &itp, &relp);
+    int rc = ipdg_solve_device(s->cp, s->rhs, s->P, rtol, maxit, &itp, &relp, s->pc);
+    if (rc == DG_ERR_UNSUPPORTED && s->pc == DG_PC_MULTILEVEL) {
+        s->pc = DG_PC_BLOCK_JACOBI;  // no multilevel preconditioner on this mesh: block Jacobi
+        rc = ipdg_solve_device(s->cp, s->rhs, s->P, rtol, maxit, &itp, &relp, s->pc);
+    }
     if (rc) return insfail(s, rc, std::string("pressure solve: ") + s->cp->err);
     // 5: velocity correction
     INS_CUDA(s, launch_nodal<N>(s, 1, s->P, s->w2, st));
@@ -510,7 +515,7 @@ int ins_step_n(dg_ins* s, const dg_ins_bdata* bd, double rtol, int maxit, dg_ins
                                                                     s->nstep > 0 ? -1.0 : 0.0, 0.0, s->U + c * KN,
                                                                     s->Uo + c * KN, nullptr, s->sol + c * KN);
         INS_CUDA(s, cudaGetLastError());
-        rc = ipdg_solve_device(s->cu, s->rhs, s->sol + c * KN, rtol, maxit, &itu[c], &relu[c]);
+        rc = ipdg_solve_device(s->cu, s->rhs, s->sol + c * KN, rtol, maxit, &itu[c], &relu[c], s->pc);
         if (rc) return insfail(s, rc, std::string("velocity solve: ") + s->cu->err);
     }
     cudaEventRecord(e1, st);

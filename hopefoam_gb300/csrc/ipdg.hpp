@@ -53,6 +53,8 @@ struct PcgScalars {
     unsigned int counter;  // arrival counter of the grid-wide sums
 };
 
+struct MgLevels;
+
 struct PcgVecs {
     double *x, *r, *z, *Ap;      // ring-order FP64 vectors of length K*Np
     double* p[2];                // search directions, ping-pong (iteration j reads p[j&1], writes p[(j+1)&1])
@@ -68,6 +70,7 @@ struct PcgVecs {
     float* dz;
     float* dp[2];
     float* r32;                  // learned Schwarz mode: FP32 copy of r for the learned kernel (else null)
+    const MgLevels* mg;          // multilevel mode (with zb): the coarse-space correction forms z
 };
 
 // largest grid of the PCG kernels (sizes the partials)

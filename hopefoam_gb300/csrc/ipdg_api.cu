@@ -3,6 +3,7 @@
 #include <cmath>
 #include <cstring>
 #include <string>
+#include <type_traits>
 #include <vector>
 
 #include "../../include/dgcu.h"
@@ -10,6 +11,7 @@
 #include "euler_flux.cuh"
 #include "ipdg.hpp"
 #include "lpc.hpp"
+#include "mg.hpp"
 
 #include <random>
 
@@ -23,6 +25,11 @@ struct IpdgState {
     double* d_J = nullptr;
     IpdgOps<double> o64h{};  // device pointers of the operator tables
     IpdgOps<float> o32h{};
+    // multilevel preconditioner (DG_PC_MULTILEVEL); rebuilt when the operator changes
+    MgLevels mg{};
+    bool mg_ready = false;
+    std::string mg_err;
+    std::vector<void*> mg_allocs;
     std::vector<double> fc_host;  // face coefficients as built (boundary types reset sJ from it)
     std::vector<int> btype;       // per boundary slot: 0 fixesValue, 1 fixesGradient, 2 neither
     double* d_blocks = nullptr;  // FP64 inverse diagonal blocks (row-major per element)
@@ -181,7 +188,7 @@ int run_cg(dg_ctx* c, const PcgVecs& v, bool fp32, double tol2, int limit, const
         IP_CUDA(c, cudaStreamSynchronize(c->stream));
         checks++;
         if (h.done == 2) break;
-        if (v.zb && h.done == 0) {
+        if (v.zb && !v.mg && h.done == 0) {
             if (best_rr < 0 || h.rr < 0.5 * best_rr) {
                 best_rr = h.rr;
                 best_it = h.it;
@@ -252,6 +259,7 @@ std::vector<int> rotation_perms(const dgb::RefOps& o) {
 void ipdg_teardown(dg_ctx* c) {
     if (!c->ipdg) return;
     for (void* p : c->ipdg->allocs) cudaFree(p);
+    for (void* p : c->ipdg->mg_allocs) cudaFree(p);
     delete c->ipdg;
     c->ipdg = nullptr;
 }
@@ -270,6 +278,71 @@ static int build_blocks(dg_ctx* c) {
     IP_CUDA(c, cudaMemcpyAsync(&st, s->d_status, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
     IP_CUDA(c, cudaStreamSynchronize(c->stream));
     if (st) return ifail(c, DG_ERR_NONFINITE, "singular diagonal block in the SIPG operator");
+    return DG_OK;
+}
+
+// (re)builds the multilevel preconditioner of the current operator
+static int mg_setup(dg_ctx* c) {
+    IpdgState* s = c->ipdg;
+    for (void* p : s->mg_allocs) cudaFree(p);
+    s->mg_allocs.clear();
+    s->mg_ready = false;
+    if (c->etov_host.empty()) {
+        s->mg_err = "the mesh descriptor has no vertex ids (EToV)";
+        return ifail(c, DG_ERR_UNSUPPORTED, s->mg_err);
+    }
+    MgBuild b;
+    std::string e = mg_build(c->K, c->N, c->Np, c->etov_host.data(), c->geo_host.data(), c->conn_host.data(),
+                             s->fc_host, s->btype, s->args.mass_coef, c->ops, b);
+    if (!e.empty()) {
+        s->mg_err = "multilevel preconditioner: " + e;
+        return ifail(c, DG_ERR_UNSUPPORTED, s->mg_err);
+    }
+    int rc = 0;
+    auto up = [&](auto** dst, const auto& h) {
+        using T = typename std::remove_reference<decltype(h)>::type::value_type;
+        T* p = nullptr;
+        if (cudaMalloc((void**)&p, std::max<size_t>(h.size(), 1) * sizeof(T)) != cudaSuccess) { rc = 1; return; }
+        s->mg_allocs.push_back(p);
+        if (!h.empty() && cudaMemcpy(p, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice) != cudaSuccess) rc = 1;
+        *dst = p;
+    };
+    auto work = [&](double** dst, int n) {
+        double* p = nullptr;
+        if (cudaMalloc((void**)&p, std::max(n, 1) * sizeof(double)) != cudaSuccess) { rc = 1; return; }
+        s->mg_allocs.push_back(p);
+        *dst = p;
+    };
+    MgLevels& m = s->mg;
+    m = MgLevels();
+    m.nl = (int)b.levels.size();
+    m.K = c->K;
+    m.Np = c->Np;
+    up((int**)&m.etov, c->etov_host);
+    up((double**)&m.lam, b.lam);
+    up((int**)&m.vptr, b.vptr);
+    up((int**)&m.vinc, b.vinc);
+    up((double**)&m.Cinv, b.Cinv);
+    for (int l = 0; l < m.nl; l++) {
+        const MgBuild::Level& L = b.levels[l];
+        MgLevel& d = m.lv[l];
+        d.n = L.n;
+        up((int**)&d.rowptr, L.rowptr);
+        up((int**)&d.col, L.col);
+        up((double**)&d.val, L.val);
+        up((double**)&d.dinv, L.dinv);
+        if (l + 1 < m.nl) {
+            up((int**)&d.agg, L.agg);
+            up((int**)&d.cptr, L.cptr);
+            up((int**)&d.cmem, L.cmem);
+        }
+        work(&d.r, L.n);
+        work(&d.x, L.n);
+        work(&d.t, L.n);
+    }
+    if (!s->d_zb) rc |= ialloc(c, s, &s->d_zb, (size_t)c->K * c->Np);
+    if (rc) return ifail(c, DG_ERR_NOMEM, "multilevel preconditioner: device allocation failed");
+    s->mg_ready = true;
     return DG_OK;
 }
 
@@ -443,6 +516,7 @@ int dg_ipdg_set_mass(dg_ctx* c, double alpha) {
     if (!c || !(alpha >= 0)) return DG_ERR_ARG;
     if (!c->ipdg || !c->ipdg->ready) return ifail(c, DG_ERR_ARG, "dg_ipdg_setup not called");
     c->ipdg->args.mass_coef = alpha;
+    c->ipdg->mg_ready = false;
     return build_blocks(c);
 }
 
@@ -466,6 +540,7 @@ int dg_ipdg_set_boundary_types(dg_ctx* c, const int* btype) {
     IP_CUDA(c, cudaMemcpyAsync((void*)s->o64h.fc, fc.data(), nfc * sizeof(double), cudaMemcpyHostToDevice, c->stream));
     IP_CUDA(c, cudaMemcpyAsync((void*)s->o32h.fc, fc32.data(), nfc * sizeof(float), cudaMemcpyHostToDevice, c->stream));
     IP_CUDA(c, cudaStreamSynchronize(c->stream));
+    s->mg_ready = false;
     return build_blocks(c);
 }
 
@@ -488,10 +563,15 @@ int dg_pcg_solve(dg_ctx* c, const double* b_host, double* x_host, double rtol, i
                  dg_solve_stats* stats) {
     if (!c || !b_host || !x_host || !(rtol > 0) || maxit < 1) return DG_ERR_ARG;
     if (!c->ipdg || !c->ipdg->ready) return ifail(c, DG_ERR_ARG, "dg_ipdg_setup not called");
-    if (pc != DG_PC_BLOCK_JACOBI && pc != DG_PC_LEARNED && pc != DG_PC_LEARNED_ONLY)
+    if (pc != DG_PC_BLOCK_JACOBI && pc != DG_PC_LEARNED && pc != DG_PC_LEARNED_ONLY && pc != DG_PC_MULTILEVEL)
         return ifail(c, DG_ERR_ARG, "unknown preconditioner");
     const bool learned = pc == DG_PC_LEARNED || pc == DG_PC_LEARNED_ONLY;
+    const bool mgm = pc == DG_PC_MULTILEVEL;
     if (learned && !c->ipdg->lpc_ready) return ifail(c, DG_ERR_ARG, "dg_lpc_setup not called");
+    if (mgm && !c->ipdg->mg_ready) {
+        const int rcm = mg_setup(c);
+        if (rcm) return rcm;
+    }
     if (precision != DG_PREC_FP64 && precision != DG_PREC_SPLIT) return ifail(c, DG_ERR_ARG, "unknown precision");
     IpdgState* s = c->ipdg;
     const size_t n = (size_t)c->K * c->Np;
@@ -506,7 +586,7 @@ int dg_pcg_solve(dg_ctx* c, const double* b_host, double* x_host, double rtol, i
     double bb = 0;
     int rc = dot_host(c, s->d_b, s->d_b, &bb);
     if (rc) return rc;
-    PcgVecs v;
+    PcgVecs v{};
     v.r = s->d_r;
     v.z = s->d_z;
     v.p[0] = s->d_p;
@@ -516,7 +596,8 @@ int dg_pcg_solve(dg_ctx* c, const double* b_host, double* x_host, double rtol, i
     v.nmax = s->nmax;
     v.P32 = s->d_P32;
     v.P64 = nullptr;
-    v.zb = learned ? s->d_zb : nullptr;
+    v.zb = (learned || mgm) ? s->d_zb : nullptr;
+    v.mg = mgm ? &s->mg : nullptr;
     v.S = s->d_S;
     const bool mirrors = precision == DG_PREC_SPLIT;  // the FP32 apply stages from FP32 offset mirrors
     v.dz = mirrors ? s->d_dz : nullptr;
@@ -533,7 +614,7 @@ int dg_pcg_solve(dg_ctx* c, const double* b_host, double* x_host, double rtol, i
         if (rc) return rc;
         IP_CUDA(c, launch_xmy(s->d_r, s->d_b, s->d_Ap, n, c->stream));
         v.x = s->d_x;
-        if (!v.zb) v.P64 = s->d_P64;  // FP64 preconditioner: an inexact one stalls CG at high condition numbers
+        if (!v.zb || mgm) v.P64 = s->d_P64;  // FP64 preconditioner: an inexact one stalls CG at high condition numbers
         rc = run_cg(c, v, false, rtol * rtol * bb, maxit, s->d_b, 0, &total_it, &stop);
         if (rc) return rc;
     } else {
@@ -605,9 +686,14 @@ int dg_pcg_solve(dg_ctx* c, const double* b_host, double* x_host, double rtol, i
 // FP64 block-Jacobi PCG on ring-order device vectors (x holds the initial
 // guess and receives the solution); used by the incompressible step
 int ipdg_solve_device(dg_ctx* c, const double* b_dev, double* x_dev, double rtol, int maxit, int* iters,
-                      double* rel_out) {
+                      double* rel_out, int pc) {
     if (!c->ipdg || !c->ipdg->ready) return ifail(c, DG_ERR_ARG, "dg_ipdg_setup not called");
     IpdgState* s = c->ipdg;
+    const bool mgm = pc == DG_PC_MULTILEVEL;
+    if (mgm && !s->mg_ready) {
+        const int rcm = mg_setup(c);
+        if (rcm) return rcm;
+    }
     const size_t n = (size_t)c->K * c->Np;
     IP_CUDA(c, cudaMemcpyAsync(s->d_b, b_dev, n * sizeof(double), cudaMemcpyDeviceToDevice, c->stream));
     IP_CUDA(c, cudaMemcpyAsync(s->d_x, x_dev, n * sizeof(double), cudaMemcpyDeviceToDevice, c->stream));
@@ -629,7 +715,8 @@ int ipdg_solve_device(dg_ctx* c, const double* b_dev, double* x_dev, double rtol
         v.nmax = s->nmax;
         v.P32 = s->d_P32;
         v.P64 = s->d_P64;
-        v.zb = nullptr;
+        v.zb = mgm ? s->d_zb : nullptr;
+        v.mg = mgm ? &s->mg : nullptr;
         v.S = s->d_S;
         v.dz = nullptr;
         v.dp[0] = v.dp[1] = nullptr;

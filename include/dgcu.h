@@ -55,7 +55,7 @@ enum {
 enum { DG_BC_INTERIOR = 0, DG_BC_FIXED = 1 };
 
 /* preconditioners for dg_pcg_solve */
-enum { DG_PC_NONE = 0, DG_PC_BLOCK_JACOBI = 1, DG_PC_LEARNED = 2, DG_PC_LEARNED_ONLY = 3 };
+enum { DG_PC_NONE = 0, DG_PC_BLOCK_JACOBI = 1, DG_PC_LEARNED = 2, DG_PC_LEARNED_ONLY = 3, DG_PC_MULTILEVEL = 4 };
 
 typedef struct dg_ctx dg_ctx;
 
@@ -199,8 +199,13 @@ int dg_ipdg_apply(dg_ctx* ctx, const double* x_host, double* y_host);
  * (replaces dgMatrix::solve -> KSPSolve, dgMatrices/dgMatrix/dgMatrix.C:162-283,
  * dgMatrixSolve.C:91-213).  x_host holds the initial guess and receives the
  * solution.  pc: DG_PC_BLOCK_JACOBI, DG_PC_LEARNED (after dg_lpc_*; falls back
- * to block Jacobi) or DG_PC_LEARNED_ONLY (no fallback: reports the learned
- * solve's own outcome).
+ * to block Jacobi), DG_PC_LEARNED_ONLY (no fallback: reports the learned
+ * solve's own outcome) or DG_PC_MULTILEVEL (block Jacobi plus a coarse-space
+ * correction: continuous piecewise-linear functions on the mesh vertices with
+ * the Galerkin operator, one V-cycle over aggregated levels per application;
+ * built on first use from the mesh's vertex ids, rebuilt after
+ * dg_ipdg_set_boundary_types / dg_ipdg_set_mass; the reference has no
+ * counterpart, its solver options are PETSc's).
  * precision DG_PREC_FP64: FP64 operator in every iteration; DG_PREC_SPLIT:
  * FP32-arithmetic operator inside CG with FP64 vectors, dot products and
  * recurrences, the recurrence residual replaced by the true FP64 residual

@@ -86,3 +86,27 @@ def test_reference_fluent_zones_and_fields():
         assert [int((m.patch == i).sum()) for i in range(2)] == [nb, nb]
     assert read_dg_field(os.path.join(REF, "pearsonVortex", "0", "p")) == 0.0
     assert np.array_equal(read_dg_field(os.path.join(REF, "pearsonVortex", "0", "U")), [0.0, 0.0, 0.0])
+
+
+@pytest.mark.parametrize("order", [1, 3, 5])
+def test_vtk_output(tmp_path, order):
+    """Every element split into N^2 counter-clockwise sub-triangles over its own
+    nodes (dgToVTK's vtkTopo.C); the sub-triangles tile the domain."""
+    from hopefoam_gb300.vtk import read_vtk, write_vtk
+
+    m = delaunay_square(60, seed=2)
+    Np = (order + 1) * (order + 2) // 2
+    rng = np.random.default_rng(0)
+    p = rng.standard_normal((m.K, Np))
+    U = rng.standard_normal((m.K, Np, 2))
+    path = str(tmp_path / "out.vtk")
+    write_vtk(path, m, order, {"p": p, "U": U})
+    r = read_vtk(path)
+    assert r["points"].shape == (m.K * Np, 3) and r["cells"].shape == (m.K * order * order, 3)
+    P = r["points"][:, :2]
+    a = P[r["cells"][:, 1]] - P[r["cells"][:, 0]]
+    b = P[r["cells"][:, 2]] - P[r["cells"][:, 0]]
+    area = 0.5 * (a[:, 0] * b[:, 1] - a[:, 1] * b[:, 0])
+    assert np.all(area > 0)
+    assert np.isclose(area.sum(), (2 * np.pi) ** 2)
+    assert np.array_equal(r["data"]["p"], p.reshape(-1)) and np.array_equal(r["data"]["U"][:, :2], U.reshape(-1, 2))

@@ -75,6 +75,10 @@ SIGNATURES = {
     "dg_ipdg_apply": (ctypes.c_int, [_vp, _dp, _dp]),
     "dg_ipdg_set_boundary_types": (ctypes.c_int, [_vp, _ip]),
     "dg_ipdg_set_mass": (ctypes.c_int, [_vp, ctypes.c_double]),
+    "dg_set_boundary_kinds": (ctypes.c_int, [_vp, _ip, _ip]),
+    "dg_limit": (ctypes.c_int, [_vp]),
+    "dg_reflect_boundary_traces": (ctypes.c_int, [_vp]),
+    "dg_limited_ssprk2_step": (ctypes.c_int, [_vp, ctypes.c_double, _dp, ctypes.c_int, ctypes.c_int]),
     "dg_ins_create": (ctypes.c_int, [ctypes.POINTER(MeshDesc), ctypes.POINTER(Opts), _ip, _ip, ctypes.c_double,
                                      ctypes.c_double, ctypes.c_double, ctypes.POINTER(_vp)]),
     "dg_ins_destroy": (ctypes.c_int, [_vp]),

@@ -105,6 +105,18 @@ int run_args_impl(dg_ctx* c, int flux, int precision) {
 int check_split_status(dg_ctx* c, int precision) { return split_status_impl(c, precision); }
 int check_run_args(dg_ctx* c, int flux, int precision) { return run_args_impl(c, flux, precision); }
 
+int euler_stage_mode(dg_ctx* c, const double* qin, double* qout, const double* qold, int mode, double dt, int flux,
+                     int precision, const double* btrace) {
+    EulerArgs a = base_args(c, flux);
+    a.qin = qin;
+    a.qout = qout;
+    a.qold = qold;
+    a.mode = mode;
+    a.dt = dt;
+    if (btrace) a.btrace = btrace;
+    return run_stage(c, a, precision);
+}
+
 int lserk_stage(dg_ctx* c, double dt, int stage, int flux, int precision) {
     EulerArgs a = base_args(c, flux);
     a.res = c->d_res;
@@ -225,6 +237,7 @@ int dg_ctx_create(const dg_mesh_desc* m, const dg_opts* o, dg_ctx** out) {
     c->geo_host = geo;
     c->conn_host = conn;
     if (m->EToV) c->etov_host.assign(m->EToV, m->EToV + 3 * (size_t)K);
+    c->vxy_host.assign(m->VXY, m->VXY + 6 * (size_t)K);
     if (split_setup(c) != DG_OK) c->split.ready = false;
     if (cudaDeviceSynchronize() != cudaSuccess) { dg_ctx_destroy(c); return DG_ERR_CUDA; }
     *out = c;
@@ -236,6 +249,7 @@ int dg_ctx_destroy(dg_ctx* c) {
     if (c->stream) cudaStreamSynchronize(c->stream);
     split_teardown(c);
     ipdg_teardown(c);
+    limiter_teardown(c);
     for (void* p : c->allocs) cudaFree(p);
     if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
     delete c;

@@ -39,6 +39,8 @@ struct dg_ctx {
     std::vector<double> geo_host;
     std::vector<int> conn_host;
     std::vector<int> etov_host;  // [K][3] vertex ids (empty when the mesh descriptor has none)
+    std::vector<double> vxy_host;  // [K][3][2] vertex coordinates
+    struct LimState* lim = nullptr;  // slope limiter / limited SSP-RK2 state (limiter.cu)
     // device buffers
     double* d_q[2] = {nullptr, nullptr};
     double* d_res = nullptr;
@@ -69,6 +71,12 @@ int lserk_stage(dg_ctx* c, double dt, int stage, int flux, int precision);
 int check_run_args(dg_ctx* c, int flux, int precision);
 // reads and clears the split kernel's timeout flag (synchronises c->stream)
 int check_split_status(dg_ctx* c, int precision);
+// one Euler stage kernel (mode: StageMode) from qin into qout with the given
+// boundary traces (null: the context's)
+int euler_stage_mode(dg_ctx* c, const double* qin, double* qout, const double* qold, int mode, double dt, int flux,
+                     int precision, const double* btrace);
+// limiter state teardown (limiter.cu)
+void limiter_teardown(dg_ctx* c);
 
 // SIPG / PCG state (ipdg_api.cu)
 namespace dgk {

@@ -128,6 +128,26 @@ class EulerContext:
     def ssprk2(self, dt, nsteps, flux=L.DG_FLUX_ROE, precision=L.DG_PREC_FP64):
         _check(self.h, self.lib.dg_ssprk2_step(self.h, float(dt), int(nsteps), flux, precision))
 
+    # --- limiter (shock cases) -------------------------------------------
+    def set_boundary_kinds(self, kinds, gref=None):
+        """Per boundary slot: 0 fixed value, 1 reflective wall, 2 other."""
+        k = np.ascontiguousarray(kinds, np.int32)
+        g = None if gref is None else np.ascontiguousarray(gref, np.int32)
+        self._keep += [k] + ([g] if g is not None else [])
+        _check(self.h, self.lib.dg_set_boundary_kinds(self.h, L.iptr(k), L.iptr(g) if g is not None else None))
+
+    def limit(self):
+        _check(self.h, self.lib.dg_limit(self.h))
+
+    def reflect_boundary_traces(self):
+        _check(self.h, self.lib.dg_reflect_boundary_traces(self.h))
+
+    def limited_ssprk2(self, dt, bdata, flux=L.DG_FLUX_ROE, precision=L.DG_PREC_FP64):
+        """One limited SSP-RK2 step; bdata (n_bfaces, 4, Nfp): this step's
+        values of the fixed-value slots."""
+        b = np.ascontiguousarray(bdata, np.float64).reshape(-1)
+        _check(self.h, self.lib.dg_limited_ssprk2_step(self.h, float(dt), L.dptr(b), flux, precision))
+
     def cfl_dt(self, cfl):
         dt = np.zeros(1)
         _check(self.h, self.lib.dg_cfl_dt(self.h, float(cfl), L.dptr(dt)))

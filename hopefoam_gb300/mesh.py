@@ -33,6 +33,7 @@ class Mesh:
     # for a boundary face, -1 for an interior face; None when not read from a file
     patch: np.ndarray = None
     patch_names: tuple = ()
+    patch_first_face: np.ndarray = None  # per patch (k, f) of its first face in the file's order
 
     @property
     def K(self):

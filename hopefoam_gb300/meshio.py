@@ -76,7 +76,18 @@ def read_fluent_msh(path):
     names = tuple(zone_names.get(z, "zone%d" % z) for z in bzones)
     edge_zone = {(min(n0, n1) - 1, max(n0, n1) - 1): bzones.index(int(z)) for n0, n1, c0, c1, z in faces if c0 == 0 or c1 == 0}
     patch = -np.ones((ncell, 3), np.int32)
+    kf_of_edge = {}
     for k, f in zip(*np.nonzero(EToE < 0)):
         a, b = int(EToV[k, f]), int(EToV[k, (f + 1) % 3])
         patch[k, f] = edge_zone[(min(a, b), max(a, b))]
-    return Mesh(EToV, VXY, EToE, EToF, ROT, BC, name=path.split("/")[-1], patch=patch, patch_names=names)
+        kf_of_edge[(min(a, b), max(a, b))] = (int(k), int(f))
+    m = Mesh(EToV, VXY, EToE, EToF, ROT, BC, name=path.split("/")[-1], patch=patch, patch_names=names)
+    # each patch's first face in file order (the reference's patch face order)
+    first = {}
+    for n0, n1, c0, c1, z in faces:
+        if c0 == 0 or c1 == 0:
+            pid = bzones.index(int(z))
+            if pid not in first:
+                first[pid] = kf_of_edge[(min(n0, n1) - 1, max(n0, n1) - 1)]
+    m.patch_first_face = np.array([first[i] for i in range(len(names))], np.int32)
+    return m

@@ -286,6 +286,28 @@ int dg_lpc_apply(dg_ctx* ctx, const double* r_host, double* z_host);
 int dg_euler_rhs_noalloc(dg_ctx* ctx, const double* q_dev, double* rhs_dev, int flux);
 
 /* ---------------------------------------------------------------------------
+ * Slope limiter and the limited SSP-RK2 step of the reference's Euler solver
+ * for flows with shocks (DG/DG/godunovFlux/limiteSchemes/scheme/Trianglelimite/
+ * Trianglelimite.C:61-861 via godunovScheme::limite;
+ * tutorials/DG/2D/doubleMach/dgEulerFoam/dgEulerFoam.C:50-101).
+ *
+ * dg_set_boundary_kinds: per boundary slot 0 fixed value, 1 reflective wall
+ * (the boundary value mirrors the interior trace's momentum,
+ * reflectiveDgPatchField.C:79-111; the limiter's ghost cell removes the normal
+ * momentum), 2 other (the limiter's ghost cell copies the owner); gref (may be
+ * NULL = itself) per slot: the slot whose first boundary value a fixed-value
+ * ghost cell takes (the reference uses the first value of the slot's patch).
+ * dg_limit: the limiter on the current state with the current boundary traces.
+ * dg_reflect_boundary_traces: the reflective slots' traces from the state.
+ * dg_limited_ssprk2_step: one step (stage, walls, limiter, stage, walls,
+ * average with the boundary values, limiter, walls); bdata [nb][4][Nfp] holds
+ * this step's values of the fixed-value slots (setBoundaryValues.H). */
+int dg_set_boundary_kinds(dg_ctx* ctx, const int* kinds, const int* gref);
+int dg_limit(dg_ctx* ctx);
+int dg_reflect_boundary_traces(dg_ctx* ctx);
+int dg_limited_ssprk2_step(dg_ctx* ctx, double dt, const double* bdata, int flux, int precision);
+
+/* ---------------------------------------------------------------------------
  * Incompressible Navier-Stokes: the velocity-correction (Chorin) step of
  * tutorials/DG/2D/pearsonVortex/dgChorinFoam/dgChorinFoam.C:63-109, FP64 on
  * the device (one step = convection, pressure Poisson solve, velocity

@@ -774,10 +774,20 @@ static void face_flux(int kind, double gamma, int Nfq, const double* nx, const d
 
 // Weak right-hand side b (before the mass solve) for all 4 conserved variables.
 // q layout: q[v*K*Np + k*Np + i], v = rho, rhou, rhov, E.
-static void euler_weak(const Oracle& O, const double* q, int kind, double gamma, const VortexBC* bc, double* bw) {
+// traces (optional): boundary values per boundary slot (boundary faces in
+// element, face order) [slot][4][Nfp] at the owner's face nodes
+static void euler_weak(const Oracle& O, const double* q, int kind, double gamma, const VortexBC* bc, double* bw,
+                       const double* traces = nullptr) {
     const TriBase& B = O.B;
     int K = O.K, Np = B.Np, Ng = B.Ng, Nfp = B.Nfp, Nfq = B.Nfq;
     size_t KN = (size_t)K * Np;
+    std::vector<int> slot(3 * K, -1);
+    {
+        int nb = 0;
+        for (int k = 0; k < K; k++)
+            for (int f = 0; f < 3; f++)
+                if (O.EToE[k][f] < 0) slot[3 * k + f] = nb++;
+    }
     // face fluxes on owner faces (dgGaussField::initField + godunovScheme::update)
     vec flux((size_t)4 * O.nFaceGauss);
     int nF = (int)O.faces.size();
@@ -810,7 +820,10 @@ static void euler_weak(const Oracle& O, const double* q, int kind, double gamma,
             for (int j = 0; j < Nfp; j++) {
                 int node = B.fci[F.fo][0][j];
                 double q4[4];
-                if (bc) vortex_exact(*bc, O.x[(size_t)F.owner * Np + node], O.y[(size_t)F.owner * Np + node], q4);
+                if (traces) {
+                    const double* t = traces + (size_t)slot[3 * F.owner + F.fo] * 4 * Nfp;
+                    for (int v = 0; v < 4; v++) q4[v] = t[v * Nfp + j];
+                } else if (bc) vortex_exact(*bc, O.x[(size_t)F.owner * Np + node], O.y[(size_t)F.owner * Np + node], q4);
                 else for (int v = 0; v < 4; v++) q4[v] = q[v * KN + (size_t)F.owner * Np + node];
                 for (int v = 0; v < 4; v++) tr[v][j] = q4[v];
             }
@@ -1252,6 +1265,183 @@ static void face_mass_lift(const Oracle& O, const int* mask, const double* g, do
         }
 }
 
+// ---------------------------------------------------------------------------
+// Slope limiter of the reference (DG/DG/godunovFlux/limiteSchemes/scheme/
+// Trianglelimite/Trianglelimite.C:61-861), restated for one state.
+// q: [4][K][Np] conserved variables (reference node order); bnd: per boundary
+// slot (boundary faces in element, face order) the boundary-field values
+// [slot][4][Nfp] at the owner's face nodes; kind: per slot 0 fixed value, 1
+// reflective, 2 other; gref: per slot the slot whose node-0 value a
+// fixed-value ghost cell takes (the reference takes the first value of the
+// patch, :182-185).  gamma 1.4 as in the reference (:73).
+static void limiter(const Oracle& O, double* q, const double* bnd, const int* kind, const int* gref) {
+    const TriBase& B = O.B;
+    const int K = O.K, Np = B.Np, Nfp = B.Nfp, N = B.N;
+    const size_t KN = (size_t)K * Np;
+    const double g = 1.4, tol = 1e-2, eps = 1e-10;
+    // slot of each boundary element face
+    std::vector<int> slot(3 * K, -1);
+    int nb = 0;
+    for (int k = 0; k < K; k++)
+        for (int f = 0; f < 3; f++)
+            if (O.EToE[k][f] < 0) slot[3 * k + f] = nb++;
+    const int T = K + nb;  // cells + one ghost per boundary face
+    // (1) averages with the column sums of the reference mass matrix / 2 (:103-137)
+    // reference mass matrix (V V^T)^-1 = invV^T invV
+    vec mpp(Np, 0.0);
+    for (int i = 0; i < Np; i++)
+        for (int j = 0; j < Np; j++) {
+            double m = 0;
+            for (int l = 0; l < Np; l++) m += B.invV(l, i) * B.invV(l, j);
+            mpp[j] += m / 2;
+        }
+    vec A0(K, 0.0), avg[4], cx(T, 0.0), cy(T, 0.0);
+    for (int v = 0; v < 4; v++) avg[v].assign(T, 0.0);
+    for (int k = 0; k < K; k++) {
+        const std::array<double, 4>& d = O.dxdr[(size_t)k * Np];
+        const double J = d[0] * d[3] - d[1] * d[2];
+        for (int i = 0; i < Np; i++) A0[k] += mpp[i] * J * 2 / 3;
+        for (int j = 0; j < Np; j++) {
+            for (int v = 0; v < 4; v++) avg[v][k] += q[v * KN + (size_t)k * Np + j] * mpp[j];
+            cx[k] += O.x[(size_t)k * Np + j] * mpp[j];
+            cy[k] += O.y[(size_t)k * Np + j] * mpp[j];
+        }
+    }
+    // (2) ghost cells (:152-259): centre reflected across the face line
+    for (int k = 0; k < K; k++)
+        for (int f = 0; f < 3; f++) {
+            const int sl = slot[3 * k + f];
+            if (sl < 0) continue;
+            const Face& F = O.faces[O.cellFace[k][f]];
+            const int gc = K + sl;
+            const double A = F.nx[0], Bn = F.ny[0];
+            const int n0 = B.fci[f][0][0];
+            const double C = -O.x[(size_t)k * Np + n0] * A - O.y[(size_t)k * Np + n0] * Bn;
+            cx[gc] = (Bn * Bn - A * A) * cx[k] - 2 * A * Bn * cy[k] - 2 * A * C;
+            cy[gc] = (-Bn * Bn + A * A) * cy[k] - 2 * A * Bn * cx[k] - 2 * Bn * C;
+            if (kind[sl] == 1) {
+                avg[0][gc] = avg[0][k];
+                avg[1][gc] = avg[1][k] - A * (A * avg[1][k] + Bn * avg[2][k]);
+                avg[2][gc] = avg[2][k] - Bn * (A * avg[1][k] + Bn * avg[2][k]);
+                avg[3][gc] = avg[3][k];
+            } else if (kind[sl] == 0) {
+                for (int v = 0; v < 4; v++) avg[v][gc] = bnd[((size_t)gref[sl] * 4 + v) * Nfp];
+            } else {
+                for (int v = 0; v < 4; v++) avg[v][gc] = avg[v][k];
+            }
+        }
+    // primitive averages (:295-306)
+    vec U(T), V(T), P(T);
+    for (int c = 0; c < T; c++) {
+        U[c] = avg[1][c] / avg[0][c];
+        V[c] = avg[2][c] / avg[0][c];
+        P[c] = (g - 1) * (avg[3][c] - 0.5 * (avg[1][c] * avg[1][c] + avg[2][c] * avg[2][c]) / avg[0][c]);
+    }
+    // (3)-(5) per face owned by a cell, in cell-loop order (:308-459, :500-575)
+    struct FaceV { int o, n; double A2, V[4][2]; };
+    std::vector<FaceV> fv;
+    vec CellA2(T, 0.0);
+    for (int k = 0; k < K; k++)
+        for (int f = 0; f < 3; f++) {
+            const Face& F = O.faces[O.cellFace[k][f]];
+            if (!(F.owner == k && F.fo == f)) continue;
+            const int S = B.fci[f][0][0], E = B.fci[f][0][N];
+            double qS[4], qE[4];
+            int nc;
+            if (F.nbr >= 0) {
+                const int nS = B.fci[F.fn][F.rot][0], nE = B.fci[F.fn][F.rot][N];
+                for (int v = 0; v < 4; v++) {
+                    qS[v] = q[v * KN + (size_t)F.nbr * Np + nS];
+                    qE[v] = q[v * KN + (size_t)F.nbr * Np + nE];
+                }
+                nc = F.nbr;
+            } else {
+                const int sl = slot[3 * k + f];
+                for (int v = 0; v < 4; v++) {
+                    qS[v] = bnd[((size_t)sl * 4 + v) * Nfp];
+                    qE[v] = bnd[((size_t)sl * 4 + v) * Nfp + Nfp - 1];
+                }
+                nc = K + sl;
+            }
+            double f0[4], f1[4];
+            for (int v = 0; v < 4; v++) {
+                f0[v] = q[v * KN + (size_t)k * Np + S] * 0.5 + qS[v] * 0.5;
+                f1[v] = q[v * KN + (size_t)k * Np + E] * 0.5 + qE[v] * 0.5;
+            }
+            const double x1v = O.x[(size_t)k * Np + S], y1v = O.y[(size_t)k * Np + S];
+            const double x2v = O.x[(size_t)k * Np + E], y2v = O.y[(size_t)k * Np + E];
+            FaceV w;
+            w.o = k;
+            w.n = nc;
+            w.A2 = F.nbr >= 0 ? A0[k] + A0[F.nbr] : A0[k] + A0[k];
+            const double x0c = cx[k], y0c = cy[k], x1c = cx[nc], y1c = cy[nc];
+            const double Af = ((x1c - x0c) * (y2v - y1v) - (x2v - x1v) * (y1c - y0c)) * 0.5;
+            // face primitives
+            double p0[4], p1[4];
+            p0[0] = f0[0];
+            p1[0] = f1[0];
+            p0[1] = f0[1] / f0[0];
+            p1[1] = f1[1] / f1[0];
+            p0[2] = f0[2] / f0[0];
+            p1[2] = f1[2] / f1[0];
+            p0[3] = (g - 1) * (f0[3] - 0.5 * f0[0] * (p0[1] * p0[1] + p0[2] * p0[2]));
+            p1[3] = (g - 1) * (f1[3] - 0.5 * f1[0] * (p1[1] * p1[1] + p1[2] * p1[2]));
+            const double* cq[4] = {avg[0].data(), U.data(), V.data(), P.data()};
+            const double t1 = x2v - x1v, t2 = x1c - x0c;
+            for (int m = 0; m < 4; m++) {
+                w.V[m][0] = 0.5 * ((cq[m][nc] - cq[m][k]) * (y2v - y1v) + (p0[m] - p1[m]) * (y1c - y0c)) / Af;
+                w.V[m][1] = -0.5 * ((cq[m][nc] - cq[m][k]) * t1 + (p0[m] - p1[m]) * t2) / Af;
+            }
+            CellA2[k] += w.A2;
+            if (nc < K) CellA2[nc] += w.A2;
+            fv.push_back(w);
+        }
+    std::vector<std::array<double, 8>> CV(T);
+    for (auto& a : CV) a.fill(0.0);
+    for (const FaceV& w : fv) {
+        for (int m = 0; m < 4; m++)
+            for (int d = 0; d < 2; d++) {
+                CV[w.o][2 * m + d] += w.A2 * w.V[m][d] / CellA2[w.o];
+                if (w.n < K) CV[w.n][2 * m + d] += w.A2 * w.V[m][d] / CellA2[w.n];
+                else CV[w.n][2 * m + d] = w.V[m][d];
+            }
+    }
+    // (6) weighted neighbour gradients and the linear reconstruction (:705-858)
+    for (int k = 0; k < K; k++) {
+        int c[3];
+        for (int f = 0; f < 3; f++) c[f] = O.EToE[k][f] >= 0 ? O.EToE[k][f] : K + slot[3 * k + f];
+        double L[4][2];
+        for (int m = 0; m < 4; m++) {
+            double gg[3];
+            for (int i = 0; i < 3; i++) gg[i] = CV[c[i]][2 * m] * CV[c[i]][2 * m] + CV[c[i]][2 * m + 1] * CV[c[i]][2 * m + 1];
+            const double fac = gg[0] * gg[0] + gg[1] * gg[1] + gg[2] * gg[2];
+            const double w1 = (gg[1] * gg[2] + eps) / (fac + 3 * eps);
+            const double w2 = (gg[0] * gg[2] + eps) / (fac + 3 * eps);
+            const double w3 = (gg[1] * gg[0] + eps) / (fac + 3 * eps);
+            for (int d = 0; d < 2; d++) L[m][d] = w1 * CV[c[0]][2 * m + d] + w2 * CV[c[1]][2 * m + d] + w3 * CV[c[2]][2 * m + d];
+        }
+        for (int p = 0; p < Np; p++) {
+            const double dx = O.x[(size_t)k * Np + p] - cx[k], dy = O.y[(size_t)k * Np + p] - cy[k];
+            double du = dx * L[0][0] + dy * L[0][1];
+            const double du1 = dx * L[1][0] + dy * L[1][1];
+            const double du2 = dx * L[2][0] + dy * L[2][1];
+            const double du3 = dx * L[3][0] + dy * L[3][1];
+            double Lrho = avg[0][k] + du;
+            for (int it = 0; it < 64 && Lrho < tol; it++) {  // (the reference loops until positive)
+                du *= 0.5;
+                Lrho = avg[0][k] + du;
+            }
+            const size_t i = (size_t)k * Np + p;
+            q[i] = Lrho;
+            q[KN + i] = avg[1][k] + avg[0][k] * du1 + du * U[k];
+            q[2 * KN + i] = avg[2][k] + avg[0][k] * du2 + du * V[k];
+            const double dE = (1 / (g - 1)) * du3 + 0.5 * du * (U[k] * U[k] + V[k] * V[k]) +
+                              avg[0][k] * (U[k] * du1 + V[k] * du2);
+            q[3 * KN + i] = avg[3][k] + dE;
+        }
+    }
+}
+
 }  // namespace orc
 
 // ---------------------------------------------------------------------------
@@ -1521,6 +1711,26 @@ void orc_ins_convection(void* h, const double* u, const double* ubnd, double* ou
 }
 void orc_face_mass_lift(void* h, const int* mask, const double* g, double* b) {
     face_mass_lift(*(Oracle*)h, mask, g, b);
+}
+
+// R(q) with boundary values per slot
+void orc_euler_rhs_traces(void* h, const double* q, double* rhs, int flux, double gamma, const double* traces) {
+    Oracle& O = *(Oracle*)h;
+    const int K = O.K, Np = O.B.Np;
+    const size_t KN = (size_t)K * Np;
+    vec bw(4 * KN);
+    euler_weak(O, q, flux, gamma, nullptr, bw.data(), traces);
+    for (int v = 0; v < 4; v++)
+        for (int k = 0; k < K; k++)
+            for (int i = 0; i < Np; i++) {
+                double sacc = 0;
+                for (int j = 0; j < Np; j++) sacc += O.Minv[k](i, j) * bw[v * KN + (size_t)k * Np + j];
+                rhs[v * KN + (size_t)k * Np + i] = sacc;
+            }
+}
+
+void orc_limiter(void* h, double* q, const double* bnd, const int* kind, const int* gref) {
+    limiter(*(Oracle*)h, q, bnd, kind, gref);
 }
 
 void orc_set_threads(int n) {

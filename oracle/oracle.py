@@ -50,6 +50,8 @@ def lib():
         L.orc_ins_curlcurl.argtypes = [ctypes.c_void_p, _dp, _dp]
         L.orc_ins_convection.argtypes = [ctypes.c_void_p, _dp, _dp, _dp]
         L.orc_face_mass_lift.argtypes = [ctypes.c_void_p, _ip, _dp, _dp]
+        L.orc_limiter.argtypes = [ctypes.c_void_p, _dp, _dp, _ip, _ip]
+        L.orc_euler_rhs_traces.argtypes = [ctypes.c_void_p, _dp, _dp, ctypes.c_int, ctypes.c_double, _dp]
         L.orc_set_threads.argtypes = [ctypes.c_int]
         L.orc_max_threads.restype = ctypes.c_int
         _lib = L
@@ -212,6 +214,25 @@ class Oracle:
         b = np.zeros(self.K * self.Np)
         self.L.orc_face_mass_lift(self.h, _i(m), _d(g), _d(b))
         return b.reshape(self.K, self.Np)
+
+    def euler_rhs_traces(self, q, traces, flux=FLUX_ROE, gamma=1.4):
+        """R(q) with fixed boundary values per boundary slot [nb][4][Nfp]."""
+        q = np.ascontiguousarray(q, np.float64).reshape(-1)
+        t = np.ascontiguousarray(traces, np.float64)
+        out = np.zeros_like(q)
+        self.L.orc_euler_rhs_traces(self.h, _d(q), _d(out), flux, gamma, _d(t))
+        return out
+
+    def limiter(self, q, bnd, kind, gref=None):
+        """The reference's slope limiter applied to q ([4][K][Np]); bnd per
+        boundary slot [nb][4][Nfp], kind per slot (0 fixed value, 1
+        reflective, 2 other), gref per slot (default: itself)."""
+        q = np.array(q, np.float64, copy=True).reshape(-1)
+        bnd = np.ascontiguousarray(bnd, np.float64)
+        kind = np.ascontiguousarray(kind, np.int32)
+        gref = np.ascontiguousarray(np.arange(len(kind)) if gref is None else gref, np.int32)
+        self.L.orc_limiter(self.h, _d(q), _d(bnd), _i(kind), _i(gref))
+        return q.reshape(4, self.K, self.Np)
 
     def blk_apply(self, diag, off, x):
         x = np.ascontiguousarray(x, np.float64)

@@ -25,6 +25,8 @@ def golden_mesh(name):
     if "patch" in d:
         m.patch = d["patch"]
         m.patch_names = tuple(str(x) for x in d["patch_names"])
+    if "patch_first_face" in d:
+        m.patch_first_face = d["patch_first_face"]
     return m
 
 

@@ -7,6 +7,9 @@
 * ``pearson_h.npz`` / ``pearson_0.5h.npz`` / ``pearson_0.25h.npz``: the
   Pearson-vortex tutorial meshes (tutorials/DG/2D/pearsonVortex/vortexh.msh,
   vortex0.5h.msh, vortex0.25h.msh) with their inlet / outlet boundary patches.
+* ``doublemach.npz``: the double-Mach-reflection tutorial mesh
+  (tutorials/DG/2D/doubleMach/doubleMach.msh) with its patches and each
+  patch's first face in file order.
 * ``vortex_kat.json``: the reference's published accuracy table for that case
   ("2017-07-24-OpenFOAM workshop.pptx", slide 18: Roe flux, SSP-RK2, exact
   fixed-value boundary, t = 2; mean absolute nodal error of rho and |rhoU|),
@@ -47,6 +50,9 @@ def main():
         m = read_fluent_msh(os.path.join(pv, src + ".msh"))
         np.savez_compressed(os.path.join(HERE, name + ".npz"), EToV=m.EToV, VXY=m.VXY, patch=m.patch,
                             patch_names=np.array(m.patch_names))
+    m = read_fluent_msh(os.path.join(root, "HopeFOAM-0.1", "tutorials", "DG", "2D", "doubleMach", "doubleMach.msh"))
+    np.savez_compressed(os.path.join(HERE, "doublemach.npz"), EToV=m.EToV, VXY=m.VXY, patch=m.patch,
+                        patch_names=np.array(m.patch_names), patch_first_face=m.patch_first_face)
     kat = {
         "source": "2017-07-24-OpenFOAM workshop.pptx, slide 18",
         "case": "isentropic vortex beta=5 centre (5,0) u_inf=1, gamma=1.4, Roe flux, SSP-RK2, exact fixed-value "

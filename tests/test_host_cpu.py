@@ -123,3 +123,37 @@ def test_batch_case_list_is_seeded():
     own = np.repeat([0, 1], [m1.K, m2.K])
     nb = big.EToE
     assert np.all(own[nb] == own[:, None])
+
+
+def test_oracle_limiter_properties():
+    """The restated limiter keeps a uniform state, keeps each element's
+    average of rho (when no density correction triggers) and leaves every
+    element linear."""
+    from hopefoam_gb300 import euler
+    from hopefoam_gb300.mesh import box_square, load_cubature
+    from oracle.oracle import Oracle
+
+    N = 3
+    m = box_square(5, 4, 1.0, 1.0)
+    orc = Oracle(m, N, load_cubature(12))
+    x, y = orc.nodes()
+    kk, ff = euler.boundary_faces(m)
+    nb = len(kk)
+    fn = euler.face_nodes(N)
+    const = np.stack([np.full_like(x, 1.2), np.full_like(x, 0.3), np.full_like(x, -0.1), np.full_like(x, 3.0)])
+    bnd = np.stack([const[:, k, fn[f]] for k, f in zip(kk, ff)])
+    out = orc.limiter(const, bnd, np.zeros(nb, np.int32))
+    assert np.allclose(out, const, rtol=0, atol=1e-13)
+    rho = 1 + 0.2 * np.sin(3 * x) * np.cos(2 * y)
+    q = np.stack([rho, rho * 0.4, rho * 0.1, 2.5 + 0.1 * x])
+    bnd = np.stack([q[:, k, fn[f]] for k, f in zip(kk, ff)])
+    out = orc.limiter(q, bnd, np.full(nb, 2, np.int32))
+    M = orc.mass()
+    w = M.sum(1)  # integral weights of each node
+    assert np.allclose((w * out[0]).sum(1), (w * q[0]).sum(1), rtol=1e-12)
+    ops = orc.operators()
+    r, s = ops["r"], ops["s"]
+    A = np.stack([np.ones_like(r), r, s], 1)  # linear fit per element is exact
+    for v in range(4):
+        coef, res, *_ = np.linalg.lstsq(A, out[v].T, rcond=None)
+        assert np.abs(A @ coef - out[v].T).max() < 1e-11

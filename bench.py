@@ -337,6 +337,11 @@ def main():
                 line[key] = fn() if key == "c1" else fn(nsteps=args.kh_steps)
             except Exception as exc:
                 line[key] = {"error": str(exc)}
+    if rank == 0 and not args.no_configs:
+        try:
+            line["shock"] = shock_bench(with_cpu=not args.no_cpu_baseline)
+        except Exception as exc:
+            line["shock"] = {"error": str(exc)}
     if rank == 0 and not args.no_ins:
         try:
             line["ins"] = ins_bench(with_cpu=not args.no_cpu_baseline)
@@ -562,6 +567,68 @@ def ins_bench(n=128, order=2, steps=4, warmup=2, with_cpu=True, cpu_steps=2):
         out["cpu_baseline"] = {"value": mesh.K * Np * 3 / el, "unit": out["unit"], "cores": threads, "kind": "port",
                                "ms_per_step": el * 1e3, "setup_s": setup,
                                "sample": "%d oracle steps on the same mesh (sparse LU factorised at setup)" % cpu_steps}
+    return out
+
+
+def shock_bench(steps=200, warmup=5, with_cpu=True, cpu_steps=3):
+    """The reference's double-Mach-reflection tutorial (5390 triangles, N = 4,
+    Roe flux, dt = 1e-5, limited SSP-RK2 with reflective wall and the moving
+    shock's boundary values): device ms per step through
+    dg_limited_ssprk2_step (the boundary data are host arrays uploaded each
+    step, as the reference sets them each step), FP64 and split precision;
+    CPU baseline: the oracle's limited step on the same state."""
+    import ctypes
+
+    import torch
+
+    from hopefoam_gb300 import _lib as L
+    from hopefoam_gb300 import euler
+    from hopefoam_gb300.mesh import Mesh, connect
+    from hopefoam_gb300.shock import DoubleMach
+
+    d = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "tests", "golden", "doublemach.npz"))
+    EToE, EToF, ROT, BC = connect(d["EToV"])
+    mesh = Mesh(d["EToV"], d["VXY"], EToE, EToF, ROT, BC, name="doubleMach", patch=d["patch"],
+                patch_names=tuple(str(x) for x in d["patch_names"]))
+    mesh.patch_first_face = d["patch_first_face"]
+    N, dt = 4, 1e-5
+    dm = DoubleMach(mesh, N)
+    out = {"workload": "double Mach reflection (tutorial mesh, K=%d), N=%d, Roe, dt=1e-5, limited SSP-RK2" % (mesh.K, N)}
+    for name, prec in (("fp64", L.DG_PREC_FP64), ("split", L.DG_PREC_SPLIT)):
+        ctx = euler.EulerContext(mesh, N)
+        ctx.upload(dm.initial_state())
+        ctx.set_boundary_traces(dm.bdata(0.0))
+        ctx.set_boundary_kinds(dm.kinds, dm.gref)
+        t = 0.0
+        bd = [np.ascontiguousarray(dm.bdata(t + i * dt)) for i in range(warmup + steps)]
+        for i in range(warmup):
+            ctx.limited_ssprk2(dt, bd[i], precision=prec)
+        stream = torch.cuda.ExternalStream(ctx.stream)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for i in range(steps):
+            ctx.limited_ssprk2(dt, bd[warmup + i], precision=prec)
+        e1.record(stream)
+        e1.synchronize()
+        ms = e0.elapsed_time(e1) / steps
+        q = ctx.download()
+        out[name] = {"ms_per_step": ms, "value": mesh.K * ctx.Np * 4 * 2 / (ms * 1e-3), "unit": "DOF-stage/s",
+                     "state_finite": bool(np.isfinite(q).all()), "rho_min_max": [float(q[0].min()), float(q[0].max())]}
+        ctx.close()
+    if with_cpu:
+        from hopefoam_gb300.mesh import load_cubature
+        from oracle import oracle
+        from oracle.limited_oracle import LimitedSSPOracle
+
+        lo = LimitedSSPOracle(mesh, N, load_cubature(3 * (N + 1)), dm.kinds, dm.gref)
+        q = dm.initial_state()
+        q = lo.step(q, dt, dm.bdata(0.0))
+        t0 = time.perf_counter()
+        for i in range(cpu_steps):
+            q = lo.step(q, dt, dm.bdata((i + 1) * dt))
+        el = (time.perf_counter() - t0) / cpu_steps
+        out["cpu_baseline"] = {"ms_per_step": el * 1e3, "kind": "port", "cores": oracle.max_threads(),
+                               "sample": "%d oracle limited steps on the same mesh" % cpu_steps}
     return out
 
 

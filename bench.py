@@ -347,6 +347,10 @@ def main():
             line["ins"] = ins_bench(with_cpu=not args.no_cpu_baseline)
         except Exception as exc:
             line["ins"] = {"error": str(exc)}
+        try:
+            line["cylinder"] = cylinder_bench(with_cpu=not args.no_cpu_baseline)
+        except Exception as exc:
+            line["cylinder"] = {"error": str(exc)}
     if rank == 0 and args.c5_study:
         try:
             line["c5_study"] = c5_study(n=args.c5_study_n)
@@ -629,6 +633,65 @@ def shock_bench(steps=200, warmup=5, with_cpu=True, cpu_steps=3):
         el = (time.perf_counter() - t0) / cpu_steps
         out["cpu_baseline"] = {"ms_per_step": el * 1e3, "kind": "port", "cores": oracle.max_threads(),
                                "sample": "%d oracle limited steps on the same mesh" % cpu_steps}
+    return out
+
+
+def cylinder_bench(steps=100, warmup=5, with_cpu=True, cpu_steps=3):
+    """The reference's cylinder tutorial as it stands (tutorials/DG/2D/cylinder:
+    its polyMesh of 1840 triangles with the two arc patches of the cylinder,
+    order 3, nu = 0.001, dt = 2e-4, time-varying inflow): device ms per Chorin
+    step through dg_ins_step (PCG to a relative residual of 1e-10, about the
+    FP64 floor of this case's pressure systems) and the oracle's step (sparse
+    LU, the reference's preonly + LU) on the same case; after the timed steps,
+    the state is compared with the oracle run for the same number of steps."""
+    from hopefoam_gb300.curved import ArcCurve
+    from hopefoam_gb300.ins import ChorinSolver, CylinderFlow
+    from hopefoam_gb300.mesh import Mesh, connect
+
+    d = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "tests", "golden", "cylinder.npz"))
+    EToE, EToF, ROT, BC = connect(d["EToV"])
+    mesh = Mesh(d["EToV"], d["VXY"], EToE, EToF, ROT, BC, name="cylinder", patch=d["patch"],
+                patch_names=tuple(str(x) for x in d["patch_names"]))
+    mesh.curves = {str(n): ArcCurve.from_code(str(c), tuple(u), name=str(n))
+                   for n, c, u in zip(d["arc_names"], d["arc_codes"], d["arc_u_range"])}
+    N, nu, dt = CylinderFlow.ORDER, CylinderFlow.NU, CylinderFlow.DT
+    uk, pk = CylinderFlow.kinds(mesh)
+    g = ChorinSolver(mesh, N, nu=nu, dt=dt, u_kind=uk, p_kind=pk)
+    cf = CylinderFlow(g)
+    g.set_state(*cf.initial_state())
+    t = 0.0
+    sts = []
+    for i in range(warmup + steps):
+        st = g.step(cf.bdata(t), rtol=1e-10)
+        if i >= warmup:
+            sts.append(st)
+        t += dt
+    U, p = g.get_state()
+    ms = float(np.mean([s["ms"] for s in sts]))
+    out = {"workload": "cylinder tutorial (polyMesh K=%d, arc patches), N=%d, nu=%g, dt=%g, rtol 1e-10"
+                       % (mesh.K, N, nu, dt),
+           "ms_per_step": ms, "steps": steps, "value": mesh.K * g.Np * 3 / (ms * 1e-3),
+           "unit": "DOF-steps/s (3 fields)",
+           "iterations_p_u": [sts[-1]["iterations_p"], list(sts[-1]["iterations_u"])],
+           "max_speed": float(np.hypot(U[0], U[1]).max())}
+    g.close()
+    if with_cpu:
+        from hopefoam_gb300.mesh import load_cubature
+        from oracle import oracle
+        from oracle.ins_oracle import ChorinOracle, CylinderCase
+
+        o = ChorinOracle(mesh, N, load_cubature(3 * (N + 1)), nu=nu, dt=dt, case=CylinderCase(nu, dt))
+        o.step()  # first step (BDF1) factorises its Helmholtz operator
+        t0 = time.perf_counter()
+        for _ in range(cpu_steps):
+            o.step()
+        el = (time.perf_counter() - t0) / cpu_steps
+        out["cpu_baseline"] = {"ms_per_step": el * 1e3, "kind": "port", "cores": oracle.max_threads(),
+                               "sample": "%d oracle steps on the same case (sparse LU at setup)" % cpu_steps}
+        for _ in range(warmup + steps - 1 - cpu_steps):
+            o.step()
+        out["state_vs_oracle"] = float(max(np.linalg.norm(U - o.U) / np.linalg.norm(o.U),
+                                           np.linalg.norm(p - o.p) / max(np.linalg.norm(o.p), 1e-300)))
     return out
 
 

@@ -75,6 +75,7 @@ SIGNATURES = {
     "dg_ipdg_apply": (ctypes.c_int, [_vp, _dp, _dp]),
     "dg_ipdg_set_boundary_types": (ctypes.c_int, [_vp, _ip]),
     "dg_ipdg_set_mass": (ctypes.c_int, [_vp, ctypes.c_double]),
+    "dg_set_node_locations": (ctypes.c_int, [_vp, _dp, _dp]),
     "dg_set_boundary_kinds": (ctypes.c_int, [_vp, _ip, _ip]),
     "dg_limit": (ctypes.c_int, [_vp]),
     "dg_reflect_boundary_traces": (ctypes.c_int, [_vp]),

@@ -40,6 +40,9 @@ struct dg_ctx {
     std::vector<int> conn_host;
     std::vector<int> etov_host;  // [K][3] vertex ids (empty when the mesh descriptor has none)
     std::vector<double> vxy_host;  // [K][3][2] vertex coordinates
+    // [2][K][Np] node locations from dg_set_node_locations (curved patches);
+    // empty: the straight element's x(r, s)
+    std::vector<double> node_xy_host;
     struct LimState* lim = nullptr;  // slope limiter / limited SSP-RK2 state (limiter.cu)
     // device buffers
     double* d_q[2] = {nullptr, nullptr};

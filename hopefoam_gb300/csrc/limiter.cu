@@ -393,7 +393,47 @@ void limiter_teardown(dg_ctx* c) {
     c->lim = nullptr;
 }
 
+// node locations in ring order: those of dg_set_node_locations, else the
+// straight element's x = -(r+s)/2 v0 + (r+1)/2 v1 + (s+1)/2 v2
+static void node_locations(const dg_ctx* c, std::vector<double>& xn, std::vector<double>& yn) {
+    const int K = c->K, Np = c->Np;
+    const dgb::RefOps& o = c->ops;
+    const size_t KN = (size_t)K * Np;
+    xn.resize(KN);
+    yn.resize(KN);
+    const bool given = c->node_xy_host.size() == 2 * KN;
+    for (int k = 0; k < K; k++) {
+        const double* v = &c->vxy_host[6 * (size_t)k];
+        for (int p = 0; p < Np; p++) {
+            const size_t d = (size_t)k * Np + p;
+            if (given) {
+                xn[d] = c->node_xy_host[(size_t)k * Np + o.ring[p]];
+                yn[d] = c->node_xy_host[KN + (size_t)k * Np + o.ring[p]];
+            } else {
+                const double r = o.r[o.ring[p]], t = o.s[o.ring[p]];
+                xn[d] = -(r + t) * 0.5 * v[0] + (r + 1) * 0.5 * v[2] + (t + 1) * 0.5 * v[4];
+                yn[d] = -(r + t) * 0.5 * v[1] + (r + 1) * 0.5 * v[3] + (t + 1) * 0.5 * v[5];
+            }
+        }
+    }
+}
+
 extern "C" {
+
+int dg_set_node_locations(dg_ctx* c, const double* x, const double* y) {
+    if (!c || !x || !y) return DG_ERR_ARG;
+    const size_t KN = (size_t)c->K * c->Np;
+    c->node_xy_host.assign(x, x + KN);
+    c->node_xy_host.insert(c->node_xy_host.end(), y, y + KN);
+    if (c->lim && c->lim->ready) {  // the limiter already holds node locations: replace them
+        std::vector<double> xn, yn;
+        node_locations(c, xn, yn);
+        LIM_CUDA(c, cudaMemcpyAsync(c->lim->xn, xn.data(), KN * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+        LIM_CUDA(c, cudaMemcpyAsync(c->lim->yn, yn.data(), KN * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+        LIM_CUDA(c, cudaStreamSynchronize(c->stream));
+    }
+    return DG_OK;
+}
 
 int dg_set_boundary_kinds(dg_ctx* c, const int* kind, const int* gref) {
     if (!c || (c->nb > 0 && !kind)) return DG_ERR_ARG;
@@ -415,17 +455,9 @@ int dg_set_boundary_kinds(dg_ctx* c, const int* kind, const int* gref) {
                 sk.push_back(k);
                 sf.push_back(f);
             }
-    // node coordinates in ring order, x = -(r+s)/2 v0 + (r+1)/2 v1 + (s+1)/2 v2
     const dgb::RefOps& o = c->ops;
-    std::vector<double> xn((size_t)K * Np), yn((size_t)K * Np), mpp(Np, 0.0);
-    for (int k = 0; k < K; k++) {
-        const double* v = &c->vxy_host[6 * (size_t)k];
-        for (int p = 0; p < Np; p++) {
-            const double r = o.r[o.ring[p]], t = o.s[o.ring[p]];
-            xn[(size_t)k * Np + p] = -(r + t) * 0.5 * v[0] + (r + 1) * 0.5 * v[2] + (t + 1) * 0.5 * v[4];
-            yn[(size_t)k * Np + p] = -(r + t) * 0.5 * v[1] + (r + 1) * 0.5 * v[3] + (t + 1) * 0.5 * v[5];
-        }
-    }
+    std::vector<double> xn, yn, mpp(Np, 0.0);
+    node_locations(c, xn, yn);
     // column sums / 2 of the reference mass matrix (V V^T)^-1 (ring order)
     for (int p = 0; p < Np; p++) {
         double sm = 0;

@@ -82,6 +82,9 @@ class EulerContext:
         self.n_bfaces = info.n_bfaces
         self.stream = info.stream
         self.device_bytes = info.device_bytes
+        if getattr(mesh, "curves", None):  # nodes next to curved patches sit on their curves
+            ops = reference_operators(order)
+            self.set_node_locations(*node_coords(mesh, ops["r"], ops["s"]))
 
     def close(self):
         if getattr(self, "h", None):
@@ -129,6 +132,14 @@ class EulerContext:
         _check(self.h, self.lib.dg_ssprk2_step(self.h, float(dt), int(nsteps), flux, precision))
 
     # --- limiter (shock cases) -------------------------------------------
+    def set_node_locations(self, x, y):
+        """Node locations (K, Np) read by the limiter (curved patches move them;
+        the operators keep the straight element's metrics)."""
+        x = np.ascontiguousarray(x, np.float64).reshape(-1)
+        y = np.ascontiguousarray(y, np.float64).reshape(-1)
+        assert x.size == self.K * self.Np and y.size == x.size
+        _check(self.h, self.lib.dg_set_node_locations(self.h, L.dptr(x), L.dptr(y)))
+
     def set_boundary_kinds(self, kinds, gref=None):
         """Per boundary slot: 0 fixed value, 1 reflective wall, 2 other."""
         k = np.ascontiguousarray(kinds, np.int32)
@@ -202,10 +213,17 @@ def boundary_traces_from_nodes(mesh, order, qnode_fn, x, y):
 
 
 def node_coords(mesh, r, s):
-    """Physical node coordinates x(r,s) of every element (triangleBaseFunction.C:303-313)."""
+    """Physical node coordinates x(r,s) of every element (triangleBaseFunction.C:303-313),
+    with the nodes next to curved patches moved onto their curves when the mesh
+    carries curves (curved.curve_node_shift)."""
     v = mesh.VXY
     x = (-(r + s)[None, :] * 0.5 * v[:, 0, 0:1] + (r + 1)[None, :] * 0.5 * v[:, 1, 0:1]
          + (s + 1)[None, :] * 0.5 * v[:, 2, 0:1])
     y = (-(r + s)[None, :] * 0.5 * v[:, 0, 1:2] + (r + 1)[None, :] * 0.5 * v[:, 1, 1:2]
          + (s + 1)[None, :] * 0.5 * v[:, 2, 1:2])
+    if getattr(mesh, "curves", None):
+        from .curved import curve_node_shift
+
+        order = int(round((np.sqrt(8 * len(r) + 1) - 3) / 2))
+        x, y = curve_node_shift(mesh, order, x, y)
     return x, y

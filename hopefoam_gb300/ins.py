@@ -7,7 +7,9 @@ ChorinSolver mirrors the solver's time loop (dgChorinFoam.C:63-109): one
 Helmholtz solve per velocity component, with BDF1/EXT1 on the first step and
 BDF2/EXT2 after.  The boundary data of each step come from the caller
 (``PearsonVortex.bdata`` restates setBoundaryValues.H, setparaT.H and the
-exact-solution terms of pCorrectEquation.H for that case).
+exact-solution terms of pCorrectEquation.H for that case; ``CylinderFlow``
+does the same for the cylinder tutorial, tutorials/DG/2D/cylinder, whose
+curved patches move the boundary nodes the inflow is evaluated at).
 """
 import ctypes
 
@@ -160,6 +162,63 @@ class PearsonVortex:
         """average and max |p - p_exact| over the nodes (chorinerror.H)."""
         d = np.abs(p - self.exact(self.s.x, self.s.y, t)[2])
         return float(d.mean()), float(d.max())
+
+
+class CylinderFlow:
+    """The cylinder tutorial (tutorials/DG/2D/cylinder: channel flow past a
+    cylinder of radius 0.05 whose two halves are arc patches; nu = 0.001,
+    dt = 2e-4, order 3): boundary kinds of its 0/U and 0/p, the inflow profile
+    and the per-step boundary data of its solver (setNonUniformInlet.H,
+    setBoundaryValues.H, setparaT.H, the inlet term of pCorrectEquation.H).
+
+    U fixedValue on inlet, channel and the cylinder (zero there), zeroGradient
+    on the outlet; p zeroGradient except on the outlet (fixedValue 0).  Inflow
+    u = 6 (y + 0.2)(0.21 - y) / 0.41^2 * sin(pi t / 8)."""
+
+    U_FIXED = ("inlet", "channel", "upcylinder", "downcylinder")
+    NU, DT, ORDER = 0.001, 2e-4, 3
+
+    @classmethod
+    def kinds(cls, mesh):
+        """(u_kind, p_kind) per boundary slot for ChorinSolver."""
+        kk, ff = boundary_faces(mesh)
+        names = [mesh.patch_names[i] for i in mesh.patch[kk, ff]]
+        fixed = np.array([n in cls.U_FIXED for n in names])
+        if not all(n in cls.U_FIXED or n == "outlet" for n in names):
+            raise ValueError("cylinder case: unexpected patch among %s" % sorted(set(names)))
+        return np.where(fixed, 0, 1).astype(np.int32), np.where(fixed, 2, 0).astype(np.int32)
+
+    def __init__(self, solver):
+        self.s = solver
+        kk, ff = solver.bk, solver.bf
+        names = list(solver.mesh.patch_names)
+        self.inlet = solver.mesh.patch[kk, ff] == names.index("inlet")
+
+    @staticmethod
+    def profile(y):
+        return (1.0 / 0.41) ** 2 * 6.0 * (y + 0.2) * (0.21 - y)
+
+    def initial_state(self):
+        z = np.zeros((self.s.K, self.s.Np))
+        return np.stack([z, z]), z.copy()
+
+    def bdata(self, t, first=None):
+        """Boundary data of the step that starts at time t.  The solver holds
+        the inflow of t (of t = 0 without the time factor before the first
+        step, setNonUniformInlet.H) and scales it by sin(pi (t+dt)/8) / its
+        factor at t (paraT4); the inlet's pressure Neumann term is
+        -n_x du/dt = -profile * pi/8 cos(pi t/8) (paraT1)."""
+        s = self.s
+        first = (t == 0.0) if first is None else first
+        fac = 1.0 if first else np.sin(PI * t / 8.0)
+        prof = self.profile(s.by)
+        inl = self.inlet[:, None]
+        u = np.where(inl, prof * fac, 0.0)
+        ub = np.stack([u, np.zeros_like(u)], 1)
+        para_t1 = PI / 8.0 * np.cos(PI * t / 8.0)
+        extra = np.where(inl, -prof * para_t1, 0.0)
+        return dict(u_value=ub, p_neumann_extra=extra, p_data_scale=para_t1,
+                    u_data_scale=np.sin(PI * (t + s.dt) / 8.0) / fac)
 
 
 def pearson_mesh(n, name=""):

@@ -34,6 +34,8 @@ class Mesh:
     patch: np.ndarray = None
     patch_names: tuple = ()
     patch_first_face: np.ndarray = None  # per patch (k, f) of its first face in the file's order
+    # curved patches: patch name -> curved.ArcCurve; their faces' nodes lie on the curve
+    curves: dict = None
 
     @property
     def K(self):

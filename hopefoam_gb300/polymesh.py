@@ -6,8 +6,9 @@ face's own point order, and swaps its last two points when they run clockwise
 seen from +z (dgPolyMesh.C:154-183 picks the face, :489-506 reorders).  The
 other boundary patches (side faces, two points in the z = 0 plane) become the
 triangles' boundary edges, tagged with their patch (``Mesh.patch``); patches
-of type ``empty`` (the two planes) are not edges.  Only triangles (prism
-cells) are read; quads (hex cells) are outside this triangle-only path.
+of type ``empty`` (the two planes) are not edges.  Patches of type ``arc``
+carry their curve (``Mesh.curves``, curved.read_arc_patches).  Only triangles
+(prism cells) are read; quads (hex cells) are outside this triangle-only path.
 
 write_polymesh writes a Mesh as such a one-layer prism mesh (points at z = 0
 and z = dz, the z = 0 triangles as the cells' first face), so that cases can
@@ -160,8 +161,11 @@ def read_polymesh(path):
         if key not in edge_patch:
             raise ValueError("boundary edge %s of cell %d belongs to no patch" % (key, k))
         patch[k, f] = edge_patch[key]
+    from .curved import read_arc_patches
+
+    curves = {n: c for n, c in read_arc_patches(_read(os.path.join(d, "boundary"))).items() if n in names}
     return Mesh(EToV, VXY, EToE, EToF, ROT, BC, name=os.path.basename(os.path.dirname(os.path.dirname(d))) or d,
-                patch=patch, patch_names=tuple(names))
+                patch=patch, patch_names=tuple(names), curves=curves or None)
 
 
 def _write(path, cls, location, obj, body):

@@ -301,7 +301,14 @@ int dg_euler_rhs_noalloc(dg_ctx* ctx, const double* q_dev, double* rhs_dev, int 
  * dg_reflect_boundary_traces: the reflective slots' traces from the state.
  * dg_limited_ssprk2_step: one step (stage, walls, limiter, stage, walls,
  * average with the boundary values, limiter, walls); bdata [nb][4][Nfp] holds
- * this step's values of the fixed-value slots (setBoundaryValues.H). */
+ * this step's values of the fixed-value slots (setBoundaryValues.H).
+ * dg_set_node_locations: node locations x, y ([K][Np] each, reference node
+ * order) for the code that reads them (the limiter's cell geometry), as the
+ * nodes next to curved arc patches are moved after the element metrics are
+ * built (physicalElementData.C:186-224); the operators keep the straight
+ * element's metrics, as the reference's do.  Default: the straight element's
+ * nodes. */
+int dg_set_node_locations(dg_ctx* ctx, const double* x, const double* y);
 int dg_set_boundary_kinds(dg_ctx* ctx, const int* kinds, const int* gref);
 int dg_limit(dg_ctx* ctx);
 int dg_reflect_boundary_traces(dg_ctx* ctx);

@@ -1493,6 +1493,15 @@ void orc_nodes(void* h, double* x, double* y) {
     std::copy(O->y.begin(), O->y.end(), y);
 }
 
+// node locations after a relocation (arc patches move nodes after the
+// metrics are built, physicalElementData.C:186-224): only the code that reads
+// node locations (the limiter, vortex boundary values) sees them
+void orc_set_nodes(void* h, const double* x, const double* y) {
+    Oracle* O = (Oracle*)h;
+    std::copy(x, x + O->x.size(), O->x.begin());
+    std::copy(y, y + O->y.size(), O->y.begin());
+}
+
 void orc_connectivity(void* h, int* EToE, int* EToF, int* rot) {
     Oracle* O = (Oracle*)h;
     for (int k = 0; k < O->K; k++)

@@ -21,9 +21,11 @@ paraT3/paraT4 factors on the Laplacians' boundary data, which is set at the
 old time), BDF1/EXT1 on the first step and BDF2/EXT2 after.  The linear
 systems are solved directly (the reference's PETSc preonly + LU).
 
-Boundary conditions of the tutorial: U fixedValue (exact) on "inlet" and
-fixedGradient (exact n.grad U) on "outlet"; p zeroGradient on "inlet" and
-fixedValue (exact) on "outlet".  Exact solution (Pearson vortex):
+Boundary conditions of the Pearson tutorial: U fixedValue (exact) on "inlet"
+and fixedGradient (exact n.grad U) on "outlet"; p zeroGradient on "inlet"
+and fixedValue (exact) on "outlet" (PearsonCase).  CylinderCase restates the
+cylinder tutorial's (tutorials/DG/2D/cylinder/dgChorinFoam), whose solver
+differs only in its boundary data and the factors paraT1 / paraT4.  Exact solution (Pearson vortex):
 u = -sin(2 pi y) e^{-4 pi^2 nu t}, v = sin(2 pi x) e^{-4 pi^2 nu t},
 p = -cos(2 pi x) cos(2 pi y) e^{-8 pi^2 nu t}.
 """
@@ -64,13 +66,107 @@ def mass_matrix(M):
     return sp.block_diag([sp.csr_matrix(m) for m in M], format="csr")
 
 
-class ChorinOracle:
-    """The Pearson-vortex Chorin solver on a mesh whose boundary faces carry the
-    patches "inlet" and "outlet" (Mesh.patch / patch_names)."""
+class PearsonCase:
+    """tutorials/DG/2D/pearsonVortex: U fixedValue (exact) on "inlet", fixedGradient
+    (exact n.grad U) on "outlet"; p zeroGradient on "inlet", fixedValue (exact)
+    on "outlet"; the exact-solution Neumann term of pCorrectEquation.H:78-90."""
 
-    def __init__(self, mesh, order, cub, nu=0.01, dt=1e-3, tau_coef=20.0, t0=0.0):
+    def __init__(self, nu, dt):
+        self.nu, self.dt = nu, dt
+
+    def masks(self, names, patch, E):
+        inlet = (patch == names.index("inlet")) & (E < 0)
+        outlet = (patch == names.index("outlet")) & (E < 0)
+        if not np.all((E >= 0) | inlet | outlet):
+            raise ValueError("boundary faces outside inlet/outlet")
+        return inlet, outlet  # U fixedValue faces, the rest of the boundary
+
+    def initial(self, x, y, t0):
+        u, v, p = pearson_exact(x, y, t0, self.nu)
+        return np.stack([u, v]), p
+
+    def u_bnd(self, xb, yb, nstep, t):
+        u, v, _ = pearson_exact(xb, yb, t, self.nu)
+        return np.stack([u, v], 2)  # (K, 3, 2, Nfp)
+
+    def grad_bnd(self, xb, yb, nx, ny, t):
+        e1 = np.exp(-4 * PI * PI * self.nu * t)
+        gx = 2 * PI * ny * (-np.cos(2 * PI * yb)) * e1
+        gy = 2 * PI * nx * np.cos(2 * PI * xb) * e1
+        return np.stack([gx, gy], 2)
+
+    def p_bnd(self, xb, yb, t):
+        return pearson_exact(xb, yb, t, self.nu)[2]
+
+    def nbp_extra(self, xb, yb, nx, ny, ufix, nstep, t):
+        para_t = -self.nu * 4 * PI * PI * np.exp(-4 * PI * PI * self.nu * t)
+        return (-nx * np.sin(2 * PI * yb) + ny * np.sin(2 * PI * xb)) * para_t
+
+    def scales(self, nstep, t):
+        """(q3, q4): the factors of the p and U Laplacians' boundary data."""
+        return np.exp(-8 * PI * PI * self.nu * self.dt), np.exp(-4 * PI * PI * self.nu * self.dt)
+
+
+class CylinderCase:
+    """tutorials/DG/2D/cylinder (0/U, 0/p, setNonUniformInlet.H,
+    setBoundaryValues.H, setparaT.H, pCorrectEquation.H:78-85): U fixedValue
+    on inlet / channel / upcylinder / downcylinder (the inflow profile on the
+    inlet, zero elsewhere), zeroGradient on outlet; p zeroGradient except the
+    outlet's fixedValue 0.  The inlet values held before step n+1 are
+    profile(y) * sin(pi t_n / 8), and profile(y) alone before the first step;
+    paraT1 = pi/8 cos(pi t_n / 8) scales the inlet Neumann term and the p
+    Laplacian's data, paraT4 = sin(pi t_{n+1}/8) / paraT3 the U Laplacian's
+    (paraT3 = 1 before the first step, then sin(pi t_n / 8))."""
+
+    def __init__(self, nu, dt):
+        self.nu, self.dt = nu, dt
+
+    @staticmethod
+    def _profile(y):
+        return 6.0 * (y + 0.2) * (0.21 - y) / (0.41 * 0.41)
+
+    def masks(self, names, patch, E):
+        bnd = E < 0
+        fixed = np.zeros_like(bnd)
+        for n in ("inlet", "channel", "upcylinder", "downcylinder"):
+            fixed |= bnd & (patch == names.index(n))
+        self.inlet = bnd & (patch == names.index("inlet"))
+        outlet = bnd & (patch == names.index("outlet"))
+        if not np.all(~bnd | fixed | outlet):
+            raise ValueError("unexpected boundary patch")
+        return fixed, outlet
+
+    def initial(self, x, y, t0):
+        return np.zeros((2,) + x.shape), np.zeros_like(x)
+
+    def u_bnd(self, xb, yb, nstep, t):
+        fac = 1.0 if nstep == 0 else np.sin(PI * t / 8)
+        u = np.where(self.inlet[:, :, None], self._profile(yb) * fac, 0.0)
+        return np.stack([u, np.zeros_like(u)], 2)
+
+    def grad_bnd(self, xb, yb, nx, ny, t):
+        return np.zeros(xb.shape[:2] + (2,) + xb.shape[2:])
+
+    def p_bnd(self, xb, yb, t):
+        return np.zeros_like(xb)
+
+    def nbp_extra(self, xb, yb, nx, ny, ufix, nstep, t):
+        return np.where(self.inlet[:, :, None], -self._profile(yb) * (PI / 8 * np.cos(PI * t / 8)), 0.0)
+
+    def scales(self, nstep, t):
+        para_t3 = 1.0 if nstep == 0 else np.sin(PI * t / 8)
+        return PI / 8 * np.cos(PI * t / 8), np.sin(PI * (t + self.dt) / 8) / para_t3
+
+
+class ChorinOracle:
+    """The Chorin solver of dgChorinFoam on a mesh with boundary patches
+    (Mesh.patch / patch_names) for one case (default: the Pearson vortex,
+    patches "inlet" and "outlet")."""
+
+    def __init__(self, mesh, order, cub, nu=0.01, dt=1e-3, tau_coef=20.0, t0=0.0, case=None):
         O = Oracle(mesh, order, cub)
         self.O, self.N, self.nu, self.dt, self.tau = O, order, nu, dt, tau_coef
+        self.case = PearsonCase(nu, dt) if case is None else case
         self.K, self.Np, self.Nfp = O.K, O.Np, O.Nfp
         ops = O.operators()
         self.fci = ops["fci"][:, 0, :]  # (3, Nfp) owner face-node order
@@ -79,16 +175,12 @@ class ChorinOracle:
         self.nx, self.ny = g[:, :, 0], g[:, :, 1]
         E, _, _ = O.connectivity()
         self.EToE = E
-        names = list(mesh.patch_names)
-        patch = mesh.patch
-        self.inlet = (patch == names.index("inlet")) & (E < 0)
-        self.outlet = (patch == names.index("outlet")) & (E < 0)
-        if not np.all((E >= 0) | self.inlet | self.outlet):
-            raise ValueError("boundary faces outside inlet/outlet")
+        # U fixedValue faces (p natural there) and the other boundary faces
+        self.inlet, self.outlet = self.case.masks(list(mesh.patch_names), mesh.patch, E)
         # face-node coordinates per element face (K, 3, Nfp)
         self.xb = np.stack([self.x[:, self.fci[f]] for f in range(3)], 1)
         self.yb = np.stack([self.y[:, self.fci[f]] for f in range(3)], 1)
-        # boundary types: U Dirichlet on inlet, Neumann on outlet; p natural on inlet, Dirichlet on outlet
+        # boundary types: U Dirichlet / Neumann, p natural / Dirichlet
         self.btU = np.where(self.outlet, 1, 0).astype(np.int32)
         self.btP = np.where(self.inlet, 2, 0).astype(np.int32)
         self.M = O.mass()
@@ -100,30 +192,13 @@ class ChorinOracle:
         self.lu_p = spl.splu(self.Lp.tocsc())
         self._lu_h = {}
         # state (dgChorinFoam createFields.H / setNonUniformInlet.H)
-        u, v, p = pearson_exact(self.x, self.y, t0, nu)
-        self.U = np.stack([u, v])
+        self.U, self.p = self.case.initial(self.x, self.y, t0)
         self.Uold = self.U.copy()
-        self.p = p
         self.Nc = np.zeros_like(self.U)
         self.Nold = np.zeros_like(self.U)
         self.nbp = np.zeros((self.K, 3, self.Nfp))
         self.t = t0
         self.nstep = 0
-
-    # boundary data at time t (setBoundaryValues.H)
-    def _u_bnd(self, t):
-        u, v, _ = pearson_exact(self.xb, self.yb, t, self.nu)
-        return np.stack([u, v], 2)  # (K, 3, 2, Nfp)
-
-    def _gradU_bnd(self, t):
-        e1 = np.exp(-4 * PI * PI * self.nu * t)
-        nx, ny = self.nx[:, :, None], self.ny[:, :, None]
-        gx = 2 * PI * ny * (-np.cos(2 * PI * self.yb)) * e1
-        gy = 2 * PI * nx * np.cos(2 * PI * self.xb) * e1
-        return np.stack([gx, gy], 2)
-
-    def _p_bnd(self, t):
-        return pearson_exact(self.xb, self.yb, t, self.nu)[2]
 
     def _helmholtz(self, g0):
         if g0 not in self._lu_h:
@@ -135,43 +210,41 @@ class ChorinOracle:
         return np.einsum("kij,kj->ki", self.M, v)
 
     def step(self):
-        nu, dt, t = self.nu, self.dt, self.t
+        nu, dt, t, c = self.nu, self.dt, self.t, self.case
         if self.nstep == 0:
             g0, a0, a1, b0, b1 = 1.0, 1.0, 0.0, 1.0, 0.0
         else:
             g0, a0, a1, b0, b1 = 1.5, 2.0, -0.5, 2.0, -1.0
-        ub = self._u_bnd(t)
+        ub = c.u_bnd(self.xb, self.yb, self.nstep, t)
         # fixedGradient and interior faces: the boundary value is the interior trace
         trace = np.stack([self.U[:, :, self.fci[f]] for f in range(3)], 1).transpose(2, 1, 0, 3)  # (K,3,2,Nfp)
         ubnd = np.where(self.inlet[:, :, None, None], ub, trace)
         Nn = self.O.convection(self.U, ubnd)
         UT = (a0 * self.U + a1 * self.Uold - dt * (b0 * Nn + b1 * self.Nold)) / g0
-        # pressure Neumann data on the inlet faces (pEqnCorrect.H, pCorrectEquation.H:78-110)
+        # pressure Neumann data on the U fixedValue faces (pEqnCorrect.H, pCorrectEquation.H:78-110)
         cu = Nn + nu * self.O.curlcurl(self.U)
         cub = np.stack([cu[:, :, self.fci[f]] for f in range(3)], 2)  # (2, K, 3, Nfp)
-        paraT = -nu * 4 * PI * PI * np.exp(-4 * PI * PI * nu * t)
-        nbp_new = self.nx[:, :, None] * cub[0] + self.ny[:, :, None] * cub[1] + \
-            (-self.nx[:, :, None] * np.sin(2 * PI * self.yb) + self.ny[:, :, None] * np.sin(2 * PI * self.xb)) * paraT
+        nx, ny = self.nx[:, :, None], self.ny[:, :, None]
+        nbp_new = nx * cub[0] + ny * cub[1] + c.nbp_extra(self.xb, self.yb, nx, ny, self.inlet, self.nstep, t)
         nbp_new = np.where(self.inlet[:, :, None], nbp_new, 0.0)
         nbp_old = b0 * nbp_new + b1 * self.nbp
         self.nbp = nbp_new
         bN = self.O.face_mass_lift(self.inlet, nbp_old)
-        _, _, bLp = self.O.ipdg_blocks_bc(self.btP, gD=self._p_bnd(t), tau_coef=self.tau)
-        q3 = np.exp(-8 * PI * PI * nu * dt)
+        _, _, bLp = self.O.ipdg_blocks_bc(self.btP, gD=c.p_bnd(self.xb, self.yb, t), tau_coef=self.tau)
+        q3, q4 = c.scales(self.nstep, t)
         rhs = q3 * bLp + bN.ravel() + (g0 / dt) * self._mass(self.O.div_nodal(UT)).ravel()
         p = self.lu_p.solve(rhs).reshape(self.K, self.Np)
         # velocity correction
         UT = UT - (dt / g0) * self.O.grad_nodal(p)
         # viscous step
         tmp = g0 / (dt * nu)
-        q4 = np.exp(-4 * PI * PI * nu * dt)
         lu = self._helmholtz(g0)
-        gU = self._gradU_bnd(t)
+        gU = c.grad_bnd(self.xb, self.yb, self.nx[:, :, None], self.ny[:, :, None], t)
         Unew = np.empty_like(self.U)
-        for c in range(2):
-            _, _, bLU = self.O.ipdg_blocks_bc(self.btU, gD=ub[:, :, c], gN=gU[:, :, c], tau_coef=self.tau)
-            rhs = tmp * self._mass(UT[c]).ravel() - q4 * bLU
-            Unew[c] = lu.solve(rhs).reshape(self.K, self.Np)
+        for k in range(2):
+            _, _, bLU = self.O.ipdg_blocks_bc(self.btU, gD=ub[:, :, k], gN=gU[:, :, k], tau_coef=self.tau)
+            rhs = tmp * self._mass(UT[k]).ravel() - q4 * bLU
+            Unew[k] = lu.solve(rhs).reshape(self.K, self.Np)
         self.Uold, self.U = self.U, Unew
         self.Nold = Nn
         self.p = p

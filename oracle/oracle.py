@@ -30,6 +30,7 @@ def lib():
         L.orc_sizes.argtypes = [ctypes.c_void_p, _ip]
         L.orc_ref_operators.argtypes = [ctypes.c_void_p] + [_dp] * 11 + [_ip]
         L.orc_nodes.argtypes = [ctypes.c_void_p, _dp, _dp]
+        L.orc_set_nodes.argtypes = [ctypes.c_void_p, _dp, _dp]
         L.orc_connectivity.argtypes = [ctypes.c_void_p, _ip, _ip, _ip]
         L.orc_mass.argtypes = [ctypes.c_void_p, _dp]
         L.orc_euler_rhs.argtypes = [ctypes.c_void_p, _dp, _dp, ctypes.c_int, ctypes.c_double, _dp]
@@ -108,6 +109,13 @@ class Oracle:
         y = np.zeros(self.K * self.Np)
         self.L.orc_nodes(self.h, _d(x), _d(y))
         return x.reshape(self.K, self.Np), y.reshape(self.K, self.Np)
+
+    def set_nodes(self, x, y):
+        """Replace the node locations (not the metrics), as arc patches do."""
+        x = np.ascontiguousarray(x, np.float64).reshape(-1)
+        y = np.ascontiguousarray(y, np.float64).reshape(-1)
+        assert x.size == self.K * self.Np and y.size == x.size
+        self.L.orc_set_nodes(self.h, _d(x), _d(y))
 
     def connectivity(self):
         E = np.zeros((self.K, 3), np.int32)
@@ -246,6 +254,59 @@ class Oracle:
         rr = np.zeros(1)
         it = self.L.orc_pcg_bj(self.h, _d(diag), _d(off), _d(rhs), _d(x), rtol, maxit, _d(rr))
         return x, int(it), float(rr[0])
+
+
+def curved_nodes(O, mesh, curved_patches, project):
+    """Node locations after the relocation of the nodes next to curved patches
+    (physicalElementData.C:186-224 and triangleBaseFunction.C:421-466).
+
+    For each boundary face (k, f) on a patch named in ``curved_patches``: the
+    face's interior nodes go to ``project(x, y)`` (closest curve points; the
+    end nodes stay), and the shift d of the face nodes is carried into the
+    element as  x_i += blend_i * sum_j d_j l_j(vr_i)  with l_j the Lagrange
+    polynomials of the face's 1D nodes and
+      f = 0: vr = r, blend = -(r + s) / (1 - vr)
+      f = 1: vr = s, blend = (r + 1) / (1 - vr)
+      f = 2: vr = s, blend = -(r + s) / (1 - vr), d reversed,
+    nodes with |1 - vr| < 1e-7 untouched."""
+    ops = O.operators()
+    r, s, fci = ops["r"], ops["s"], ops["fci"][:, 0, :]
+    x, y = O.nodes()
+    x, y = x.copy(), y.copy()
+    E, _, _ = O.connectivity()
+    Nfp = fci.shape[1]
+    t = r[fci[0]]  # the 1D nodes: face 0 runs along r
+
+    def lagrange(z):
+        Lm = np.ones((z.size, Nfp))
+        for j in range(Nfp):
+            for m in range(Nfp):
+                if m != j:
+                    Lm[:, j] *= (z - t[m]) / (t[j] - t[m])
+        return Lm
+
+    names = list(mesh.patch_names)
+    for k in range(O.K):
+        for f in range(3):
+            if E[k, f] >= 0 or names[mesh.patch[k, f]] not in curved_patches:
+                continue
+            ids = fci[f]
+            sx, sy = x[k, ids].copy(), y[k, ids].copy()
+            px, py = project(sx[1:-1], sy[1:-1])
+            d = np.zeros((Nfp, 2))
+            d[1:-1, 0] = np.asarray(px) - sx[1:-1]
+            d[1:-1, 1] = np.asarray(py) - sy[1:-1]
+            if f == 2:
+                d = d[::-1]
+            vr = r if f == 0 else s
+            move = lagrange(vr) @ d
+            for i in range(O.Np):
+                if abs(1.0 - vr[i]) < 1e-7:
+                    continue
+                b = (r[i] + 1) / (1 - vr[i]) if f == 1 else -(r[i] + s[i]) / (1 - vr[i])
+                x[k, i] += b * move[i, 0]
+                y[k, i] += b * move[i, 1]
+    return x, y
 
 
 def lserk4_coeffs():

@@ -27,6 +27,11 @@ def golden_mesh(name):
         m.patch_names = tuple(str(x) for x in d["patch_names"])
     if "patch_first_face" in d:
         m.patch_first_face = d["patch_first_face"]
+    if "arc_names" in d:
+        from hopefoam_gb300.curved import ArcCurve
+
+        m.curves = {str(n): ArcCurve.from_code(str(c), tuple(u), name=str(n))
+                    for n, c, u in zip(d["arc_names"], d["arc_codes"], d["arc_u_range"])}
     return m
 
 

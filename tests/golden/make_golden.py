@@ -10,6 +10,10 @@
 * ``doublemach.npz``: the double-Mach-reflection tutorial mesh
   (tutorials/DG/2D/doubleMach/doubleMach.msh) with its patches and each
   patch's first face in file order.
+* ``cylinder.npz``: the cylinder tutorial's polyMesh
+  (tutorials/DG/2D/cylinder/constant/polyMesh) read by
+  hopefoam_gb300.polymesh, with its patches and the code and u range of its
+  two ``arc`` patches (the cylinder's halves).
 * ``vortex_kat.json``: the reference's published accuracy table for that case
   ("2017-07-24-OpenFOAM workshop.pptx", slide 18: Roe flux, SSP-RK2, exact
   fixed-value boundary, t = 2; mean absolute nodal error of rho and |rhoU|),
@@ -19,6 +23,7 @@ Usage: python tests/golden/make_golden.py [reference root]
 """
 import json
 import os
+import re
 import sys
 
 import numpy as np
@@ -27,6 +32,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, os.path.join(HERE, "..", ".."))
 
 from hopefoam_gb300.meshio import read_fluent_msh  # noqa: E402
+from hopefoam_gb300.polymesh import read_polymesh  # noqa: E402
 
 # slide 18: order -> (rho err h, h/2, h/4, rhoU err h, h/2, h/4)
 SLIDE18 = {
@@ -53,6 +59,18 @@ def main():
     m = read_fluent_msh(os.path.join(root, "HopeFOAM-0.1", "tutorials", "DG", "2D", "doubleMach", "doubleMach.msh"))
     np.savez_compressed(os.path.join(HERE, "doublemach.npz"), EToV=m.EToV, VXY=m.VXY, patch=m.patch,
                         patch_names=np.array(m.patch_names), patch_first_face=m.patch_first_face)
+    cyl = os.path.join(root, "HopeFOAM-0.1", "tutorials", "DG", "2D", "cylinder", "constant", "polyMesh")
+    m = read_polymesh(cyl)
+    text = open(os.path.join(cyl, "boundary")).read()
+    arcs = sorted(m.curves)
+    codes, ranges = [], []
+    for n in arcs:
+        body = re.search(r"\b%s\s*\{((?:[^{}]|#\{.*?#\})*)\}" % n, text, re.S).group(1)
+        codes.append(re.search(r"code\s*#\{(.*?)#\}", body, re.S).group(1).strip())
+        ranges.append(m.curves[n].u_range)
+    np.savez_compressed(os.path.join(HERE, "cylinder.npz"), EToV=m.EToV, VXY=m.VXY, patch=m.patch,
+                        patch_names=np.array(m.patch_names), arc_names=np.array(arcs), arc_codes=np.array(codes),
+                        arc_u_range=np.array(ranges))
     kat = {
         "source": "2017-07-24-OpenFOAM workshop.pptx, slide 18",
         "case": "isentropic vortex beta=5 centre (5,0) u_inf=1, gamma=1.4, Roe flux, SSP-RK2, exact fixed-value "

@@ -108,3 +108,44 @@ def test_pearson_vortex_convergence_on_gpu(gpu_lib):
         errs.append(e[0])
         g.close()
     assert np.all(np.log2(np.array(errs[:-1]) / np.array(errs[1:])) > 2.0)
+
+
+def test_cylinder_steps_against_oracle(gpu_lib):
+    """The cylinder tutorial as it stands (its polyMesh with the arc patches,
+    N = 3, nu = 0.001, dt = 2e-4) for ten steps against the oracle's
+    CylinderCase.
+
+    Tolerances: this case's pressure systems are far less well conditioned
+    than the Pearson meshes' (graded mesh around the cylinder, Dirichlet data
+    on the outlet only: condition number about 1e8) and their right-hand
+    sides are small against |A| |p| (ratio up to 2e6 after the first steps),
+    so an FP64 residual cannot fall much below 1e-10 of |b| -- the oracle's
+    direct LU solutions leave 1e-12 to 2e-10 -- and PCG stops at a relative
+    residual of 1e-10.  The condition number carries that into differences of
+    order 1e-8 in the state: 1e-8 relative after the first step, 2e-7 after
+    ten."""
+    from hopefoam_gb300.ins import ChorinSolver, CylinderFlow
+    from hopefoam_gb300.mesh import load_cubature
+    from oracle.ins_oracle import ChorinOracle, CylinderCase
+
+    m = golden_mesh("cylinder")
+    N, nu, dt = CylinderFlow.ORDER, CylinderFlow.NU, CylinderFlow.DT
+    uk, pk = CylinderFlow.kinds(m)
+    g = ChorinSolver(m, N, nu=nu, dt=dt, u_kind=uk, p_kind=pk)
+    cf = CylinderFlow(g)
+    g.set_state(*cf.initial_state())
+    o = ChorinOracle(m, N, load_cubature(3 * (N + 1)), nu=nu, dt=dt, case=CylinderCase(nu, dt))
+    t = 0.0
+    for i in range(10):
+        st = g.step(cf.bdata(t), rtol=1e-10)
+        o.step()
+        t += dt
+        if i == 0:
+            U1, p1 = g.get_state()
+            assert rel_l2(U1, o.U) < 1e-8 and rel_l2(p1, o.p) < 1e-8
+    Ug, pg = g.get_state()
+    eu, ep = rel_l2(Ug, o.U), rel_l2(pg, o.p)
+    print("cylinder, 10 Chorin steps, GPU vs oracle: U %.2e  p %.2e; PCG its p %d u %s" %
+          (eu, ep, st["iterations_p"], st["iterations_u"]))
+    assert np.abs(Ug).max() > 1e-4 and eu < 2e-7 and ep < 2e-7
+    g.close()

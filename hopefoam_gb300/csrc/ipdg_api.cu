@@ -179,11 +179,58 @@ int run_cg(dg_ctx* c, const PcgVecs& v, bool fp32, double tol2, int limit, const
     const int STALL = 256;
     double best_rr = -1.0;
     int best_it = 0;
+    // A batch of CHECK iterations is ~20 kernels per iteration; on small
+    // operators each is a few microseconds of device work, less than the
+    // host's cost of launching it.  From the second full batch on, a batch is
+    // one CUDA graph (captured once per solve, parity of the first iteration
+    // as its key; the kernels read all vectors and scalars from device memory,
+    // so the graph stays valid while this solve's buffers do).  If capture is
+    // not possible on this stream the batches are launched directly.
+    struct GraphGuard {
+        cudaGraphExec_t g = nullptr;
+        ~GraphGuard() {
+            if (g) cudaGraphExecDestroy(g);
+        }
+    } graph;
+    int gparity = -1;
+    bool use_graph = true;
+    auto launch_batch = [&](int it0, int count) -> cudaError_t {
+        if (use_graph && count == CHECK && checks > 0) {
+            const int par = it0 & 1;
+            if (graph.g && par != gparity) {
+                cudaGraphExecDestroy(graph.g);
+                graph.g = nullptr;
+            }
+            if (!graph.g) {
+                cudaGraph_t g = nullptr;
+                cudaError_t e = cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeRelaxed);
+                if (e == cudaSuccess) {
+                    for (int j = 0; j < CHECK && e == cudaSuccess; j++)
+                        e = launch_pcg_iteration(s->args, v, fp32, (it0 + j) & 1, pnet, pfa, c->stream);
+                    const cudaError_t e2 = cudaStreamEndCapture(c->stream, &g);
+                    if (e == cudaSuccess) e = e2;
+                }
+                if (e == cudaSuccess) e = cudaGraphInstantiate(&graph.g, g, 0);
+                if (g) cudaGraphDestroy(g);
+                if (e != cudaSuccess) {
+                    (void)cudaGetLastError();
+                    graph.g = nullptr;
+                    use_graph = false;
+                } else {
+                    gparity = par;
+                }
+            }
+            if (graph.g) return cudaGraphLaunch(graph.g, c->stream);
+        }
+        for (int j = 0; j < count; j++) {
+            const cudaError_t e = launch_pcg_iteration(s->args, v, fp32, (it0 + j) & 1, pnet, pfa, c->stream);
+            if (e != cudaSuccess) return e;
+        }
+        return cudaSuccess;
+    };
     while (h.it < limit) {
         const int batch = std::min(CHECK, limit - h.it);
-        for (int j = 0; j < batch; j++) {
-            IP_CUDA(c, launch_pcg_iteration(s->args, v, fp32, (h.it + j) & 1, pnet, pfa, c->stream));
-        }
+        IP_CUDA(c, launch_batch(h.it, batch));
         IP_CUDA(c, cudaMemcpyAsync(&h, s->d_S, sizeof(h), cudaMemcpyDeviceToHost, c->stream));
         IP_CUDA(c, cudaStreamSynchronize(c->stream));
         checks++;

@@ -125,6 +125,7 @@ struct SplitArgs {
     const float* b1;     // device image of B1 (canonical layout, hi then lo)
     const float* b2;     // device image of B2
     int* status;         // nonzero on a bounded-wait timeout
+    int qbulk;           // N <= 6: the state is 16-byte aligned, tiles arrive by bulk copy
 };
 
 constexpr uint32_t kWaitLimit = 1u << 22;
@@ -155,6 +156,7 @@ __global__ void __launch_bounds__(512, 1) euler_stage_split_kernel(SplitArgs sa)
     uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bar1 + 3);
     volatile int* fail_flag = reinterpret_cast<volatile int*>(bar1 + 4);  // set by thread 0, read after a barrier
     uint64_t* bfull = bar1 + 5;  // [NBUF] streamed operand buffer filled (N = 7)
+    uint64_t* bq = bar1 + 7;     // N <= 6: the FP64 tile copy has landed
 
     const EulerArgs& a = sa.e;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -168,6 +170,19 @@ __global__ void __launch_bounds__(512, 1) euler_stage_split_kernel(SplitArgs sa)
         umma::mbar_arrive_expect_tx(bfull + b, D::SZ_BC);
         umma::bulk_g2s(smem + D::OFF_BC + b * D::AL_BC, bsrc + (size_t)c * (D::SZ_BC / 4), D::SZ_BC, bfull + b);
         pend |= 1u << b;
+    };
+    // N <= 6: the next tile's FP64 state is copied into sQ64 by one bulk copy,
+    // issued as soon as the current tile's staging has read sQ64 (the
+    // epilogue reads the stage input from L2), so it lands during the face
+    // and volume phases
+    uint32_t pq = 0;
+    bool qpend = false;
+    auto issue_q = [&](int t) {
+        const int k0t = t * E;
+        const uint32_t bytes = (uint32_t)min(E, a.K - k0t) * 4u * (uint32_t)Np * 8u;
+        umma::mbar_arrive_expect_tx(bq, bytes);
+        umma::bulk_g2s(sQ64, a.qin + (size_t)k0t * 4 * Np, bytes, bq);
+        qpend = true;
     };
 
     // constant operands and zero padding, once per CTA
@@ -187,12 +202,16 @@ __global__ void __launch_bounds__(512, 1) euler_stage_split_kernel(SplitArgs sa)
         for (int b = 0; b < D::NBUF; b++) umma::mbar_init(bar2 + b, 1);
         if constexpr (D::STREAM)
             for (int b = 0; b < D::NBUF; b++) umma::mbar_init(bfull + b, 1);
+        else if (sa.qbulk)
+            umma::mbar_init(bq, 1);
         umma::fence_mbar_init();
         if constexpr (D::STREAM) {
             if ((int)blockIdx.x < ntiles) {
                 issue_chunk(0, 0);
                 issue_chunk(1, 1);
             }
+        } else {
+            if (sa.qbulk && (int)blockIdx.x < ntiles) issue_q(blockIdx.x);
         }
     }
     if (warp == 0) {
@@ -281,8 +300,15 @@ __global__ void __launch_bounds__(512, 1) euler_stage_split_kernel(SplitArgs sa)
             // N <= 6: FP64 tile copy, FP64 reference state copy; one FP64
             // subtraction and one conversion per value (at these orders the
             // kernel is issue-bound and the FP64 form takes fewer instructions)
-            for (int i = tid; i < ne * 4 * Np; i += blockDim.x) sQ64[i] = qtile[i];
-            __syncthreads();
+            if (sa.qbulk) {
+                const bool okq = umma::mbar_wait(bq, pq, kWaitLimit);
+                pq ^= 1;
+                if (okq) qpend = false;
+                if (__syncthreads_or(!okq)) { failed = true; break; }
+            } else {
+                for (int i = tid; i < ne * 4 * Np; i += blockDim.x) sQ64[i] = qtile[i];
+                __syncthreads();
+            }
             if (tid < D::ROWS) {
                 const int e = tid >> 2, v = tid & 3;
                 float qb = 1.f;
@@ -313,6 +339,10 @@ __global__ void __launch_bounds__(512, 1) euler_stage_split_kernel(SplitArgs sa)
         umma::fence_before_sync();
         __syncthreads();
         umma::fence_after_sync();
+        if constexpr (!D::STREAM) {
+            // sQ64 has been read: the next tile's copy may overwrite it
+            if (tid == 0 && sa.qbulk && tile + (int)gridDim.x < ntiles) issue_q(tile + gridDim.x);
+        }
         if (tid == 0) {
             // GEMM1: D1 = dQ (hi,lo) x Vg (hi,lo)^T, 3 passes per K=8 step
 #pragma unroll
@@ -582,15 +612,16 @@ __global__ void __launch_bounds__(512, 1) euler_stage_split_kernel(SplitArgs sa)
         constexpr int EPI = D::EPI;
         const bool first = (a.rka == 0.0);
         float resp[EPI];
-        double q0v[D::STREAM ? EPI : 1];  // N = 7: the stage input again (L2)
+        double q0v[EPI];  // N = 7, and N <= 6 with bulk tile copies: the stage input again (L2)
         {
             const size_t base = (size_t)k0 * 4 * Np;
             const bool need = a.mode == MODE_LSERK && !first;
+            const bool needq = a.mode != MODE_RHS && (D::STREAM || sa.qbulk);
 #pragma unroll
             for (int j = 0; j < EPI; j++) {
                 const int i = tid + j * D::THREADS;
                 resp[j] = (need && i < ne * 4 * Np) ? __ldg(sa.res32 + base + i) : 0.f;
-                if constexpr (D::STREAM) q0v[j] = (a.mode != MODE_RHS && i < ne * 4 * Np) ? __ldg(qtile + i) : 0.0;
+                q0v[j] = (needq && i < ne * 4 * Np) ? __ldg(qtile + i) : 0.0;
             }
         }
         // outstanding commits: the last NBUF chunks (one per buffer)
@@ -638,7 +669,7 @@ __global__ void __launch_bounds__(512, 1) euler_stage_split_kernel(SplitArgs sa)
                 const float R = sRS[i];
                 double q0;
                 if constexpr (D::STREAM) q0 = q0v[j];
-                else q0 = sQ64[i];
+                else q0 = sa.qbulk ? q0v[j] : sQ64[i];
                 const size_t idx = base + i;
                 const float dtf = a.dtk ? (float)(a.dt * a.dtk[k0 + i / (4 * Np)]) : dtf0;
                 switch (a.mode) {
@@ -661,6 +692,8 @@ __global__ void __launch_bounds__(512, 1) euler_stage_split_kernel(SplitArgs sa)
         if (tid == 0)
             for (int b = 0; b < D::NBUF; b++)
                 if ((pend >> b) & 1u) umma::mbar_wait(bfull + b, (pb >> b) & 1u, kWaitLimit);
+    } else {
+        if (tid == 0 && qpend) umma::mbar_wait(bq, pq, kWaitLimit);
     }
     umma::fence_before_sync();
     __syncthreads();
@@ -762,6 +795,7 @@ static cudaError_t launch_split_n(const EulerArgs& a, const SplitPlan& plan, cud
     sa.b1 = static_cast<const float*>(plan.d_ops);
     sa.b2 = static_cast<const float*>(plan.d_ops) + plan.b2_offset;
     sa.status = plan.d_status;
+    sa.qbulk = (reinterpret_cast<uintptr_t>(a.qin) & 15u) == 0;
     const int ntiles = (a.K + D::E - 1) / D::E;
     const int sms = (plan.sm_budget > 0 && plan.sm_budget < plan.sms) ? plan.sm_budget : plan.sms;
     const int want = sms * (plan.ctas_per_sm > 0 ? plan.ctas_per_sm : 1);

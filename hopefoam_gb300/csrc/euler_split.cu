@@ -92,6 +92,10 @@ struct SplitDims {
     // reference state FP32 (+ FP64 copy on the resident path), FP32 metrics
     static constexpr int OFF_GEO_IN_QB = ROWS * 4 + (STREAM ? 0 : ROWS * 8);
     static constexpr int SZ_QB = OFF_GEO_IN_QB + E * 4 * 4;
+    // the neighbour traces of the tile's faces, FP64 [3 E][Nfp][4], gathered
+    // by asynchronous copies while the tile is staged, where shared memory
+    // has room for them (N <= 5); otherwise the face phase loads them itself
+    static constexpr int SZ_NB_FULL = 3 * E * Nfp * 4 * 8;
     static constexpr int al(int x) { return (x + 1023) / 1024 * 1024; }
     static constexpr int OFF_B1 = 0;
     static constexpr int OFF_B2 = OFF_B1 + al(SZ_B1);
@@ -104,7 +108,10 @@ struct SplitDims {
     static constexpr int OFF_QF = OFF_AF + al(SZ_AF);
     static constexpr int OFF_Q64 = OFF_QF + al(SZ_QF);
     static constexpr int OFF_QB = OFF_Q64 + al(SZ_Q64);
-    static constexpr int OFF_BAR = OFF_QB + al(SZ_QB);
+    static constexpr int OFF_NB = OFF_QB + al(SZ_QB);
+    static constexpr bool GATHER = !STREAM && OFF_NB + al(SZ_NB_FULL) + 64 <= 232448;
+    static constexpr int SZ_NB = GATHER ? SZ_NB_FULL : 0;
+    static constexpr int OFF_BAR = OFF_NB + al(SZ_NB);
     static constexpr int SMEM = OFF_BAR + 64;
     static constexpr int RS_FLOATS = E * 4 * Np;      // epilogue staging (aliases chunk buffer 0)
     static constexpr int TILE_VALS = E * 4 * Np;
@@ -150,6 +157,7 @@ __global__ void __launch_bounds__(512, 1) euler_stage_split_kernel(SplitArgs sa)
     float* sQB = reinterpret_cast<float*>(smem + D::OFF_QB);                      // [ROWS]
     double* sQBd = reinterpret_cast<double*>(smem + D::OFF_QB + D::ROWS * 4);    // FP64 copy (resident path)
     float* sGeo = reinterpret_cast<float*>(smem + D::OFF_QB + D::OFF_GEO_IN_QB);  // [E][rx, sx, ry, sy]
+    double* sNB = reinterpret_cast<double*>(smem + D::OFF_NB);                   // gathered neighbour traces
     float* sRS = reinterpret_cast<float*>(smem + D::OFF_AC);  // after GEMM2 completed
     uint64_t* bar1 = reinterpret_cast<uint64_t*>(smem + D::OFF_BAR);
     uint64_t* bar2 = bar1 + 1;  // [NBUF]
@@ -177,6 +185,38 @@ __global__ void __launch_bounds__(512, 1) euler_stage_split_kernel(SplitArgs sa)
     // and volume phases
     uint32_t pq = 0;
     bool qpend = false;
+    // the neighbour side of every face node of a tile (interior: the neighbour
+    // element's node in its own face order, rotation applied; boundary: the
+    // slot's trace) into sNB by 8-byte asynchronous copies; cnv[j] holds the
+    // face link of this thread's task j (loaded by the caller, 0 = the first
+    // tile, whose links are loaded here)
+    constexpr int GT = (3 * E * Nfp + D::THREADS - 1) / D::THREADS;
+    int cn[GT];
+    auto gather = [&](int t0, const int* cnv) {
+        const int kt = t0 * E;
+        const int nt = 3 * min(E, a.K - kt) * Nfp;
+#pragma unroll
+        for (int j = 0; j < GT; j++) {
+            const int t = tid + j * D::THREADS;
+            if (t >= nt) break;
+            const int ef = t / Nfp, i = t - ef * Nfp;  // ef = 3 e + f
+            const int c = (t0 == (int)blockIdx.x) ? __ldg(a.conn + (size_t)kt * 3 + ef) : cnv[j];
+            const double* src;
+            int vstride;
+            if (c >= 0) {
+                const int nb = c >> 3, fn = c & 3, rot = (c >> 2) & 1;
+                const int jj = rot ? (N - i) : i;
+                src = a.qin + (size_t)nb * 4 * Np + (fn * N + jj) % NB;
+                vstride = Np;
+            } else {
+                src = a.btrace + (size_t)(-1 - c) * 4 * Nfp + i;
+                vstride = Nfp;
+            }
+            double* dst = sNB + (size_t)t * 4;
+#pragma unroll
+            for (int v = 0; v < 4; v++) umma::cp_async8(dst + v, src + v * vstride);
+        }
+    };
     auto issue_q = [&](int t) {
         const int k0t = t * E;
         const uint32_t bytes = (uint32_t)min(E, a.K - k0t) * 4u * (uint32_t)Np * 8u;
@@ -248,6 +288,19 @@ __global__ void __launch_bounds__(512, 1) euler_stage_split_kernel(SplitArgs sa)
         //      mean of the three vertex values, in FP32), FP32 metrics, FP32
         //      deltas, TF32 hi/lo of the deltas.
         const double* qtile = a.qin + (size_t)k0 * 4 * Np;
+        if constexpr (D::GATHER) {
+            // this tile's neighbour traces were requested during the previous
+            // tile (the first tile's here); read the next tile's face links now,
+            // so that its requests go out without a dependent load
+            if (tile == (int)blockIdx.x) gather(tile, cn);
+            const int nt = tile + (int)gridDim.x;
+#pragma unroll
+            for (int j = 0; j < GT; j++) {
+                const int t = tid + j * D::THREADS;
+                cn[j] = (nt < ntiles && t < 3 * min(E, a.K - nt * E) * Nfp) ? __ldg(a.conn + (size_t)nt * E * 3 + t / Nfp)
+                                                                          : 0;
+            }
+        }
         if constexpr (D::STREAM) {
             // N = 7: no FP64 tile copy (the values stay in registers across the
             // reference-state barrier; the vertex values come from L2), and the
@@ -335,6 +388,7 @@ __global__ void __launch_bounds__(512, 1) euler_stage_split_kernel(SplitArgs sa)
                 sA1[off + LO_A1 / 4] = lo;
             }
         }
+        if constexpr (D::GATHER) umma::cp_async_wait_all();  // this thread's neighbour-trace copies
         umma::fence_async_smem();
         umma::fence_before_sync();
         __syncthreads();
@@ -393,22 +447,28 @@ __global__ void __launch_bounds__(512, 1) euler_stage_split_kernel(SplitArgs sa)
 #pragma unroll
                         for (int v = 0; v < 4; v++) own[v] = sQF[e * 4 * Np + v * Np + pos];
                     }
-                    const int c = __ldg(a.conn + (size_t)k * 3 + f);
-                    if (c >= 0) {
-                        const int nb = c >> 3, fn = c & 3, rot = (c >> 2) & 1;
-                        const int jj = rot ? (N - i) : i;
-                        const int npos = (fn * N + jj) % NB;
-                        const double* qn = a.qin + (size_t)nb * 4 * Np + npos;
+                    if constexpr (D::GATHER) {
+                        const double* nv = sNB + (size_t)((3 * e + f) * Nfp + i) * 4;
 #pragma unroll
-                        for (int v = 0; v < 4; v++)
-                            nbr[v] = D::STREAM ? f64s::minus_f32(__ldg(qn + v * Np), qbv[v])
-                                               : (float)(__ldg(qn + v * Np) - qbd[v]);
+                        for (int v = 0; v < 4; v++) nbr[v] = (float)(nv[v] - qbd[v]);
                     } else {
-                        const double* bt = a.btrace + (size_t)(-1 - c) * 4 * Nfp + i;
+                        const int c = __ldg(a.conn + (size_t)k * 3 + f);
+                        if (c >= 0) {
+                            const int nb = c >> 3, fn = c & 3, rot = (c >> 2) & 1;
+                            const int jj = rot ? (N - i) : i;
+                            const int npos = (fn * N + jj) % NB;
+                            const double* qn = a.qin + (size_t)nb * 4 * Np + npos;
 #pragma unroll
-                        for (int v = 0; v < 4; v++)
-                            nbr[v] = D::STREAM ? f64s::minus_f32(__ldg(bt + v * Nfp), qbv[v])
-                                               : (float)(__ldg(bt + v * Nfp) - qbd[v]);
+                            for (int v = 0; v < 4; v++)
+                                nbr[v] = D::STREAM ? f64s::minus_f32(__ldg(qn + v * Np), qbv[v])
+                                                   : (float)(__ldg(qn + v * Np) - qbd[v]);
+                        } else {
+                            const double* bt = a.btrace + (size_t)(-1 - c) * 4 * Nfp + i;
+#pragma unroll
+                            for (int v = 0; v < 4; v++)
+                                nbr[v] = D::STREAM ? f64s::minus_f32(__ldg(bt + v * Nfp), qbv[v])
+                                                   : (float)(__ldg(bt + v * Nfp) - qbd[v]);
+                        }
                     }
                 }
                 // interpolate both traces to Gauss point i (shuffles within the group)
@@ -474,6 +534,11 @@ __global__ void __launch_bounds__(512, 1) euler_stage_split_kernel(SplitArgs sa)
         ph1 ^= 1;
         if (__syncthreads_or(!ok)) { failed = true; break; }
         umma::fence_after_sync();
+        if constexpr (D::GATHER) {
+            // every warp has read sNB: request the next tile's traces, which land
+            // during the volume phase
+            if (tile + (int)gridDim.x < ntiles) gather(tile + gridDim.x, cn);
+        }
         for (int ch = 0; ch < D::NCH; ch++) {
             const int buf = (D::NBUF == 2) ? (ch & 1) : 0;
             float* sAC = reinterpret_cast<float*>(smem + D::OFF_AC + buf * STRIDE_AC);
@@ -694,6 +759,7 @@ __global__ void __launch_bounds__(512, 1) euler_stage_split_kernel(SplitArgs sa)
                 if ((pend >> b) & 1u) umma::mbar_wait(bfull + b, (pb >> b) & 1u, kWaitLimit);
     } else {
         if (tid == 0 && qpend) umma::mbar_wait(bq, pq, kWaitLimit);
+        if constexpr (D::GATHER) umma::cp_async_wait_all();  // after a timeout: copies still in flight
     }
     umma::fence_before_sync();
     __syncthreads();

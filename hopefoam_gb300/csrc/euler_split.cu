@@ -72,6 +72,8 @@ struct SplitDims {
     // hi + lo operand, which holds them exactly.
     static constexpr bool STREAM = (N == 7);
     static constexpr int NBUF = (N <= 5 || STREAM) ? 2 : 1;  // chunk buffers
+    // N <= 5: the two buffers are filled in one pass (two chunks per thread)
+    static constexpr bool PAIR = NBUF == 2 && !STREAM;
     // face phase: one (element, face) per segment of SW lanes, SPW segments per
     // warp.  Power-of-two groups (SW = 8) where packing would not save a pass
     // over the tile's 96 faces, packed segments (SW = Nfq) otherwise: at N = 7
@@ -539,137 +541,179 @@ __global__ void __launch_bounds__(512, 1) euler_stage_split_kernel(SplitArgs sa)
             // during the volume phase
             if (tile + (int)gridDim.x < ntiles) gather(tile + gridDim.x, cn);
         }
-        for (int ch = 0; ch < D::NCH; ch++) {
-            const int buf = (D::NBUF == 2) ? (ch & 1) : 0;
-            float* sAC = reinterpret_cast<float*>(smem + D::OFF_AC + buf * STRIDE_AC);
-            // this thread's row (e, v) at 4 cubature points of the chunk
-            float x[4];
-            umma::tmem_ld4(tD1 + ((uint32_t)(32 * qd) << 16) + ch * CH + sub * 4, x);
-            umma::tmem_ld_wait();
-            float fr[1][4], fs[1][4];
-            {
-                // gather the 4 variables at point (sub*4 + my_v) from the element's 4 lanes
-                float got[4], dq[4];
+        // volume flux of this thread's row (e, v) at 4 cubature points of chunk
+        // ch; x = the row's values there (tensor memory)
+        auto vol_flux = [&](const float* x, int ch, float* fr, float* fs) {
+            // gather the 4 variables at point (sub*4 + my_v) from the element's 4 lanes
+            float got[4], dq[4];
 #pragma unroll
-                for (int s = 0; s < 4; s++) {
-                    const float send = pick4(x, (my_v + s) & 3);
-                    got[s] = __shfl_sync(0xffffffffu, send, (lane & ~3) | ((my_v - s) & 3));
-                }
-                // variable t arrived in round s = (my_v - t) mod 4 (selects, no local memory)
-#pragma unroll
-                for (int t = 0; t < 4; t++) dq[t] = pick4(got, (my_v - t) & 3);
-                const int g = ch * CH + sub * 4 + my_v;
-                if (g < Ng && my_e < ne) {
-                    const DeltaPrim d = delta_prim(gamma, bref, dq);
-                    float fx[4], fy[4];
-                    flux_delta(bref, dq, d, fx, fy);
-#pragma unroll
-                    for (int v = 0; v < 4; v++) {
-                        fr[0][v] = rx * fx[v] + ry * fy[v];
-                        fs[0][v] = sx * fx[v] + sy * fy[v];
-                    }
-                } else {
-#pragma unroll
-                    for (int v = 0; v < 4; v++) fr[0][v] = fs[0][v] = 0.f;
-                }
+            for (int s = 0; s < 4; s++) {
+                const float send = pick4(x, (my_v + s) & 3);
+                got[s] = __shfl_sync(0xffffffffu, send, (lane & ~3) | ((my_v - s) & 3));
             }
-            if constexpr (D::NBUF >= 2) {
-                // buffer reuse: thread 0 confirmed, before the previous chunk's
-                // barrier, that the MMAs which last read this buffer are complete
-                if (ch >= D::NBUF) ph2 ^= 1u << buf;
-            } else {
-                // one buffer: the previous chunk's MMAs are issued after its barrier,
-                // so every thread waits for them here
-                if (ch >= D::NBUF) {
-                    ok = umma::mbar_wait(bar2 + buf, (ph2 >> buf) & 1u, kWaitLimit);
-                    ph2 ^= 1u << buf;
-                    if (__syncthreads_or(!ok)) { failed = true; break; }
-                }
-            }
-            {
-                // (4-way bank conflicts: a rotation of the variable order per element
-                // pair removes them but costs more issue slots than it saves)
-                const int gl = sub * 4 + my_v;
+            // variable t arrived in round s = (my_v - t) mod 4 (selects, no local memory)
+#pragma unroll
+            for (int t = 0; t < 4; t++) dq[t] = pick4(got, (my_v - t) & 3);
+            const int g = ch * CH + sub * 4 + my_v;
+            if (g < Ng && my_e < ne) {
+                const DeltaPrim d = delta_prim(gamma, bref, dq);
+                float fx[4], fy[4];
+                flux_delta(bref, dq, d, fx, fy);
 #pragma unroll
                 for (int v = 0; v < 4; v++) {
-                    const int r = 4 * my_e + v;
-                    float hi, lo;
-                    umma::split_tf32(fr[0][v], hi, lo);
-                    uint32_t off = umma::kmajor_offset(r, gl, KC) >> 2;
-                    sAC[off] = hi;
-                    sAC[off + LO_AC / 4] = lo;
-                    umma::split_tf32(fs[0][v], hi, lo);
-                    off = umma::kmajor_offset(r, CH + gl, KC) >> 2;
-                    sAC[off] = hi;
-                    sAC[off + LO_AC / 4] = lo;
+                    fr[v] = rx * fx[v] + ry * fy[v];
+                    fs[v] = sx * fx[v] + sy * fy[v];
                 }
-            }
-            umma::fence_async_smem();
-            umma::fence_before_sync();
-            if constexpr (D::NBUF >= 2) {
-                // chunk ch + 1 reuses the buffer of chunk ch + 1 - NBUF <= ch - 1, whose
-                // MMAs were issued before this point
-                if (tid == 0 && ch + 1 < D::NCH && ch + 1 >= D::NBUF) {
-                    const int nb = (ch + 1) % D::NBUF;
-                    if (!umma::mbar_wait(bar2 + nb, (ph2 >> nb) & 1u, kWaitLimit)) *fail_flag = 1;
-                    else if constexpr (D::STREAM) issue_chunk(ch + 1, nb);  // its buffer is free now
-                }
-            }
-            if constexpr (D::STREAM) {
-                // this chunk's [Sr|Ss] slice has landed (issued one chunk earlier)
-                if (tid == 0) {
-                    if (!umma::mbar_wait(bfull + buf, (pb >> buf) & 1u, kWaitLimit)) {
-                        *fail_flag = 1;
-                    } else {
-                        pend &= ~(1u << buf);
-                        pb ^= 1u << buf;
-                    }
-                }
-            }
-            __syncthreads();
-            umma::fence_after_sync();
-            if (*fail_flag) { failed = true; break; }
-            if (tid == 0) {
-                constexpr uint32_t sboA = (KC / 4) * 128, sboB = (KP2 / 4) * 128;
-                const uint32_t aC = aAC + buf * STRIDE_AC;
+            } else {
 #pragma unroll
-                for (int s = 0; s < KC / 8; s++) {
-                    const uint64_t ah = umma::smem_desc(aC + s * 256, 128, sboA);
-                    const uint64_t al = umma::smem_desc(aC + LO_AC + s * 256, 128, sboA);
-                    uint64_t bh, bl;
-                    if constexpr (D::STREAM) {
-                        // the streamed slice has the chunk's own K layout [Sr 16 | Ss 16]
-                        const uint32_t bC = aBC + buf * D::AL_BC;
-                        bh = umma::smem_desc(bC + s * 256, 128, sboA);
-                        bl = umma::smem_desc(bC + LO_BC + s * 256, 128, sboA);
-                    } else {
-                        // chunk K step s: Fr part (s < 2) at B2 k = ch*CH + 8s, Fs part at NG + ch*CH + 8(s-2)
-                        const int kb = (s < CH / 8) ? (ch * CH + 8 * s) : (NG + ch * CH + 8 * (s - CH / 8));
-                        bh = umma::smem_desc(aB2 + kb * 32, 128, sboB);
-                        bl = umma::smem_desc(aB2 + LO_B2 + kb * 32, 128, sboB);
-                    }
-                    const uint32_t acc = (ch > 0 || s > 0) ? 1u : 0u;
-                    umma::mma_tf32(tD2, ah, bh, idesc2, acc);
+                for (int v = 0; v < 4; v++) fr[v] = fs[v] = 0.f;
+            }
+        };
+        // TF32 hi/lo of the chunk's flux rows into chunk buffer buf
+        // (4-way bank conflicts: a rotation of the variable order per element
+        // pair removes them but costs more issue slots than it saves)
+        auto store_chunk = [&](int buf, const float* fr, const float* fs) {
+            float* sAC = reinterpret_cast<float*>(smem + D::OFF_AC + buf * STRIDE_AC);
+            const int gl = sub * 4 + my_v;
+#pragma unroll
+            for (int v = 0; v < 4; v++) {
+                const int r = 4 * my_e + v;
+                float hi, lo;
+                umma::split_tf32(fr[v], hi, lo);
+                uint32_t off = umma::kmajor_offset(r, gl, KC) >> 2;
+                sAC[off] = hi;
+                sAC[off + LO_AC / 4] = lo;
+                umma::split_tf32(fs[v], hi, lo);
+                off = umma::kmajor_offset(r, CH + gl, KC) >> 2;
+                sAC[off] = hi;
+                sAC[off + LO_AC / 4] = lo;
+            }
+        };
+        // thread 0: GEMM2's MMAs for chunk ch in buffer buf (with the lift part
+        // after the last chunk), completion on bar2[buf]
+        auto issue_mma = [&](int ch, int buf) {
+            constexpr uint32_t sboA = (KC / 4) * 128, sboB = (KP2 / 4) * 128;
+            const uint32_t aC = aAC + buf * STRIDE_AC;
+#pragma unroll
+            for (int s = 0; s < KC / 8; s++) {
+                const uint64_t ah = umma::smem_desc(aC + s * 256, 128, sboA);
+                const uint64_t al = umma::smem_desc(aC + LO_AC + s * 256, 128, sboA);
+                uint64_t bh, bl;
+                if constexpr (D::STREAM) {
+                    // the streamed slice has the chunk's own K layout [Sr 16 | Ss 16]
+                    const uint32_t bC = aBC + buf * D::AL_BC;
+                    bh = umma::smem_desc(bC + s * 256, 128, sboA);
+                    bl = umma::smem_desc(bC + LO_BC + s * 256, 128, sboA);
+                } else {
+                    // chunk K step s: Fr part (s < 2) at B2 k = ch*CH + 8s, Fs part at NG + ch*CH + 8(s-2)
+                    const int kb = (s < CH / 8) ? (ch * CH + 8 * s) : (NG + ch * CH + 8 * (s - CH / 8));
+                    bh = umma::smem_desc(aB2 + kb * 32, 128, sboB);
+                    bl = umma::smem_desc(aB2 + LO_B2 + kb * 32, 128, sboB);
+                }
+                const uint32_t acc = (ch > 0 || s > 0) ? 1u : 0u;
+                umma::mma_tf32(tD2, ah, bh, idesc2, acc);
+                umma::mma_tf32(tD2, al, bh, idesc2, 1);
+                umma::mma_tf32(tD2, ah, bl, idesc2, 1);
+            }
+            if (ch == D::NCH - 1) {
+                constexpr uint32_t sboF = (NF / 4) * 128;
+#pragma unroll
+                for (int s = 0; s < NF / 8; s++) {
+                    // lift part: B2 k = 2 NG + 8s (resident image), or k = 8s of the lift-only image
+                    const int kb = D::STREAM ? 8 * s : 2 * NG + 8 * s;
+                    constexpr uint32_t sbo = D::STREAM ? sboF : sboB;
+                    const uint64_t ah = umma::smem_desc(aAF + s * 256, 128, sboF);
+                    const uint64_t al = umma::smem_desc(aAF + LO_AF + s * 256, 128, sboF);
+                    const uint64_t bh = umma::smem_desc(aB2 + kb * 32, 128, sbo);
+                    const uint64_t bl = umma::smem_desc(aB2 + LO_B2 + kb * 32, 128, sbo);
+                    umma::mma_tf32(tD2, ah, bh, idesc2, 1);
                     umma::mma_tf32(tD2, al, bh, idesc2, 1);
                     umma::mma_tf32(tD2, ah, bl, idesc2, 1);
                 }
-                if (ch == D::NCH - 1) {
-                    constexpr uint32_t sboF = (NF / 4) * 128;
-#pragma unroll
-                    for (int s = 0; s < NF / 8; s++) {
-                        // lift part: B2 k = 2 NG + 8s (resident image), or k = 8s of the lift-only image
-                        const int kb = D::STREAM ? 8 * s : 2 * NG + 8 * s;
-                        constexpr uint32_t sbo = D::STREAM ? sboF : sboB;
-                        const uint64_t ah = umma::smem_desc(aAF + s * 256, 128, sboF);
-                        const uint64_t al = umma::smem_desc(aAF + LO_AF + s * 256, 128, sboF);
-                        const uint64_t bh = umma::smem_desc(aB2 + kb * 32, 128, sbo);
-                        const uint64_t bl = umma::smem_desc(aB2 + LO_B2 + kb * 32, 128, sbo);
-                        umma::mma_tf32(tD2, ah, bh, idesc2, 1);
-                        umma::mma_tf32(tD2, al, bh, idesc2, 1);
-                        umma::mma_tf32(tD2, ah, bl, idesc2, 1);
+            }
+            umma::commit(bar2 + buf);
+        };
+        if constexpr (D::PAIR) {
+            // two chunks per pass, one per buffer: each thread carries two
+            // independent flux evaluations and a pass has one barrier; before
+            // rewriting the buffers every thread waits for the previous pass's
+            // MMAs (issued one pass earlier, normally complete by then)
+            int prev_n = 0;
+            for (int ch0 = 0; ch0 < D::NCH; ch0 += 2) {
+                const int n = (D::NCH - ch0 >= 2) ? 2 : 1;
+                float x0[4], x1[4];
+                umma::tmem_ld4(tD1 + ((uint32_t)(32 * qd) << 16) + ch0 * CH + sub * 4, x0);
+                if (n == 2) umma::tmem_ld4(tD1 + ((uint32_t)(32 * qd) << 16) + (ch0 + 1) * CH + sub * 4, x1);
+                umma::tmem_ld_wait();
+                float fr0[4], fs0[4], fr1[4], fs1[4];
+                vol_flux(x0, ch0, fr0, fs0);
+                if (n == 2) vol_flux(x1, ch0 + 1, fr1, fs1);
+                bool okw = true;
+                for (int b = 0; b < prev_n; b++) {
+                    okw = umma::mbar_wait(bar2 + b, (ph2 >> b) & 1u, kWaitLimit) && okw;
+                    ph2 ^= 1u << b;
+                }
+                store_chunk(0, fr0, fs0);
+                if (n == 2) store_chunk(1, fr1, fs1);
+                umma::fence_async_smem();
+                umma::fence_before_sync();
+                if (__syncthreads_or(!okw)) { failed = true; break; }
+                umma::fence_after_sync();
+                if (tid == 0) {
+                    issue_mma(ch0, 0);
+                    if (n == 2) issue_mma(ch0 + 1, 1);
+                }
+                prev_n = n;
+            }
+        } else {
+            for (int ch = 0; ch < D::NCH; ch++) {
+                const int buf = (D::NBUF == 2) ? (ch & 1) : 0;
+                // this thread's row (e, v) at 4 cubature points of the chunk
+                float x[4];
+                umma::tmem_ld4(tD1 + ((uint32_t)(32 * qd) << 16) + ch * CH + sub * 4, x);
+                umma::tmem_ld_wait();
+                float fr[4], fs[4];
+                vol_flux(x, ch, fr, fs);
+                if constexpr (D::NBUF >= 2) {
+                    // buffer reuse: thread 0 confirmed, before the previous chunk's
+                    // barrier, that the MMAs which last read this buffer are complete
+                    if (ch >= D::NBUF) ph2 ^= 1u << buf;
+                } else {
+                    // one buffer: the previous chunk's MMAs are issued after its barrier,
+                    // so every thread waits for them here
+                    if (ch >= D::NBUF) {
+                        ok = umma::mbar_wait(bar2 + buf, (ph2 >> buf) & 1u, kWaitLimit);
+                        ph2 ^= 1u << buf;
+                        if (__syncthreads_or(!ok)) { failed = true; break; }
                     }
                 }
-                umma::commit(bar2 + buf);
+                store_chunk(buf, fr, fs);
+                umma::fence_async_smem();
+                umma::fence_before_sync();
+                if constexpr (D::NBUF >= 2) {
+                    // chunk ch + 1 reuses the buffer of chunk ch + 1 - NBUF <= ch - 1, whose
+                    // MMAs were issued before this point
+                    if (tid == 0 && ch + 1 < D::NCH && ch + 1 >= D::NBUF) {
+                        const int nb = (ch + 1) % D::NBUF;
+                        if (!umma::mbar_wait(bar2 + nb, (ph2 >> nb) & 1u, kWaitLimit)) *fail_flag = 1;
+                        else if constexpr (D::STREAM) issue_chunk(ch + 1, nb);  // its buffer is free now
+                    }
+                }
+                if constexpr (D::STREAM) {
+                    // this chunk's [Sr|Ss] slice has landed (issued one chunk earlier)
+                    if (tid == 0) {
+                        if (!umma::mbar_wait(bfull + buf, (pb >> buf) & 1u, kWaitLimit)) {
+                            *fail_flag = 1;
+                        } else {
+                            pend &= ~(1u << buf);
+                            pb ^= 1u << buf;
+                        }
+                    }
+                }
+                __syncthreads();
+                umma::fence_after_sync();
+                if (*fail_flag) { failed = true; break; }
+                if (tid == 0) issue_mma(ch, buf);
             }
         }
         if (failed) break;
@@ -689,15 +733,28 @@ __global__ void __launch_bounds__(512, 1) euler_stage_split_kernel(SplitArgs sa)
                 q0v[j] = (needq && i < ne * 4 * Np) ? __ldg(qtile + i) : 0.0;
             }
         }
-        // outstanding commits: the last NBUF chunks (one per buffer)
+        // outstanding commits
+        if constexpr (D::PAIR) {
+            // the last pass's buffers
+            constexpr int last_n = (D::NCH % 2 == 0) ? 2 : 1;
+            bool okw = true;
 #pragma unroll
-        for (int b = 0; b < D::NBUF; b++) {
-            const int chb = D::NCH - D::NBUF + b;
-            if (chb < 0) continue;
-            const int buf = (D::NBUF == 2) ? (chb & 1) : 0;
-            ok = umma::mbar_wait(bar2 + buf, (ph2 >> buf) & 1u, kWaitLimit);
-            ph2 ^= 1u << buf;
-            if (__syncthreads_or(!ok)) { failed = true; break; }
+            for (int b = 0; b < last_n; b++) {
+                okw = umma::mbar_wait(bar2 + b, (ph2 >> b) & 1u, kWaitLimit) && okw;
+                ph2 ^= 1u << b;
+            }
+            if (__syncthreads_or(!okw)) { failed = true; break; }
+        } else {
+            // the last NBUF chunks (one per buffer)
+#pragma unroll
+            for (int b = 0; b < D::NBUF; b++) {
+                const int chb = D::NCH - D::NBUF + b;
+                if (chb < 0) continue;
+                const int buf = (D::NBUF == 2) ? (chb & 1) : 0;
+                ok = umma::mbar_wait(bar2 + buf, (ph2 >> buf) & 1u, kWaitLimit);
+                ph2 ^= 1u << buf;
+                if (__syncthreads_or(!ok)) { failed = true; break; }
+            }
         }
         if (failed) break;
         umma::fence_after_sync();

@@ -781,7 +781,26 @@ __global__ void __launch_bounds__(512, 1) euler_stage_split_kernel(SplitArgs sa)
         }
         umma::fence_before_sync();
         __syncthreads();
-        {
+        if (a.mode == MODE_LSERK && !a.dtk) {
+            // the LSERK stage with one time step for all elements: straight-line
+            // loads and stores (no early exit, no per-value mode dispatch)
+            const size_t base = (size_t)k0 * 4 * Np;
+            const float rka = (float)a.rka, dtf0 = (float)a.dt, rkb = (float)a.rkb;
+            const int nv = ne * 4 * Np;
+#pragma unroll
+            for (int j = 0; j < EPI; j++) {
+                const int i = tid + j * D::THREADS;
+                if (i < nv) {
+                    const float R = sRS[i];
+                    double q0;
+                    if constexpr (D::STREAM) q0 = q0v[j];
+                    else q0 = sa.qbulk ? q0v[j] : sQ64[i];
+                    const float r = first ? dtf0 * R : fmaf(rka, resp[j], dtf0 * R);
+                    sa.res32_out[base + i] = r;
+                    a.qout[base + i] = q0 + (double)(rkb * r);
+                }
+            }
+        } else {
             const size_t base = (size_t)k0 * 4 * Np;
             const float rka = (float)a.rka, dtf0 = (float)a.dt, rkb = (float)a.rkb;
 #pragma unroll

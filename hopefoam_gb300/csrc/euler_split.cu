@@ -32,8 +32,8 @@
 // lane segments, one per (element, face) (gather, Gauss interpolation and
 // wave-speed max by shuffles) while GEMM1 runs -> per chunk of 16 cubature
 // points: tensor memory ->
-// registers, the 4 variables of a point exchanged by warp shuffles within
-// the element's 4 lanes -> FP32 delta flux -> TF32 split into a
+// registers, the 4 variables of a point exchanged by a two-stage butterfly of
+// warp shuffles within the element's 4 lanes -> FP32 delta flux -> TF32 split into a
 // double-buffered chunk operand -> GEMM2 MMAs for that K chunk -> epilogue:
 // tensor memory -> shared -> coalesced LSERK update.  At N = 7 the volume
 // operator is streamed from L2 per chunk and the tile is not copied to shared
@@ -138,10 +138,6 @@ struct SplitArgs {
 };
 
 constexpr uint32_t kWaitLimit = 1u << 22;
-
-__device__ __forceinline__ float pick4(const float* x, int i) {
-    return i == 0 ? x[0] : (i == 1 ? x[1] : (i == 2 ? x[2] : x[3]));
-}
 
 template <int N>
 __global__ void __launch_bounds__(512, 1) euler_stage_split_kernel(SplitArgs sa) {
@@ -544,16 +540,29 @@ __global__ void __launch_bounds__(512, 1) euler_stage_split_kernel(SplitArgs sa)
         // volume flux of this thread's row (e, v) at 4 cubature points of chunk
         // ch; x = the row's values there (tensor memory)
         auto vol_flux = [&](const float* x, int ch, float* fr, float* fs) {
-            // gather the 4 variables at point (sub*4 + my_v) from the element's 4 lanes
-            float got[4], dq[4];
-#pragma unroll
-            for (int s = 0; s < 4; s++) {
-                const float send = pick4(x, (my_v + s) & 3);
-                got[s] = __shfl_sync(0xffffffffu, send, (lane & ~3) | ((my_v - s) & 3));
+            // the 4 variables at point (sub*4 + my_v): a 4 x 4 transpose across the
+            // element's 4 lanes in two butterfly stages (lane bit 1, then bit 0);
+            // in a stage a lane sends the two slots whose index bit differs from
+            // its own lane bit and receives the partner's into them
+            float dq[4] = {x[0], x[1], x[2], x[3]};
+            {
+                const bool b = (my_v & 2) != 0;
+                const float r0 = __shfl_xor_sync(0xffffffffu, b ? dq[0] : dq[2], 2);
+                const float r1 = __shfl_xor_sync(0xffffffffu, b ? dq[1] : dq[3], 2);
+                dq[0] = b ? r0 : dq[0];
+                dq[1] = b ? r1 : dq[1];
+                dq[2] = b ? dq[2] : r0;
+                dq[3] = b ? dq[3] : r1;
             }
-            // variable t arrived in round s = (my_v - t) mod 4 (selects, no local memory)
-#pragma unroll
-            for (int t = 0; t < 4; t++) dq[t] = pick4(got, (my_v - t) & 3);
+            {
+                const bool b = (my_v & 1) != 0;
+                const float r0 = __shfl_xor_sync(0xffffffffu, b ? dq[0] : dq[1], 1);
+                const float r1 = __shfl_xor_sync(0xffffffffu, b ? dq[2] : dq[3], 1);
+                dq[0] = b ? r0 : dq[0];
+                dq[2] = b ? r1 : dq[2];
+                dq[1] = b ? dq[1] : r0;
+                dq[3] = b ? dq[3] : r1;
+            }
             const int g = ch * CH + sub * 4 + my_v;
             if (g < Ng && my_e < ne) {
                 const DeltaPrim d = delta_prim(gamma, bref, dq);

@@ -139,6 +139,12 @@ struct SplitArgs {
 
 constexpr uint32_t kWaitLimit = 1u << 22;
 
+// GEMM2's A rows (and so its result rows in tensor memory) in the order
+// r = 32 (e / 8) + 8 v + e % 8: the 8 elements a warp stores for one variable
+// then sit in 8 different 16-byte slots of a core matrix, so the operand
+// stores are free of bank conflicts.  GEMM1 keeps r = 4 e + v.
+__device__ __forceinline__ int g2row(int e, int v) { return ((e >> 3) << 5) | (v << 3) | (e & 7); }
+
 template <int N>
 __global__ void __launch_bounds__(512, 1) euler_stage_split_kernel(SplitArgs sa) {
     using D = SplitDims<N>;
@@ -514,7 +520,7 @@ __global__ void __launch_bounds__(512, 1) euler_stage_split_kernel(SplitArgs sa)
                     for (int v = 0; v < 4; v++) {
                         float hi, lo;
                         umma::split_tf32(-fsc * F[v], hi, lo);
-                        const uint32_t off = umma::kmajor_offset(4 * e + v, f * Nfq + i, NF) >> 2;
+                        const uint32_t off = umma::kmajor_offset(g2row(e, v), f * Nfq + i, NF) >> 2;
                         sAF[off] = hi;
                         sAF[off + LO_AF / 4] = lo;
                     }
@@ -586,7 +592,7 @@ __global__ void __launch_bounds__(512, 1) euler_stage_split_kernel(SplitArgs sa)
             const int gl = sub * 4 + my_v;
 #pragma unroll
             for (int v = 0; v < 4; v++) {
-                const int r = 4 * my_e + v;
+                const int r = g2row(my_e, v);
                 float hi, lo;
                 umma::split_tf32(fr[v], hi, lo);
                 uint32_t off = umma::kmajor_offset(r, gl, KC) >> 2;
@@ -776,6 +782,7 @@ __global__ void __launch_bounds__(512, 1) euler_stage_split_kernel(SplitArgs sa)
         }
         // ---- (D) epilogue: R (tensor memory) -> staging -> coalesced stage update
         {
+            const int e2 = 8 * qd + (lane & 7), v2 = lane >> 3;  // this lane's GEMM2 row (g2row)
 #pragma unroll
             for (int col = sub * 8; col < NP2; col += 32) {
                 float val[8];
@@ -784,7 +791,8 @@ __global__ void __launch_bounds__(512, 1) euler_stage_split_kernel(SplitArgs sa)
 #pragma unroll
                 for (int j = 0; j < 8; j++) {
                     const int p = col + j;
-                    if (p < Np && my_e < ne) sRS[(4 * my_e + my_v) * Np + p] = val[j];
+                    // tensor-memory lane (within the quarter) 8 v + e % 8
+                    if (p < Np && e2 < ne) sRS[(4 * e2 + v2) * Np + p] = val[j];
                 }
             }
         }

@@ -454,7 +454,7 @@ __global__ void __launch_bounds__(512, 1) euler_stage_split_kernel(SplitArgs sa)
                     if constexpr (D::GATHER) {
                         const double* nv = sNB + (size_t)((3 * e + f) * Nfp + i) * 4;
 #pragma unroll
-                        for (int v = 0; v < 4; v++) nbr[v] = (float)(nv[v] - qbd[v]);
+                        for (int v = 0; v < 4; v++) nbr[v] = f64s::minus_f32(nv[v], qbv[v]);
                     } else {
                         const int c = __ldg(a.conn + (size_t)k * 3 + f);
                         if (c >= 0) {

@@ -81,6 +81,12 @@ struct SplitDims {
     static constexpr bool PACKED = (N == 7) || (N <= 3);
     static constexpr int SW = PACKED ? Nfq : 8;
     static constexpr int SPW = 32 / SW;
+    // N = 4..6: two Gauss points per lane, FW = ceil(Nfq / 2) lanes per face,
+    // all 3 E faces of a tile in one pass
+    static constexpr int FP = (!STREAM && !PACKED) ? 2 : 1;
+    static constexpr int FW = (Nfq + 1) / 2;
+    static constexpr int FPW = 32 / FW;
+    static_assert(FP == 1 || (16 * FPW >= 3 * E && 2 * FW >= Nfp), "one-pass face groups");
     // shared-memory layout (bytes, operand buffers 1024-aligned)
     static constexpr int SZ_B1 = 2 * NG * KP1 * 4;    // Vg hi/lo
     static constexpr int SZ_BC = 2 * NP2 * KC * 4;    // one streamed [Sr|Ss] chunk hi/lo
@@ -415,9 +421,128 @@ __global__ void __launch_bounds__(512, 1) euler_stage_split_kernel(SplitArgs sa)
             }
             umma::commit(bar1);
         }
-        // ---- (B) face fluxes while GEMM1 runs: one (element, face) per segment of
-        //      SW lanes, lane i = face node i (gather) and face Gauss point i (flux)
-        {
+        // ---- (B) face fluxes while GEMM1 runs
+        if constexpr (D::FP == 2) {
+            // N = 4..6: one (element, face) per segment of FW = ceil(Nfq / 2) lanes,
+            // lane li = face nodes li, li + FW (gather) and Gauss points li, li + FW
+            // (flux): every face of the tile in one pass, two independent flux
+            // evaluations per lane, and each shuffled node value serves both points
+            constexpr int FW = D::FW, FPW = D::FPW;
+            const int seg = lane / FW, li = lane - seg * FW;  // lanes with seg >= FPW idle
+            const int sbase = (seg < FPW ? seg : 0) * FW;
+            const int G = warp * FPW + seg;
+            const bool gok = seg < FPW && G < 3 * E;
+            const int Gc = gok ? G : warp * FPW;
+            const int e = Gc / 3, f = Gc - 3 * e;
+            const bool valid = gok && e < ne;
+            const int k = k0 + (valid ? e : 0);
+            float qbv[4];
+            double qbd[4];
+#pragma unroll
+            for (int v = 0; v < 4; v++) {
+                qbv[v] = sQB[4 * (valid ? e : 0) + v];
+                qbd[v] = sQBd[4 * (valid ? e : 0) + v];
+            }
+            float own[2][4], nbr[2][4];
+#pragma unroll
+            for (int sl = 0; sl < 2; sl++) {
+                const int i = li + sl * FW;
+#pragma unroll
+                for (int v = 0; v < 4; v++) own[sl][v] = nbr[sl][v] = 0.f;
+                if (valid && i < Nfp) {
+                    const int pos = (f * N + i) % NB;
+#pragma unroll
+                    for (int v = 0; v < 4; v++) own[sl][v] = sQF[e * 4 * Np + v * Np + pos];
+                    if constexpr (D::GATHER) {
+                        const double* nv = sNB + (size_t)((3 * e + f) * Nfp + i) * 4;
+#pragma unroll
+                        for (int v = 0; v < 4; v++) nbr[sl][v] = f64s::minus_f32(nv[v], qbv[v]);
+                    } else {
+                        const int c = __ldg(a.conn + (size_t)k * 3 + f);
+                        const double* src;
+                        int vs;
+                        if (c >= 0) {
+                            const int nb = c >> 3, fn = c & 3, rot = (c >> 2) & 1;
+                            const int jj = rot ? (N - i) : i;
+                            src = a.qin + (size_t)nb * 4 * Np + (fn * N + jj) % NB;
+                            vs = Np;
+                        } else {
+                            src = a.btrace + (size_t)(-1 - c) * 4 * Nfp + i;
+                            vs = Nfp;
+                        }
+#pragma unroll
+                        for (int v = 0; v < 4; v++) nbr[sl][v] = (float)(__ldg(src + v * vs) - qbd[v]);
+                    }
+                }
+            }
+            // both traces at this lane's two Gauss points
+            float dm[2][4], dp[2][4];
+            int gi[2];
+#pragma unroll
+            for (int sl = 0; sl < 2; sl++) {
+                gi[sl] = (li + sl * FW < Nfq) ? li + sl * FW : 0;
+#pragma unroll
+                for (int v = 0; v < 4; v++) dm[sl][v] = dp[sl][v] = 0.f;
+            }
+#pragma unroll
+            for (int jn = 0; jn < Nfp; jn++) {
+                const int src = sbase + jn % FW;
+                const float w0 = (float)__ldg(a.ops.If + gi[0] * Nfp + jn);
+                const float w1 = (float)__ldg(a.ops.If + gi[1] * Nfp + jn);
+#pragma unroll
+                for (int v = 0; v < 4; v++) {
+                    const float om = __shfl_sync(0xffffffffu, own[jn / FW][v], src);
+                    const float op = __shfl_sync(0xffffffffu, nbr[jn / FW][v], src);
+                    dm[0][v] = fmaf(w0, om, dm[0][v]);
+                    dp[0][v] = fmaf(w0, op, dp[0][v]);
+                    dm[1][v] = fmaf(w1, om, dm[1][v]);
+                    dp[1][v] = fmaf(w1, op, dp[1][v]);
+                }
+            }
+            const float* gk = sGeo + 4 * (valid ? e : 0);
+            float nx, ny, fsc;
+            face_normal_f(f, gk[0], gk[1], gk[2], gk[3], nx, ny, fsc);
+            const RefState b = make_ref(gamma, qbv);
+            DeltaPrim pm[2], pp[2];
+#pragma unroll
+            for (int sl = 0; sl < 2; sl++) {
+                pm[sl] = delta_prim(gamma, b, dm[sl]);
+                pp[sl] = delta_prim(gamma, b, dp[sl]);
+            }
+            float F[2][4];
+            if (a.flux == 1) {
+#pragma unroll
+                for (int sl = 0; sl < 2; sl++) roe_flux_delta(gamma, nx, ny, b, dm[sl], pm[sl], dp[sl], pp[sl], F[sl]);
+            } else {
+                float lam = 0.f;
+#pragma unroll
+                for (int sl = 0; sl < 2; sl++)
+                    if (li + sl * FW < Nfq)
+                        lam = fmaxf(lam, fmaxf(wave_speed_delta(gamma, nx, ny, b, pm[sl]),
+                                               wave_speed_delta(gamma, nx, ny, b, pp[sl])));
+                float m = lam;
+#pragma unroll
+                for (int j = 0; j < FW; j++) m = fmaxf(m, __shfl_sync(0xffffffffu, lam, sbase + j));
+#pragma unroll
+                for (int sl = 0; sl < 2; sl++) lf_flux_delta(nx, ny, m, b, dm[sl], pm[sl], dp[sl], pp[sl], F[sl]);
+            }
+#pragma unroll
+            for (int sl = 0; sl < 2; sl++) {
+                const int g = li + sl * FW;
+                if (valid && g < Nfq) {
+#pragma unroll
+                    for (int v = 0; v < 4; v++) {
+                        float hi, lo;
+                        umma::split_tf32(-fsc * F[sl][v], hi, lo);
+                        const uint32_t off = umma::kmajor_offset(g2row(e, v), f * Nfq + g, NF) >> 2;
+                        sAF[off] = hi;
+                        sAF[off + LO_AF / 4] = lo;
+                    }
+                }
+            }
+        } else {
+            // one (element, face) per segment of SW lanes, lane i = face node i
+            // (gather) and face Gauss point i (flux)
             constexpr int SW = D::SW, SPW = D::SPW;
             const int seg = lane / SW, i = lane - seg * SW;  // lanes with seg >= SPW idle
             const int sbase = (seg < SPW ? seg : 0) * SW;     // first lane of this segment

@@ -76,10 +76,11 @@ def test_split_lserk4_step(gpu_lib, N):
     assert err < TOL_STEP_SPLIT
 
 
-@pytest.mark.parametrize("N", [3, 7])
+@pytest.mark.parametrize("N", [3, 4, 5, 6, 7])
 def test_split_tail_tile_and_boundary(gpu_lib, N):
     """K not a multiple of the 32-element tile, fixed-value boundary faces
-    (N = 7: the streamed-operator variant of the kernel)."""
+    (N <= 5: neighbour traces gathered into shared memory; N = 4..6: two Gauss
+    points per face lane; N = 7: the streamed-operator variant of the kernel)."""
     from hopefoam_gb300 import _lib as L
     from hopefoam_gb300 import euler
 

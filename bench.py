@@ -54,7 +54,7 @@ def alg_bytes_per_elem_stage(order, split=True):
 
 # dram__bytes_read.sum + dram__bytes_write.sum of one stage launch at this
 # workload (profiles/euler_stage_split_N5.md)
-SPLIT_STAGE_TRAFFIC_N5 = 223.4e6
+SPLIT_STAGE_TRAFFIC_N5 = 222.0e6
 
 
 class ClockSampler:
@@ -310,8 +310,8 @@ def main():
                      "traffic": SPLIT_STAGE_TRAFFIC_N5 if (prec_name == "split" and order == 5 and args.nx == 256)
                      else None, "peak_kind": peak_kind, "bytes_per_elem_stage": bpe,
                      "kernel": "euler_stage_%s" % prec_name,
-                     "note": "the stage is bound by FP64 conversions and SIMT issue, not HBM "
-                             "(profiles/euler_stage_split_N5.md)"},
+                     "note": "the stage is latency-bound at 16 warps per SM (issue 36 %, FP64 pipe 39 %), "
+                             "not HBM-bound (profiles/euler_stage_split_N5.md)"},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": n * 8, "d2h_bytes_per_step": n * 8},
         "gpu_launches": launches,
         "clocks": ck,

@@ -81,9 +81,9 @@ struct SplitDims {
     static constexpr bool PACKED = (N == 7) || (N <= 3);
     static constexpr int SW = PACKED ? Nfq : 8;
     static constexpr int SPW = 32 / SW;
-    // N = 4..6: two Gauss points per lane, FW = ceil(Nfq / 2) lanes per face,
+    // N = 4..7: two Gauss points per lane, FW = ceil(Nfq / 2) lanes per face,
     // all 3 E faces of a tile in one pass
-    static constexpr int FP = (!STREAM && !PACKED) ? 2 : 1;
+    static constexpr int FP = (STREAM || !PACKED) ? 2 : 1;
     static constexpr int FW = (Nfq + 1) / 2;
     static constexpr int FPW = 32 / FW;
     static_assert(FP == 1 || (16 * FPW >= 3 * E && 2 * FW >= Nfp), "one-pass face groups");
@@ -423,7 +423,7 @@ __global__ void __launch_bounds__(512, 1) euler_stage_split_kernel(SplitArgs sa)
         }
         // ---- (B) face fluxes while GEMM1 runs
         if constexpr (D::FP == 2) {
-            // N = 4..6: one (element, face) per segment of FW = ceil(Nfq / 2) lanes,
+            // N = 4..7: one (element, face) per segment of FW = ceil(Nfq / 2) lanes,
             // lane li = face nodes li, li + FW (gather) and Gauss points li, li + FW
             // (flux): every face of the tile in one pass, two independent flux
             // evaluations per lane, and each shuffled node value serves both points
@@ -441,7 +441,7 @@ __global__ void __launch_bounds__(512, 1) euler_stage_split_kernel(SplitArgs sa)
 #pragma unroll
             for (int v = 0; v < 4; v++) {
                 qbv[v] = sQB[4 * (valid ? e : 0) + v];
-                qbd[v] = sQBd[4 * (valid ? e : 0) + v];
+                if constexpr (!D::STREAM) qbd[v] = sQBd[4 * (valid ? e : 0) + v];
             }
             float own[2][4], nbr[2][4];
 #pragma unroll
@@ -451,8 +451,17 @@ __global__ void __launch_bounds__(512, 1) euler_stage_split_kernel(SplitArgs sa)
                 for (int v = 0; v < 4; v++) own[sl][v] = nbr[sl][v] = 0.f;
                 if (valid && i < Nfp) {
                     const int pos = (f * N + i) % NB;
+                    if constexpr (D::STREAM) {
 #pragma unroll
-                    for (int v = 0; v < 4; v++) own[sl][v] = sQF[e * 4 * Np + v * Np + pos];
+                        for (int v = 0; v < 4; v++) {
+                            // the FP32 delta, read back from the TF32 operand: hi + lo is exact
+                            const uint32_t off = umma::kmajor_offset(4 * e + v, pos, KP1) >> 2;
+                            own[sl][v] = sA1[off] + sA1[off + LO_A1 / 4];
+                        }
+                    } else {
+#pragma unroll
+                        for (int v = 0; v < 4; v++) own[sl][v] = sQF[e * 4 * Np + v * Np + pos];
+                    }
                     if constexpr (D::GATHER) {
                         const double* nv = sNB + (size_t)((3 * e + f) * Nfp + i) * 4;
 #pragma unroll
@@ -471,7 +480,9 @@ __global__ void __launch_bounds__(512, 1) euler_stage_split_kernel(SplitArgs sa)
                             vs = Nfp;
                         }
 #pragma unroll
-                        for (int v = 0; v < 4; v++) nbr[sl][v] = (float)(__ldg(src + v * vs) - qbd[v]);
+                        for (int v = 0; v < 4; v++)
+                            nbr[sl][v] = D::STREAM ? f64s::minus_f32(__ldg(src + v * vs), qbv[v])
+                                                   : (float)(__ldg(src + v * vs) - qbd[v]);
                     }
                 }
             }

@@ -266,19 +266,23 @@ __global__ void lim_reconstruct_kernel(LimArgs a, double* __restrict__ q) {
 }
 
 // boundary field of reflective slots: the mirrored interior trace
-// (reflectiveDgPatchField.C:79-111: (I - 2 n n^T) on the vector)
+// (reflectiveDgPatchField.C:79-111: (I - 2 n n^T) on the vector); of
+// zero-gradient slots: the interior trace itself (dgPatchField's
+// patchInternalField), both re-evaluated where the reference corrects its
+// boundary conditions
 __global__ void lim_reflect_kernel(LimArgs a, const double* __restrict__ q, double* __restrict__ bnd) {
     const int idx = blockIdx.x * blockDim.x + threadIdx.x;
     if (idx >= a.nb * a.Nfp) return;
     const int sl = idx / a.Nfp, j = idx - sl * a.Nfp;
-    if (a.kind[sl] != 1) return;
+    const int kd = a.kind[sl];
+    if (kd != 1 && kd != 3) return;
     const int k = a.sk[sl], f = a.sf[sl];
     const double* g = a.geo + 4 * (size_t)k;
     double nx, ny, fsc;
     face_normal(f, g[0], g[1], g[2], g[3], nx, ny, fsc);
     const int p = (f * a.N + j) % (3 * a.N);
     const double* qk = q + (size_t)k * 4 * a.Np;
-    const double ru = qk[a.Np + p], rv = qk[2 * a.Np + p], m = nx * ru + ny * rv;
+    const double ru = qk[a.Np + p], rv = qk[2 * a.Np + p], m = kd == 1 ? nx * ru + ny * rv : 0.0;
     double* b = bnd + (size_t)sl * 4 * a.Nfp;
     b[j] = qk[p];
     b[a.Nfp + j] = ru - 2 * nx * m;
@@ -438,7 +442,7 @@ int dg_set_node_locations(dg_ctx* c, const double* x, const double* y) {
 int dg_set_boundary_kinds(dg_ctx* c, const int* kind, const int* gref) {
     if (!c || (c->nb > 0 && !kind)) return DG_ERR_ARG;
     for (int i = 0; i < c->nb; i++) {
-        if (kind[i] < 0 || kind[i] > 2) return lfail(c, DG_ERR_ARG, "boundary kind must be 0, 1 or 2");
+        if (kind[i] < 0 || kind[i] > 3) return lfail(c, DG_ERR_ARG, "boundary kind must be 0, 1, 2 or 3");
         if (gref && (gref[i] < 0 || gref[i] >= c->nb)) return lfail(c, DG_ERR_ARG, "gref out of range");
     }
     limiter_teardown(c);

@@ -141,7 +141,8 @@ class EulerContext:
         _check(self.h, self.lib.dg_set_node_locations(self.h, L.dptr(x), L.dptr(y)))
 
     def set_boundary_kinds(self, kinds, gref=None):
-        """Per boundary slot: 0 fixed value, 1 reflective wall, 2 other."""
+        """Per boundary slot: 0 fixed value, 1 reflective wall, 2 other (value as
+        set), 3 zero gradient (the interior trace)."""
         k = np.ascontiguousarray(kinds, np.int32)
         g = None if gref is None else np.ascontiguousarray(gref, np.int32)
         self._keep += [k] + ([g] if g is not None else [])

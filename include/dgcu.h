@@ -294,11 +294,14 @@ int dg_euler_rhs_noalloc(dg_ctx* ctx, const double* q_dev, double* rhs_dev, int 
  * dg_set_boundary_kinds: per boundary slot 0 fixed value, 1 reflective wall
  * (the boundary value mirrors the interior trace's momentum,
  * reflectiveDgPatchField.C:79-111; the limiter's ghost cell removes the normal
- * momentum), 2 other (the limiter's ghost cell copies the owner); gref (may be
+ * momentum), 2 other (the boundary value stays as set; the limiter's ghost
+ * cell copies the owner), 3 zero gradient (the boundary value is the interior
+ * trace, re-evaluated with the walls'; the ghost cell copies the owner); gref (may be
  * NULL = itself) per slot: the slot whose first boundary value a fixed-value
  * ghost cell takes (the reference uses the first value of the slot's patch).
  * dg_limit: the limiter on the current state with the current boundary traces.
- * dg_reflect_boundary_traces: the reflective slots' traces from the state.
+ * dg_reflect_boundary_traces: the reflective and zero-gradient slots' traces
+ * from the state.
  * dg_limited_ssprk2_step: one step (stage, walls, limiter, stage, walls,
  * average with the boundary values, limiter, walls); bdata [nb][4][Nfp] holds
  * this step's values of the fixed-value slots (setBoundaryValues.H).

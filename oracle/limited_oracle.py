@@ -42,6 +42,8 @@ class LimitedSSPOracle:
         r[:, 2] = t[:, 2] - 2 * ny * m
         B = B.copy()
         B[self.walls] = r[self.walls]
+        zg = self.kinds == 3  # zero gradient: the interior trace
+        B[zg] = t[zg]
         return B
 
     def rhs(self, q, B):

@@ -234,7 +234,8 @@ class Oracle:
     def limiter(self, q, bnd, kind, gref=None):
         """The reference's slope limiter applied to q ([4][K][Np]); bnd per
         boundary slot [nb][4][Nfp], kind per slot (0 fixed value, 1
-        reflective, 2 other), gref per slot (default: itself)."""
+        reflective, 2 other, 3 zero gradient: ghost cells as 2), gref per slot
+        (default: itself)."""
         q = np.array(q, np.float64, copy=True).reshape(-1)
         bnd = np.ascontiguousarray(bnd, np.float64)
         kind = np.ascontiguousarray(kind, np.int32)

@@ -157,3 +157,32 @@ def test_oracle_limiter_properties():
     for v in range(4):
         coef, res, *_ = np.linalg.lstsq(A, out[v].T, rcond=None)
         assert np.abs(A @ coef - out[v].T).max() < 1e-11
+
+
+def test_oracle_boundary_kinds_in_limited_step():
+    """Zero-gradient slots take the interior trace, walls the trace with the
+    normal momentum reversed, fixed-value and other slots keep their values
+    (the limited step's boundary bookkeeping, oracle/limited_oracle.py)."""
+    from hopefoam_gb300 import euler
+    from hopefoam_gb300.mesh import box_square, load_cubature
+    from oracle.limited_oracle import LimitedSSPOracle
+
+    N = 2
+    m = box_square(4, 3, 1.0, 0.8)
+    kk, ff = euler.boundary_faces(m)
+    kinds = (np.arange(len(kk)) % 4).astype(np.int32)
+    lo = LimitedSSPOracle(m, N, load_cubature(9), kinds)
+    x, y = lo.O.nodes()
+    rho = 1 + 0.2 * np.sin(3 * x)
+    q = np.stack([rho, 0.3 * rho + 0.1 * y, -0.2 * rho, 2.5 + 0.1 * x])
+    B0 = np.random.default_rng(1).standard_normal((len(kk), 4, N + 1))
+    B = lo.reflect(q, B0)
+    t = lo.traces(q)
+    assert np.array_equal(B[kinds == 3], t[kinds == 3])
+    assert np.array_equal(B[kinds == 0], B0[kinds == 0]) and np.array_equal(B[kinds == 2], B0[kinds == 2])
+    w = kinds == 1
+    nx, ny = lo.nx[w][:, None], lo.ny[w][:, None]
+    # the wall value's normal momentum is the trace's, negated; tangential and scalars kept
+    assert np.allclose(nx * B[w, 1] + ny * B[w, 2], -(nx * t[w, 1] + ny * t[w, 2]), atol=1e-14)
+    assert np.allclose(-ny * B[w, 1] + nx * B[w, 2], -ny * t[w, 1] + nx * t[w, 2], atol=1e-14)
+    assert np.array_equal(B[w, 0], t[w, 0]) and np.array_equal(B[w, 3], t[w, 3])

@@ -32,7 +32,7 @@ def _box_case(N, seed=0):
     fn = euler.face_nodes(N)
     rng = np.random.default_rng(seed)
     bnd = np.stack([q[:, k, fn[f]] for k, f in zip(kk, ff)]) * (1 + 0.05 * rng.standard_normal((nb, 4, N + 1)))
-    kinds = rng.integers(0, 3, nb).astype(np.int32)
+    kinds = rng.integers(0, 4, nb).astype(np.int32)
     gref = rng.integers(0, nb, nb).astype(np.int32)
     return m, ctx, orc, q, bnd, kinds, gref
 
@@ -52,12 +52,14 @@ def test_limiter_against_oracle(gpu_lib, N):
     ctx.close()
 
 
-def test_reflective_traces(gpu_lib):
+@pytest.mark.parametrize("kind", [1, 3])
+def test_reflective_traces(gpu_lib, kind):
+    """Walls (mirrored momentum) and zero-gradient slots (the interior trace)."""
     from hopefoam_gb300 import euler
 
     N = 3
     m, ctx, orc, q, bnd, kinds, gref = _box_case(N)
-    kinds[:] = 1
+    kinds[:] = kind
     ctx.upload(q)
     ctx.set_boundary_traces(bnd)
     ctx.set_boundary_kinds(kinds)
@@ -105,4 +107,40 @@ def test_double_mach_steps_against_oracle(gpu_lib):
     print("double Mach, 10 limited SSP-RK2 steps: GPU vs oracle %.2e; rho range %.3f..%.3f" %
           (err, qg[0].min(), qg[0].max()))
     assert np.isfinite(qg).all() and err < 1e-10
+    ctx.close()
+
+
+def test_double_mach_zero_gradient_outflow(gpu_lib):
+    """The double-Mach case with its right-hand patch as a zero-gradient
+    outflow (the interior trace, re-evaluated with the walls) for ten steps."""
+    from hopefoam_gb300 import _lib as L
+    from hopefoam_gb300 import euler
+    from hopefoam_gb300.mesh import load_cubature
+    from hopefoam_gb300.shock import DoubleMach
+    from oracle.limited_oracle import LimitedSSPOracle
+
+    N, dt = 3, 1e-5
+    m = golden_mesh("doublemach")
+    dm = DoubleMach(m, N)
+    kk, ff = euler.boundary_faces(m)
+    xmid = 0.5 * (m.VXY[kk, ff, 0] + m.VXY[kk, (ff + 1) % 3, 0])
+    kinds = dm.kinds.copy()
+    kinds[(xmid > xmid.max() - 1e-9) & (kinds == 0)] = 3
+    assert (kinds == 3).sum() > 0
+    ctx = euler.EulerContext(m, N)
+    q0 = dm.initial_state()
+    ctx.upload(q0)
+    ctx.set_boundary_traces(dm.bdata(0.0))
+    ctx.set_boundary_kinds(kinds, dm.gref)
+    lo = LimitedSSPOracle(m, N, load_cubature(3 * (N + 1)), kinds, dm.gref)
+    qo = q0.copy()
+    t = 0.0
+    for _ in range(10):
+        b = dm.bdata(t)
+        ctx.limited_ssprk2(dt, b, flux=L.DG_FLUX_ROE, precision=L.DG_PREC_FP64)
+        qo = lo.step(qo, dt, b)
+        t += dt
+    err = rel_l2(ctx.download(), qo)
+    print("double Mach with a zero-gradient outflow, 10 steps: GPU vs oracle %.2e" % err)
+    assert err < 1e-10
     ctx.close()

@@ -126,7 +126,9 @@ int lserk_stage(dg_ctx* c, double dt, int stage, int flux, int precision) {
     a.qout = c->d_q[c->cur ^ 1];
     a.rka = kRk4a[stage];
     a.rkb = kRk4b[stage];
-    int rc = run_stage(c, a, precision);
+    int rc = refresh_boundary_traces(c, a.qin);
+    if (rc) return rc;
+    rc = run_stage(c, a, precision);
     if (rc) return rc;
     c->cur ^= 1;
     return DG_OK;
@@ -368,6 +370,8 @@ int dg_lserk4_step(dg_ctx* c, double dt, int nsteps, int flux, int precision) {
             a.qout = c->d_q[c->cur ^ 1];
             a.rka = kRk4a[st];
             a.rkb = kRk4b[st];
+            rc = refresh_boundary_traces(c, a.qin);
+            if (rc) return rc;
             rc = run_stage(c, a, precision);
             if (rc) return rc;
             c->cur ^= 1;
@@ -386,6 +390,7 @@ int dg_ssprk2_step(dg_ctx* c, double dt, int nsteps, int flux, int precision) {
         a.qin = c->d_q[c->cur];
         a.qout = c->d_q[c->cur ^ 1];
         a.mode = MODE_EULER;
+        if ((rc = refresh_boundary_traces(c, a.qin))) return rc;
         rc = run_stage(c, a, precision);
         if (rc) return rc;
         // stage 2: q = q/2 + (q1 + dt R(q1))/2, written over q (element-local reads of q only)
@@ -393,6 +398,7 @@ int dg_ssprk2_step(dg_ctx* c, double dt, int nsteps, int flux, int precision) {
         a.qold = c->d_q[c->cur];
         a.qout = c->d_q[c->cur];
         a.mode = MODE_SSP2;
+        if ((rc = refresh_boundary_traces(c, a.qin))) return rc;
         rc = run_stage(c, a, precision);
         if (rc) return rc;
     }

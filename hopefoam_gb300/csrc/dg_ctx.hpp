@@ -80,6 +80,8 @@ int euler_stage_mode(dg_ctx* c, const double* qin, double* qout, const double* q
                      int precision, const double* btrace);
 // limiter state teardown (limiter.cu)
 void limiter_teardown(dg_ctx* c);
+// traces of wall and zero-gradient slots from state q (no-op without such slots)
+int refresh_boundary_traces(dg_ctx* c, const double* q);
 
 // SIPG / PCG state (ipdg_api.cu)
 namespace dgk {

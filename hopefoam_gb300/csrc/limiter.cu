@@ -38,6 +38,7 @@ struct LimState {
     double* bs = nullptr;  // boundary field of the stage state
     double* bdata = nullptr;
     bool bq_set = false;
+    bool dynamic = false;  // some slot is a wall or zero gradient (traces follow the state)
 };
 
 namespace dgk {
@@ -390,6 +391,15 @@ int reflect(dg_ctx* c, const double* q, double* bnd) {
 
 }  // namespace
 
+// walls and zero-gradient slots: their boundary traces from the state q
+// (the unlimited steppers call this before every stage, as the reference
+// corrects its boundary conditions after every equation solve,
+// dgMatrixSolve.C:209); no work when no slot is of those kinds
+int refresh_boundary_traces(dg_ctx* c, const double* q) {
+    if (!c->lim || !c->lim->ready || !c->lim->dynamic) return DG_OK;
+    return reflect(c, q, c->d_btrace);
+}
+
 void limiter_teardown(dg_ctx* c) {
     if (!c->lim) return;
     for (void* p : c->lim->allocs) cudaFree(p);
@@ -450,6 +460,7 @@ int dg_set_boundary_kinds(dg_ctx* c, const int* kind, const int* gref) {
     c->lim = s;
     const int K = c->K, Np = c->Np, N = c->N, nb = c->nb, T = K + nb;
     s->kind_h.assign(kind, kind + nb);
+    for (int i = 0; i < nb; i++) s->dynamic |= kind[i] == 1 || kind[i] == 3;
     s->gref_h.resize(nb);
     for (int i = 0; i < nb; i++) s->gref_h[i] = gref ? gref[i] : i;
     std::vector<int> sk, sf;

@@ -301,7 +301,10 @@ int dg_euler_rhs_noalloc(dg_ctx* ctx, const double* q_dev, double* rhs_dev, int 
  * ghost cell takes (the reference uses the first value of the slot's patch).
  * dg_limit: the limiter on the current state with the current boundary traces.
  * dg_reflect_boundary_traces: the reflective and zero-gradient slots' traces
- * from the state.
+ * from the state.  Once kinds are set, dg_lserk4_step and dg_ssprk2_step also
+ * take those slots' traces from each stage's input state (the reference
+ * corrects its boundary conditions after every equation solve,
+ * dgMatrixSolve.C:209); fixed-value and other slots keep the traces as set.
  * dg_limited_ssprk2_step: one step (stage, walls, limiter, stage, walls,
  * average with the boundary values, limiter, walls); bdata [nb][4][Nfp] holds
  * this step's values of the fixed-value slots (setBoundaryValues.H).

@@ -67,3 +67,26 @@ class LimitedSSPOracle:
         q = self.limit(q, self.Bq)
         self.Bq = self.reflect(q, self.Bq)
         return q
+
+    def step_unlimited(self, q, dt, B):
+        """The reference's unlimited SSP-RK2 step (dgEulerFoam.C:69-117) with
+        wall and zero-gradient traces taken from each stage's input state;
+        B holds the traces of the other slots (kept)."""
+        B = self.reflect(q, B)
+        q1 = q + dt * self.rhs(q, B)
+        B = self.reflect(q1, B)
+        q2 = q1 + dt * self.rhs(q1, B)
+        return 0.5 * q + 0.5 * q2, B
+
+    def lserk4_unlimited(self, q, dt, B, res=None):
+        """One LSERK4 step with the same boundary rule (coefficients of
+        oracle.lserk4_coeffs)."""
+        from .oracle import lserk4_coeffs
+
+        a, b, _ = lserk4_coeffs()
+        res = np.zeros_like(q) if res is None else res
+        for s in range(5):
+            B = self.reflect(q, B)
+            res = a[s] * res + dt * self.rhs(q, B)
+            q = q + b[s] * res
+        return q, B, res

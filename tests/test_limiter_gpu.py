@@ -144,3 +144,53 @@ def test_double_mach_zero_gradient_outflow(gpu_lib):
     print("double Mach with a zero-gradient outflow, 10 steps: GPU vs oracle %.2e" % err)
     assert err < 1e-10
     ctx.close()
+
+
+@pytest.mark.parametrize("precision", ["fp64", "split"])
+def test_unlimited_steps_with_walls_and_outflow(gpu_lib, precision):
+    """dg_ssprk2_step and dg_lserk4_step with wall and zero-gradient slots:
+    their traces follow each stage's input state (the reference corrects its
+    boundary conditions after every solve); fixed-value slots keep theirs.
+    Tolerance: 1e-12 relative (FP64); split precision 1e-7 over these 3-5
+    steps (measured about 1.1e-8 per step: the split path's coarse-mesh
+    per-step figure, with the walls' and outflow's gradients in the boundary
+    elements)."""
+    from hopefoam_gb300 import _lib as L
+    from hopefoam_gb300 import euler
+    from hopefoam_gb300.mesh import box_square, load_cubature
+    from oracle.limited_oracle import LimitedSSPOracle
+
+    N = 4
+    m = box_square(9, 7, 10.0, 10.0)
+    kk, ff = euler.boundary_faces(m)
+    kinds = np.array([0, 1, 3])[np.arange(len(kk)) % 3].astype(np.int32)
+    ctx = euler.EulerContext(m, N)
+    lo = LimitedSSPOracle(m, N, load_cubature(3 * (N + 1)), kinds)
+    x, y = lo.O.nodes()
+    vortex = lambda a, b: euler.isentropic_vortex(a, b, x0=5.0, y0=5.0, uinf=0.3)
+    q0 = vortex(x, y)
+    B0 = euler.boundary_traces_from_nodes(m, N, vortex, x, y)
+    ctx.set_boundary_kinds(kinds)
+    prec = L.DG_PREC_FP64 if precision == "fp64" else L.DG_PREC_SPLIT
+    tol = 1e-12 if precision == "fp64" else 1e-7
+    dt = 0.004  # CFL about 0.4
+    # SSP-RK2
+    ctx.upload(q0)
+    ctx.set_boundary_traces(B0)
+    ctx.ssprk2(dt, 5, flux=L.DG_FLUX_ROE, precision=prec)
+    qo, B = q0.copy(), B0.copy()
+    for _ in range(5):
+        qo, B = lo.step_unlimited(qo, dt, B)
+    e1 = rel_l2(ctx.download(), qo)
+    # LSERK4 (LF flux)
+    lo.flux = L.DG_FLUX_LF
+    ctx.upload(q0)
+    ctx.set_boundary_traces(B0)
+    ctx.lserk4(dt, 3, flux=L.DG_FLUX_LF, precision=prec)
+    qo, B, res = q0.copy(), B0.copy(), None
+    for _ in range(3):
+        qo, B, res = lo.lserk4_unlimited(qo, dt, B, res)
+    e2 = rel_l2(ctx.download(), qo)
+    print("%s: SSP-RK2 with walls/outflow %.2e, LSERK4 %.2e" % (precision, e1, e2))
+    assert e1 < tol and e2 < tol
+    ctx.close()

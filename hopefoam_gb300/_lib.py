@@ -13,6 +13,7 @@ ERR_NAMES = {0: "DG_OK", 1: "DG_ERR_ARG", 2: "DG_ERR_CUDA", 3: "DG_ERR_TIMEOUT",
 DG_FLUX_LF, DG_FLUX_ROE = 0, 1
 DG_PREC_FP64, DG_PREC_SPLIT = 0, 1
 DG_PC_NONE, DG_PC_BLOCK_JACOBI, DG_PC_LEARNED, DG_PC_LEARNED_ONLY, DG_PC_MULTILEVEL = 0, 1, 2, 3, 4
+DG_PC_LEARNED_MULTILEVEL = 5
 DG_LPC_RELU, DG_LPC_LINEAR, DG_LPC_SCHWARZ = 0, 1, 2
 
 _dp = ctypes.POINTER(ctypes.c_double)

@@ -699,6 +699,14 @@ static cudaError_t pcg_precondition(const IpdgArgs& a, const PcgVecs& v, const L
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess || !v.zb) return e;
     const int lmode = mode == 0 ? LPC_PCG_INIT : LPC_PCG_REFRESH;
+    if (v.mg && v.zl && lpc && lpc->sw) {
+        // learned local stage into zl, then the coarse-space correction forms z
+        e = launch_schwarz_local(*lpc->sw, v.r, v.r32, lpc->U, nullptr, s);
+        if (e == cudaSuccess)
+            e = launch_schwarz_collect(*lpc->sw, v.zb, lpc->U, nullptr, v.zl, v.dz, LPC_APPLY, v.S, v.part, s);
+        if (e != cudaSuccess) return e;
+        return launch_mg_correction(*v.mg, v.r, v.zl, v.z, v.dz, lmode, v.S, v.part, v.nmax, nullptr, s);
+    }
     if (v.mg) return launch_mg_correction(*v.mg, v.r, v.zb, v.z, v.dz, lmode, v.S, v.part, v.nmax, nullptr, s);
     if (lpc->sw) {
         e = launch_schwarz_local(*lpc->sw, v.r, v.r32, lpc->U, nullptr, s);
@@ -726,7 +734,13 @@ cudaError_t launch_pcg_iteration(const IpdgArgs& a, const PcgVecs& v, bool fp32,
     ROWS_DISPATCH(a.Np,
                   (pcg_update_kernel<NP><<<rows_grid<NP>(a), RowDims<NP>::THREADS, 0, s>>>(v, a.K, parity)));
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
-    if (v.zb && v.mg) {
+    if (v.zb && v.mg && v.zl && lpc && lpc->sw) {
+        e = launch_schwarz_local(*lpc->sw, v.r, v.r32, lpc->U, &v.S->done, s);
+        if (e == cudaSuccess)
+            e = launch_schwarz_collect(*lpc->sw, v.zb, lpc->U, nullptr, v.zl, v.dz, LPC_APPLY, v.S, v.part, s);
+        if (e == cudaSuccess)
+            e = launch_mg_correction(*v.mg, v.r, v.zl, v.z, v.dz, LPC_PCG_ITERATION, v.S, v.part, v.nmax, nullptr, s);
+    } else if (v.zb && v.mg) {
         e = launch_mg_correction(*v.mg, v.r, v.zb, v.z, v.dz, LPC_PCG_ITERATION, v.S, v.part, v.nmax, nullptr, s);
     } else if (v.zb) {
         if (lpc->sw) {

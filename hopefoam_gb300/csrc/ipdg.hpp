@@ -71,6 +71,7 @@ struct PcgVecs {
     float* dp[2];
     float* r32;                  // learned Schwarz mode: FP32 copy of r for the learned kernel (else null)
     const MgLevels* mg;          // multilevel mode (with zb): the coarse-space correction forms z
+    double* zl;                  // learned + multilevel: the learned output, before the coarse correction
 };
 
 // largest grid of the PCG kernels (sizes the partials)

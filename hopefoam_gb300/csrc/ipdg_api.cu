@@ -63,6 +63,7 @@ struct IpdgState {
     __nv_bfloat16 *d_W1b = nullptr, *d_W2b = nullptr;
     int* d_perm = nullptr;
     double* d_zb = nullptr;
+    double* d_zl = nullptr;  // learned + multilevel: the learned output before the coarse correction
     float* d_sc = nullptr;  // per-element feature scale
     __nv_bfloat16* d_X = nullptr;  // features of the current residual (K x F)
     float *d_Hs = nullptr, *d_y = nullptr, *d_dY = nullptr;  // hidden (+ its gradient), output, output gradient
@@ -610,11 +611,14 @@ int dg_pcg_solve(dg_ctx* c, const double* b_host, double* x_host, double rtol, i
                  dg_solve_stats* stats) {
     if (!c || !b_host || !x_host || !(rtol > 0) || maxit < 1) return DG_ERR_ARG;
     if (!c->ipdg || !c->ipdg->ready) return ifail(c, DG_ERR_ARG, "dg_ipdg_setup not called");
-    if (pc != DG_PC_BLOCK_JACOBI && pc != DG_PC_LEARNED && pc != DG_PC_LEARNED_ONLY && pc != DG_PC_MULTILEVEL)
+    if (pc != DG_PC_BLOCK_JACOBI && pc != DG_PC_LEARNED && pc != DG_PC_LEARNED_ONLY && pc != DG_PC_MULTILEVEL &&
+        pc != DG_PC_LEARNED_MULTILEVEL)
         return ifail(c, DG_ERR_ARG, "unknown preconditioner");
-    const bool learned = pc == DG_PC_LEARNED || pc == DG_PC_LEARNED_ONLY;
-    const bool mgm = pc == DG_PC_MULTILEVEL;
+    const bool learned = pc == DG_PC_LEARNED || pc == DG_PC_LEARNED_ONLY || pc == DG_PC_LEARNED_MULTILEVEL;
+    const bool mgm = pc == DG_PC_MULTILEVEL || pc == DG_PC_LEARNED_MULTILEVEL;
     if (learned && !c->ipdg->lpc_ready) return ifail(c, DG_ERR_ARG, "dg_lpc_setup not called");
+    if (pc == DG_PC_LEARNED_MULTILEVEL && c->ipdg->lpc_form != DG_LPC_SCHWARZ)
+        return ifail(c, DG_ERR_ARG, "learned + multilevel needs the learned Schwarz form");
     if (mgm && !c->ipdg->mg_ready) {
         const int rcm = mg_setup(c);
         if (rcm) return rcm;
@@ -645,6 +649,10 @@ int dg_pcg_solve(dg_ctx* c, const double* b_host, double* x_host, double rtol, i
     v.P64 = nullptr;
     v.zb = (learned || mgm) ? s->d_zb : nullptr;
     v.mg = mgm ? &s->mg : nullptr;
+    if (pc == DG_PC_LEARNED_MULTILEVEL) {
+        if (!s->d_zl && ialloc(c, s, &s->d_zl, n)) return ifail(c, DG_ERR_NOMEM, "device allocation failed");
+        v.zl = s->d_zl;
+    }
     v.S = s->d_S;
     const bool mirrors = precision == DG_PREC_SPLIT;  // the FP32 apply stages from FP32 offset mirrors
     v.dz = mirrors ? s->d_dz : nullptr;

@@ -55,7 +55,14 @@ enum {
 enum { DG_BC_INTERIOR = 0, DG_BC_FIXED = 1 };
 
 /* preconditioners for dg_pcg_solve */
-enum { DG_PC_NONE = 0, DG_PC_BLOCK_JACOBI = 1, DG_PC_LEARNED = 2, DG_PC_LEARNED_ONLY = 3, DG_PC_MULTILEVEL = 4 };
+enum {
+    DG_PC_NONE = 0,
+    DG_PC_BLOCK_JACOBI = 1,
+    DG_PC_LEARNED = 2,
+    DG_PC_LEARNED_ONLY = 3,
+    DG_PC_MULTILEVEL = 4,
+    DG_PC_LEARNED_MULTILEVEL = 5
+};
 
 typedef struct dg_ctx dg_ctx;
 
@@ -205,7 +212,9 @@ int dg_ipdg_apply(dg_ctx* ctx, const double* x_host, double* y_host);
  * the Galerkin operator, one V-cycle over aggregated levels per application;
  * built on first use from the mesh's vertex ids, rebuilt after
  * dg_ipdg_set_boundary_types / dg_ipdg_set_mass; the reference has no
- * counterpart, its solver options are PETSc's).
+ * counterpart, its solver options are PETSc's) or DG_PC_LEARNED_MULTILEVEL
+ * (after dg_lpc_*: the learned local preconditioner in place of block Jacobi,
+ * plus the same coarse-space correction).
  * precision DG_PREC_FP64: FP64 operator in every iteration; DG_PREC_SPLIT:
  * FP32-arithmetic operator inside CG with FP64 vectors, dot products and
  * recurrences, the recurrence residual replaced by the true FP64 residual

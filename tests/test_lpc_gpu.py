@@ -185,3 +185,13 @@ def test_training_gains_and_solve(gpu_lib):
     assert st["rel_residual"] <= 1e-10 and st["iterations"] > 0
     assert st["iterations"] < stb["iterations"], (st["iterations"], stb["iterations"])
     assert rel_l2(x, xb) < 1e-8
+    # the learned local stage under the coarse-space correction: the same
+    # solution, fewer iterations than either preconditioner alone
+    for prec in (L.DG_PREC_SPLIT, L.DG_PREC_FP64):
+        xm, stm = ps.solve(b, rtol=1e-10, pc=L.DG_PC_MULTILEVEL, maxit=5000, precision=prec)
+        xl, stl = ps.solve(b, rtol=1e-10, pc=L.DG_PC_LEARNED_MULTILEVEL, maxit=5000, precision=prec)
+        print("learned %d, multilevel %d, learned + multilevel %d iterations" %
+              (st["iterations"], stm["iterations"], stl["iterations"]))
+        assert stl["rel_residual"] <= 1e-10 and stl["iterations"] < st["iterations"]
+        assert stl["iterations"] <= 1.2 * stm["iterations"]
+        assert rel_l2(xl, xb) < 1e-8

@@ -34,11 +34,55 @@ def workload(nx=256, order=5):
 
 
 def initial_state(mesh, order):
+    """The vortex at the product's nodes (libdgcu's reference element)."""
     from hopefoam_gb300 import euler
 
     ops = euler.reference_operators(order)
     x, y = euler.node_coords(mesh, ops["r"], ops["s"])
     return euler.isentropic_vortex(x, y, x0=5.0, y0=5.0), x, y
+
+
+def initial_state_oracle(orc):
+    """The vortex at the oracle's own nodes: the reference arm never loads
+    libdgcu."""
+    from hopefoam_gb300 import euler
+
+    x, y = orc.nodes()
+    return euler.isentropic_vortex(x, y, x0=5.0, y0=5.0)
+
+
+def host_cfl_dt(mesh, order, q, cfl=0.5, gamma=1.4):
+    """The CFL rule of dg_cfl_dt, evaluated on the host from the initial
+    state: dt = cfl * min_k(2 * area_k / longest edge_k) / ((N+1)^2 *
+    max(|u| + c)).  Both bench arms use this dt, so they run the same
+    configuration."""
+    v = np.asarray(mesh.VXY, np.float64)
+    e = np.stack([np.hypot(*(v[:, (f + 1) % 3] - v[:, f]).T) for f in range(3)], 1)
+    xr, yr = 0.5 * (v[:, 1, 0] - v[:, 0, 0]), 0.5 * (v[:, 1, 1] - v[:, 0, 1])
+    xs, ys = 0.5 * (v[:, 2, 0] - v[:, 0, 0]), 0.5 * (v[:, 2, 1] - v[:, 0, 1])
+    J = xr * ys - xs * yr
+    min_h = float(np.min(4.0 * J / e.max(1)))
+    q = np.asarray(q, np.float64).reshape(4, -1)
+    rho, u, w = q[0], q[1] / q[0], q[2] / q[0]
+    p = (gamma - 1.0) * (q[3] - 0.5 * rho * (u * u + w * w))
+    smax = float(np.max(np.hypot(u, w) + np.sqrt(np.abs(gamma * p / rho))))
+    return cfl * min_h / ((order + 1) ** 2 * smax)
+
+
+def headline_config(mesh, order, dt):
+    """The workload the headline metric is quoted on (identical in both arms)."""
+    return {"workload": "isentropic vortex, periodic 256x256x2 perturbed 10%%, N=%d (Np=%d), LF flux, LSERK4 CFL 0.5"
+                        % (order, (order + 1) * (order + 2) // 2),
+            "K": int(mesh.K), "order": order, "flux": "LF", "dt": float("%.12e" % dt),
+            "step": "one LSERK4 time step = 5 RK stages over the whole mesh",
+            "l2": "working set (q in/out + RK register) > 129 MB L2, no flush"}
+
+
+def alg_bytes_per_elem_stage_fp64res(order):
+    """The same minimum with an FP64 RK register and 5 FP64 metrics:
+    128 Np + 96 Nfp + 124 bytes per element-stage."""
+    Np = (order + 1) * (order + 2) // 2
+    return 128 * Np + 96 * (order + 1) + 124
 
 
 def alg_bytes_per_elem_stage(order, split=True):
@@ -52,8 +96,8 @@ def alg_bytes_per_elem_stage(order, split=True):
     return 4 * Np * (8 + 8 + 2 * res) + 96 * Nfp + 32 + 12
 
 
-# dram__bytes_read.sum + dram__bytes_write.sum of one stage launch at this
-# workload (profiles/euler_stage_split_N5.md)
+# dram__bytes_read.sum + dram__bytes_write.sum of one split-stage launch at
+# the headline workload (one ncu capture of euler_stage_split_kernel<5>)
 SPLIT_STAGE_TRAFFIC_N5 = 222.0e6
 
 
@@ -117,9 +161,10 @@ def peaks():
     return 6800.0, "fallback"
 
 
-def cpu_baseline(mesh, order, q0, dt, threads):
+def cpu_baseline(mesh, order, q0, dt, threads, one_thread=True):
     """Oracle LSERK4 (one time step = 5 stages) on the full mesh with all host
-    threads; returns DOF-stage/s."""
+    threads, and one stage on one thread; returns DOF-stage/s for both and the
+    seconds each sample took."""
     from hopefoam_gb300.mesh import load_cubature
     from oracle import oracle
 
@@ -130,16 +175,28 @@ def cpu_baseline(mesh, order, q0, dt, threads):
     orc.lserk4(q, dt, 1, flux=0)
     el = time.perf_counter() - t
     dofs = mesh.K * orc.Np * 4
-    return dofs * 5 / el, el
+    out = {"value": dofs * 5 / el, "seconds": el}
+    if one_thread:
+        oracle.set_threads(1)
+        t = time.perf_counter()
+        orc.euler_rhs(q, flux=0)
+        el1 = time.perf_counter() - t
+        oracle.set_threads(threads)
+        out["value_1thread"] = dofs / el1
+        out["seconds_1thread"] = el1
+    return out
 
 
 def run_reference(args):
+    """The reference arm: the oracle (the reference's algorithm restated in
+    C++, OpenMP over all host threads) on the headline workload, its initial
+    state built at the oracle's own nodes and stepped at the same dt.  Nothing
+    here loads libdgcu."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
-    order = 5
-    mesh = workload()
-    q0, _, _ = initial_state(mesh, order)
+    order = args.order
+    mesh = workload(args.nx, order)
     from oracle import oracle
 
     from hopefoam_gb300.mesh import load_cubature
@@ -147,7 +204,8 @@ def run_reference(args):
     threads = oracle.max_threads()
     oracle.set_threads(threads)
     orc = oracle.Oracle(mesh, order, load_cubature(3 * (order + 1)))
-    dt = 1e-4
+    q0 = initial_state_oracle(orc)
+    dt = host_cfl_dt(mesh, order, q0)
     q = q0.reshape(-1)
     res = None
     for _ in range(args.warmup):
@@ -161,14 +219,22 @@ def run_reference(args):
     dofs_stage = mesh.K * Np * 4 * 5
     tot = float(np.sum(vals))
     value = dofs_stage * args.steps / tot
+    # one right-hand side on one thread (a bounded sample of the same work)
+    oracle.set_threads(1)
+    t = time.perf_counter()
+    orc.euler_rhs(q, flux=0)
+    el1 = time.perf_counter() - t
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1e3 * tot / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "impl": "reference",
-            "config": {"workload": "isentropic vortex, periodic 256x256x2 perturbed, N=5, LSERK4, LF flux",
-                       "K": mesh.K, "order": order},
+            "config": headline_config(mesh, order, dt),
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
-                             "sample": "one LSERK4 step (5 stages) over all 131072 elements per bench step"},
+                             "sample": "one LSERK4 step (5 stages) over all %d elements per bench step" % mesh.K,
+                             "value_1thread": mesh.K * Np * 4 / el1,
+                             "sample_1thread": "one right-hand side over all %d elements on 1 thread, %.1f s"
+                                               % (mesh.K, el1),
+                             "build": "g++ -O3 -fopenmp (portable flags: the same source builds on x86 and Arm)"},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
 
@@ -185,6 +251,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-poisson", action="store_true")
     ap.add_argument("--no-batch", action="store_true")
+    ap.add_argument("--no-fp64", action="store_true", help="skip timing the plain FP64 path beside the split path")
     ap.add_argument("--no-configs", action="store_true")
     ap.add_argument("--kh-steps", type=int, default=2)
     ap.add_argument("--no-ins", action="store_true", help="skip the incompressible (Chorin) step benchmark")
@@ -211,9 +278,9 @@ def main():
     order = args.order
     mesh = workload(args.nx, order)
     q0, x, y = initial_state(mesh, order)
+    dt = host_cfl_dt(mesh, order, q0)
     ctx = euler.EulerContext(mesh, order)
     ctx.upload(q0)
-    dt = ctx.cfl_dt(0.5)
     prec_name = args.precision
     if prec_name == "auto":
         prec_name = "split" if _split_ready(ctx) else "fp64"
@@ -253,27 +320,48 @@ def main():
     launches = 5 * args.steps
     per_launch_s = ms * 1e-3 / launches
     bpe = alg_bytes_per_elem_stage(order, split=(prec_name == "split"))
+    bpe_survey = alg_bytes_per_elem_stage_fp64res(order)
     achieved = bpe * mesh.K / per_launch_s / 1e9
     peak, peak_kind = peaks()
     qfin = ctx.download()
     finite = bool(np.isfinite(qfin).all())
-    # precision of the timed path: one LSERK4 step from the same state against the FP64
-    # path (itself equal to the oracle to 1e-12, tests/test_euler_gpu.py)
+
+    # the plain FP64 path on the same workload (same dt, same state)
+    fp64 = None
+    if prec_name == "split" and not args.no_fp64:
+        ctx.upload(q0)
+        ctx.lserk4(dt, 1, flux=L.DG_FLUX_LF, precision=L.DG_PREC_FP64)  # warm-up
+        ctx.upload(q0)
+        n64 = max(2, min(args.steps, 4))
+        ms64 = _timed_lserk4(ctx, dt, n64, L.DG_FLUX_LF, L.DG_PREC_FP64)
+        fp64 = {"value": mesh.K * Np * 4 * 5 * n64 / (ms64 * 1e-3), "unit": UNIT, "ms_per_step": ms64 / n64,
+                "steps": n64, "split_speedup": (ms64 / n64) / (ms / args.steps)}
+
+    # precision of the timed path against the FP64 path (itself equal to the
+    # oracle to 1e-12, tests/test_euler_gpu.py) from the benchmark state: the
+    # right-hand side, and the state after one LSERK4 step
     precision_check = None
     if prec_name == "split":
         ctx.upload(qfin)
+        r64 = ctx.rhs(flux=L.DG_FLUX_LF, precision=L.DG_PREC_FP64)
+        rsp = ctx.rhs(flux=L.DG_FLUX_LF, precision=L.DG_PREC_SPLIT)
         ctx.lserk4(dt, 1, flux=L.DG_FLUX_LF, precision=L.DG_PREC_FP64)
         q64 = ctx.download()
         ctx.upload(qfin)
         ctx.lserk4(dt, 1, flux=L.DG_FLUX_LF, precision=prec)
         qsp = ctx.download()
         d = (qsp - q64).reshape(4, -1)
-        r64 = q64.reshape(4, -1)
-        precision_check = {"against": "FP64 path, one LSERK4 step from the benchmark state",
-                           "rel_l2": float(np.linalg.norm(d) / np.linalg.norm(r64)),
-                           "rel_linf": float(np.abs(d).max() / np.abs(r64).max()),
-                           "rel_l2_per_variable": [float(np.linalg.norm(d[v]) / np.linalg.norm(r64[v]))
-                                                   for v in range(4)]}
+        r64v = q64.reshape(4, -1)
+        dr = rsp - r64
+        precision_check = {
+            "against": "FP64 GPU path from the benchmark state after the timed steps",
+            "rhs_rel_l2": float(np.linalg.norm(dr) / np.linalg.norm(r64)),
+            "rhs_rel_linf": float(np.abs(dr).max() / np.abs(r64).max()),
+            "step_rel_l2": float(np.linalg.norm(d) / np.linalg.norm(r64v)),
+            "step_rel_linf": float(np.abs(d).max() / np.abs(r64v).max()),
+            "step_rel_l2_per_variable": [float(np.linalg.norm(d[v]) / np.linalg.norm(r64v[v])) for v in range(4)],
+            "reading": "the 1e-9 target is met by the state after one step (step_rel_l2); the right-hand side "
+                       "itself carries FP32 flux round-off times the volume/surface cancellation (rhs_rel_l2)"}
 
     # end to end through the public API with pinned host buffers
     n = 4 * mesh.K * Np
@@ -303,28 +391,31 @@ def main():
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f64" if prec_name == "fp64" else "tf32x3+f32acc, f64 state", "data": "synthetic",
-        "config": {"workload": "isentropic vortex, periodic 256x256x2 perturbed 10%, N=5 (Np=21), LF flux, LSERK4 "
-                               "CFL 0.5", "K": mesh.K, "order": order, "precision": prec_name,
-                   "l2": "working set (q in/out + res) %.0f MB > 129 MB L2, no flush" % (3 * n * 8 / 1e6)},
+        "config": headline_config(mesh, order, dt),
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "traffic": SPLIT_STAGE_TRAFFIC_N5 if (prec_name == "split" and order == 5 and args.nx == 256)
                      else None, "peak_kind": peak_kind, "bytes_per_elem_stage": bpe,
-                     "kernel": "euler_stage_%s" % prec_name,
-                     "note": "the stage is latency-bound at 16 warps per SM (issue 36 %, FP64 pipe 39 %), "
-                             "not HBM-bound (profiles/euler_stage_split_N5.md)"},
+                     "frac_at_fp64_register_bytes": bpe_survey * mesh.K / per_launch_s / 1e9 / peak,
+                     "kernel": "euler_stage_%s_kernel<%d>" % (prec_name, order)},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": n * 8, "d2h_bytes_per_step": n * 8},
         "gpu_launches": launches,
         "clocks": ck,
         "state_finite": finite,
+        "precision": prec_name,
         "precision_check": precision_check,
+        "fp64": fp64,
     }
     if rank == 0 and not args.no_cpu_baseline:
         from oracle import oracle
 
         threads = oracle.max_threads()
-        v, el = cpu_baseline(mesh, order, q0, dt, threads)
-        line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
-                                "sample": "one LSERK4 step (5 stages) over all %d elements, %.1f s" % (mesh.K, el)}
+        cb = cpu_baseline(mesh, order, q0, dt, threads)
+        line["cpu_baseline"] = {"value": cb["value"], "unit": UNIT, "cores": threads, "kind": "port",
+                                "sample": "one LSERK4 step (5 stages) over all %d elements, %.1f s"
+                                          % (mesh.K, cb["seconds"]),
+                                "value_1thread": cb.get("value_1thread"),
+                                "sample_1thread": "one right-hand side over all %d elements on 1 thread, %.1f s"
+                                                  % (mesh.K, cb.get("seconds_1thread", 0.0))}
     ctx.close()
     if rank == 0 and not args.no_poisson:
         try:
@@ -334,7 +425,7 @@ def main():
     if rank == 0 and not args.no_configs:
         for key, fn in (("c1", c1_bench), ("c5", c5_bench)):
             try:
-                line[key] = fn() if key == "c1" else fn(nsteps=args.kh_steps)
+                line[key] = fn(with_oracle=not args.no_cpu_baseline) if key == "c1" else fn(nsteps=args.kh_steps)
             except Exception as exc:
                 line[key] = {"error": str(exc)}
     if rank == 0 and not args.no_configs:
@@ -362,12 +453,61 @@ def main():
         except Exception as exc:
             line["batched"] = {"error": str(exc)}
     if rank == 0:
+        line["summary"] = summary(line)  # last key: the end of the line is what a log tail shows
         print(json.dumps(line))
     if world > 1:
         torch.distributed.destroy_process_group()
 
 
-def c1_bench(nsteps=100, order=3):
+def summary(line):
+    """A compact digest of every workload of the line (3 significant digits)."""
+    def g(d, *path):
+        for p in path:
+            if not isinstance(d, dict) or p not in d:
+                return None
+            d = d[p]
+        if isinstance(d, float):
+            return float("%.3g" % d)
+        return d
+
+    out = {"headline": {"value": g(line, "value"), "e2e": g(line, "e2e", "value"), "frac": g(line, "roofline", "frac"),
+                        "ms_per_step": g(line, "ms_per_step"), "cpu": g(line, "cpu_baseline", "value"),
+                        "cpu_1thread": g(line, "cpu_baseline", "value_1thread")},
+           "fp64_path": {"value": g(line, "fp64", "value"), "split_speedup": g(line, "fp64", "split_speedup")},
+           "split_vs_fp64": {k: g(line, "precision_check", k) for k in ("rhs_rel_l2", "rhs_rel_linf", "step_rel_l2",
+                                                                           "step_rel_linf")}}
+    p = line.get("poisson")
+    if isinstance(p, dict):
+        out["poisson_ms"] = {"block_jacobi": g(p, "bj_mixed", "ms"), "bj_iters": g(p, "bj_mixed", "iterations"),
+                             "bj_frac": g(p, "bj_mixed", "roofline", "frac"),
+                             "multilevel": g(p, "multilevel_mixed", "ms"),
+                             "ml_iters": g(p, "multilevel_mixed", "iterations"),
+                             "learned": g(p, "learned", "ms"), "learned_iters": g(p, "learned", "iterations"),
+                             "learned_vs_bj": g(p, "learned", "speedup_vs_block_jacobi"),
+                             "learned_multilevel": g(p, "learned_multilevel", "ms"),
+                             "cpu": g(p, "cpu_baseline", "ms")}
+    for k in ("c1", "c5", "batched", "shock", "ins", "cylinder"):
+        d = line.get(k)
+        if not isinstance(d, dict):
+            continue
+        if "error" in d:
+            out[k] = {"error": str(d["error"])[:120]}
+            continue
+        out[k] = {kk: g(d, *pp) for kk, pp in {
+            "c1": {"value": ("value",), "rho_err_l2": ("rho_err_l2",), "state_vs_oracle": ("state_vs_oracle",)},
+            "c5": {"split_ms": ("split", "ms_per_step"), "fp64_ms": ("fp64", "ms_per_step"),
+                   "speedup": ("split_speedup_vs_fp64",), "frac": ("split", "roofline", "frac"),
+                   "step_l2": ("split_step_error", "rel_l2")},
+            "batched": {"value": ("value",), "frac": ("roofline", "frac"), "ms": ("ms",)},
+            "shock": {"fp64_ms": ("fp64", "ms_per_step"), "split_ms": ("split", "ms_per_step"),
+                      "cpu_ms": ("cpu_baseline", "ms_per_step")},
+            "ins": {"ms": ("ms_per_step",), "cpu_ms": ("cpu_baseline", "ms_per_step")},
+            "cylinder": {"ms": ("ms_per_step",), "cpu_ms": ("cpu_baseline", "ms_per_step"),
+                         "vs_oracle": ("state_vs_oracle",)}}[k].items()}
+    return out
+
+
+def c1_bench(nsteps=100, order=3, with_oracle=True):
     """The reference's CPU-sized case: isentropic vortex on the periodic
     40x40x2 mesh of [0,10]^2 (K = 3200), N = 3, LF flux, LSERK4 at CFL 0.5,
     100 steps on the FP64 path; L2 / Linf errors of density against the exact
@@ -399,10 +539,21 @@ def c1_bench(nsteps=100, order=3):
     ex = euler.isentropic_vortex(x, y, t=nsteps * dt, x0=5.0, y0=5.0)
     d = q[0] - ex[0]
     ctx.close()
-    return {"workload": "isentropic vortex, periodic 40x40x2 (K=3200), N=3, LF, LSERK4 CFL 0.5, %d steps, FP64"
-                        % nsteps, "dt": dt, "t": nsteps * dt,
-            "rho_err_l2": float(np.linalg.norm(d) / np.linalg.norm(ex[0])), "rho_err_linf": float(np.abs(d).max()),
-            "value": mesh.K * ops["r"].size * 4 * 5 * nsteps / (ms * 1e-3), "unit": UNIT, "ms": ms}
+    out = {"workload": "isentropic vortex, periodic 40x40x2 (K=3200), N=3, LF, LSERK4 CFL 0.5, %d steps, FP64"
+                       % nsteps, "dt": dt, "t": nsteps * dt,
+           "rho_err_l2": float(np.linalg.norm(d) / np.linalg.norm(ex[0])), "rho_err_linf": float(np.abs(d).max()),
+           "value": mesh.K * ops["r"].size * 4 * 5 * nsteps / (ms * 1e-3), "unit": UNIT, "ms": ms}
+    if with_oracle:
+        # the same 100 steps on the oracle: FP64 state parity at the configured size
+        from hopefoam_gb300.mesh import load_cubature
+        from oracle import oracle
+
+        orc = oracle.Oracle(mesh, order, load_cubature(3 * (order + 1)))
+        t0 = time.perf_counter()
+        qo, _ = orc.lserk4(q0.reshape(-1), dt, nsteps, flux=0)
+        out["oracle_s"] = time.perf_counter() - t0
+        out["state_vs_oracle"] = float(np.linalg.norm(q.reshape(-1) - qo) / np.linalg.norm(qo))
+    return out
 
 
 def _kh_context(n, order):

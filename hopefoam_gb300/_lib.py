@@ -68,12 +68,16 @@ SIGNATURES = {
     "dg_download_state_device": (ctypes.c_int, [_vp, _vp]),
     "dg_set_boundary_traces": (ctypes.c_int, [_vp, _dp]),
     "dg_euler_rhs": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, _dp]),
+    "dg_euler_rhs_device": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, _vp]),
+    "dg_forward_euler_stage": (ctypes.c_int, [_vp, ctypes.c_double, ctypes.c_int, ctypes.c_int]),
+    "dg_sync": (ctypes.c_int, [_vp]),
     "dg_lserk4_step": (ctypes.c_int, [_vp, ctypes.c_double, ctypes.c_int, ctypes.c_int, ctypes.c_int]),
     "dg_ssprk2_step": (ctypes.c_int, [_vp, ctypes.c_double, ctypes.c_int, ctypes.c_int, ctypes.c_int]),
     "dg_cfl_dt": (ctypes.c_int, [_vp, ctypes.c_double, _dp]),
     "dg_reference_operators": (ctypes.c_int, [ctypes.c_int, _dp, ctypes.c_int, _dp, _dp, _dp, _dp, _dp, _dp, _dp]),
     "dg_ipdg_setup": (ctypes.c_int, [_vp, ctypes.c_double]),
     "dg_ipdg_apply": (ctypes.c_int, [_vp, _dp, _dp]),
+    "dg_ipdg_apply_device": (ctypes.c_int, [_vp, _vp, _vp]),
     "dg_ipdg_set_boundary_types": (ctypes.c_int, [_vp, _ip]),
     "dg_ipdg_set_mass": (ctypes.c_int, [_vp, ctypes.c_double]),
     "dg_set_node_locations": (ctypes.c_int, [_vp, _dp, _dp]),
@@ -92,6 +96,8 @@ SIGNATURES = {
     "dg_ins_operator": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.POINTER(InsBdata), _dp, _dp]),
     "dg_pcg_solve": (ctypes.c_int, [_vp, _dp, _dp, ctypes.c_double, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                     ctypes.POINTER(SolveStats)]),
+    "dg_pcg_solve_device": (ctypes.c_int, [_vp, _vp, _vp, ctypes.c_double, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                           ctypes.POINTER(SolveStats)]),
     "dg_euler_rhs_noalloc": (ctypes.c_int, [_vp, _vp, _vp, ctypes.c_int]),
     "dg_lpc_setup": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_ulonglong, ctypes.c_int, ctypes.c_int]),
     "dg_lpc_add_residual": (ctypes.c_int, [_vp, _dp]),

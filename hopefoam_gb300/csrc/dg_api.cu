@@ -141,6 +141,10 @@ int dg_ctx_create(const dg_mesh_desc* m, const dg_opts* o, dg_ctx** out) {
     *out = nullptr;
     if (!m || !o || m->K <= 0 || !m->VXY || !m->EToE || !m->EToF) return DG_ERR_ARG;
     dg_ctx* c = new dg_ctx();
+    if (cudaGetDevice(&c->device) != cudaSuccess) {
+        delete c;
+        return DG_ERR_CUDA;
+    }
     c->K = m->K;
     c->N = o->order;
     c->gamma = o->gamma > 0 ? o->gamma : 1.4;
@@ -344,6 +348,7 @@ int dg_euler_rhs(dg_ctx* c, int flux, int precision, double* rhs_host) {
     a.qin = c->d_q[c->cur];
     a.rhs = c->d_q[c->cur ^ 1];  // scratch: the spare state buffer
     a.mode = MODE_RHS;
+    if ((rc = refresh_boundary_traces(c, a.qin))) return rc;
     rc = run_stage(c, a, precision);
     if (rc) return rc;
     rc = check_split_status(c, precision);
@@ -352,6 +357,45 @@ int dg_euler_rhs(dg_ctx* c, int flux, int precision, double* rhs_host) {
     if (e != cudaSuccess) return cuda_fail(c, e, "to_reference");
     DG_CUDA(c, cudaMemcpyAsync(rhs_host, c->d_stage, (size_t)c->K * 4 * c->Np * sizeof(double), cudaMemcpyDeviceToHost,
                                c->stream));
+    DG_CUDA(c, cudaStreamSynchronize(c->stream));
+    return DG_OK;
+}
+
+int dg_euler_rhs_device(dg_ctx* c, int flux, int precision, double* rhs_dev) {
+    int rc = check_run_args(c, flux, precision);
+    if (rc) return rc;
+    if (!rhs_dev) return fail(c, DG_ERR_ARG, "rhs_dev is NULL");
+    EulerArgs a = base_args(c, flux);
+    a.qin = c->d_q[c->cur];
+    a.rhs = c->d_q[c->cur ^ 1];  // scratch: the spare state buffer
+    a.mode = MODE_RHS;
+    if ((rc = refresh_boundary_traces(c, a.qin))) return rc;
+    rc = run_stage(c, a, precision);
+    if (rc) return rc;
+    cudaError_t e = launch_to_reference(a.rhs, rhs_dev, c->d_ring, c->K, c->Np, c->stream);
+    if (e != cudaSuccess) return cuda_fail(c, e, "to_reference");
+    return DG_OK;
+}
+
+int dg_forward_euler_stage(dg_ctx* c, double dt, int flux, int precision) {
+    int rc = check_run_args(c, flux, precision);
+    if (rc) return rc;
+    if (!(dt > 0)) return fail(c, DG_ERR_ARG, "bad dt");
+    EulerArgs a = base_args(c, flux);
+    a.dt = dt;
+    a.mode = MODE_EULER;
+    a.qin = c->d_q[c->cur];
+    a.qout = c->d_q[c->cur ^ 1];
+    if ((rc = refresh_boundary_traces(c, a.qin))) return rc;
+    rc = run_stage(c, a, precision);
+    if (rc) return rc;
+    c->cur ^= 1;
+    return DG_OK;
+}
+
+int dg_sync(dg_ctx* c) {
+    if (!c) return DG_ERR_ARG;
+    if (c->split.ready) return check_split_status(c, DG_PREC_SPLIT);
     DG_CUDA(c, cudaStreamSynchronize(c->stream));
     return DG_OK;
 }

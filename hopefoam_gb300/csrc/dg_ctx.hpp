@@ -31,6 +31,7 @@ cudaError_t launch_euler_split(int N, const EulerArgs& a, const SplitPlan& plan,
 
 struct dg_ctx {
     int K = 0, N = 0, Np = 0, Ng = 0, Nfp = 0, Nfq = 0, nb = 0;
+    int device = 0;  // the CUDA device current at dg_ctx_create (every buffer lives there)
     double gamma = 1.4;
     double min_h = 0;
     cudaStream_t stream = nullptr;

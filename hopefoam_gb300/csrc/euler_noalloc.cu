@@ -11,6 +11,11 @@
 // another framework and may not be grown behind its back; and loops with a
 // real-time budget, where an allocation's latency or failure is not allowed.
 //
+// Boundary slots: fixed-value slots use the traces set on the context; wall
+// and zero-gradient slots (dg_set_boundary_kinds) are recomputed from q_dev
+// into the context's trace buffer, as dg_euler_rhs does from the context's
+// state.
+//
 // Limits: 4 * K * Np <= DG_NOALLOC_MAX_VALUES (524288 values, 4 MiB per
 // buffer, 8 MiB in total).  Every GPU that loads this library keeps the array
 // until the process exits.  All calls share the array and it keeps the last
@@ -69,6 +74,11 @@ extern "C" int dg_euler_rhs_noalloc(dg_ctx* c, const double* q_dev, double* rhs_
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess || dev < 0 || dev >= kMaxDevices) return nfail(c, DG_ERR_CUDA, "cudaGetDevice failed");
+    // the scratch address is per device: another device's would be a foreign
+    // address for the kernels queued on this context's stream
+    if (dev != c->device)
+        return nfail(c, DG_ERR_ARG, "dg_euler_rhs_noalloc: the context's device (" + std::to_string(c->device) +
+                                        ") is not the current device (" + std::to_string(dev) + ")");
     double* scratch = nullptr;
     e = scratch_address(dev, &scratch);
     if (e != cudaSuccess) return nfail(c, DG_ERR_CUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
@@ -76,6 +86,10 @@ extern "C" int dg_euler_rhs_noalloc(dg_ctx* c, const double* q_dev, double* rhs_
     double* rhs_int = scratch + kMaxValues;
     e = dgk::launch_to_internal(q_dev, q_int, c->d_ring, c->K, c->Np, c->stream);
     if (e != cudaSuccess) return nfail(c, DG_ERR_CUDA, std::string("to_internal: ") + cudaGetErrorString(e));
+    // wall and zero-gradient slots take their traces from this state (a kernel
+    // writing the context's own trace buffer: no allocation)
+    const int rc = refresh_boundary_traces(c, q_int);
+    if (rc) return rc;
     dgk::EulerArgs a;
     memset(&a, 0, sizeof(a));
     a.qin = q_int;

@@ -607,9 +607,24 @@ int dg_ipdg_apply(dg_ctx* c, const double* x_host, double* y_host) {
     return DG_OK;
 }
 
-int dg_pcg_solve(dg_ctx* c, const double* b_host, double* x_host, double rtol, int maxit, int pc, int precision,
-                 dg_solve_stats* stats) {
+int dg_ipdg_apply_device(dg_ctx* c, const double* x_dev, double* y_dev) {
+    if (!c || !x_dev || !y_dev) return DG_ERR_ARG;
+    if (!c->ipdg || !c->ipdg->ready) return ifail(c, DG_ERR_ARG, "dg_ipdg_setup not called");
+    IpdgState* s = c->ipdg;
+    IP_CUDA(c, launch_permute(x_dev, s->d_p, c->d_ring, c->K, c->Np, true, c->stream));
+    int rc = apply64(c, s->d_p, s->d_Ap);
+    if (rc) return rc;
+    IP_CUDA(c, launch_permute(s->d_Ap, y_dev, c->d_ring, c->K, c->Np, false, c->stream));
+    return DG_OK;
+}
+
+// The PCG solve behind dg_pcg_solve (host vectors) and dg_pcg_solve_device
+// (device vectors): the two differ only in the direction of their copies.
+static int pcg_solve_impl(dg_ctx* c, const double* b_host, double* x_host, double rtol, int maxit, int pc,
+                          int precision, dg_solve_stats* stats, bool dev) {
     if (!c || !b_host || !x_host || !(rtol > 0) || maxit < 1) return DG_ERR_ARG;
+    const cudaMemcpyKind kin = dev ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+    const cudaMemcpyKind kout = dev ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
     if (!c->ipdg || !c->ipdg->ready) return ifail(c, DG_ERR_ARG, "dg_ipdg_setup not called");
     if (pc != DG_PC_BLOCK_JACOBI && pc != DG_PC_LEARNED && pc != DG_PC_LEARNED_ONLY && pc != DG_PC_MULTILEVEL &&
         pc != DG_PC_LEARNED_MULTILEVEL)
@@ -629,9 +644,9 @@ int dg_pcg_solve(dg_ctx* c, const double* b_host, double* x_host, double rtol, i
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
-    IP_CUDA(c, cudaMemcpyAsync(s->d_z, b_host, n * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+    IP_CUDA(c, cudaMemcpyAsync(s->d_z, b_host, n * sizeof(double), kin, c->stream));
     IP_CUDA(c, launch_permute(s->d_z, s->d_b, c->d_ring, c->K, c->Np, true, c->stream));
-    IP_CUDA(c, cudaMemcpyAsync(s->d_z, x_host, n * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+    IP_CUDA(c, cudaMemcpyAsync(s->d_z, x_host, n * sizeof(double), kin, c->stream));
     IP_CUDA(c, launch_permute(s->d_z, s->d_x, c->d_ring, c->K, c->Np, true, c->stream));
     cudaEventRecord(e0, c->stream);
     double bb = 0;
@@ -711,7 +726,7 @@ int dg_pcg_solve(dg_ctx* c, const double* b_host, double* x_host, double rtol, i
         cudaEventElapsedTime(&ms_learned, e0, e1);
         cudaEventDestroy(e0);
         cudaEventDestroy(e1);
-        int rc2 = dg_pcg_solve(c, b_host, x_host, rtol, maxit, DG_PC_BLOCK_JACOBI, precision, stats);
+        int rc2 = pcg_solve_impl(c, b_host, x_host, rtol, maxit, DG_PC_BLOCK_JACOBI, precision, stats, dev);
         if (stats) {
             stats->iterations = -stats->iterations;  // negative: the learned solve fell back
             stats->ms += ms_learned;
@@ -719,7 +734,7 @@ int dg_pcg_solve(dg_ctx* c, const double* b_host, double* x_host, double rtol, i
         return rc2;
     }
     IP_CUDA(c, launch_permute(s->d_x, s->d_z, c->d_ring, c->K, c->Np, false, c->stream));
-    IP_CUDA(c, cudaMemcpyAsync(x_host, s->d_z, n * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    IP_CUDA(c, cudaMemcpyAsync(x_host, s->d_z, n * sizeof(double), kout, c->stream));
     IP_CUDA(c, cudaStreamSynchronize(c->stream));
     float ms = 0;
     cudaEventElapsedTime(&ms, e0, e1);
@@ -734,6 +749,16 @@ int dg_pcg_solve(dg_ctx* c, const double* b_host, double* x_host, double rtol, i
     if (!(rel == rel) || stop == 2) return ifail(c, DG_ERR_NONFINITE, "PCG breakdown or non-finite residual");
     if (rel > rtol) return ifail(c, DG_ERR_NOT_CONVERGED, "PCG reached the iteration limit");
     return DG_OK;
+}
+
+int dg_pcg_solve(dg_ctx* c, const double* b_host, double* x_host, double rtol, int maxit, int pc, int precision,
+                 dg_solve_stats* stats) {
+    return pcg_solve_impl(c, b_host, x_host, rtol, maxit, pc, precision, stats, false);
+}
+
+int dg_pcg_solve_device(dg_ctx* c, const double* b_dev, double* x_dev, double rtol, int maxit, int pc, int precision,
+                        dg_solve_stats* stats) {
+    return pcg_solve_impl(c, b_dev, x_dev, rtol, maxit, pc, precision, stats, true);
 }
 
 }  // extern "C"

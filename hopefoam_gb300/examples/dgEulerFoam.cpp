@@ -1,7 +1,8 @@
 // dgEulerFoam.cpp -- the reference's isentropic-vortex solver loop
 // (tutorials/DG/2D/isentropicVortex/dgEulerFoam/dgEulerFoam.C:64-131) written
-// against the dgcu C++ stand-ins: SSP-RK2 stages as three
-// dg::solveEquation calls each, on a periodic square mesh, then the same number
+// against the dgcu C++ stand-ins, with the reference's call signatures: SSP-RK2
+// stages as three dg::solveEquation calls each (the state stays on the device
+// between the stages), on a periodic square mesh, then the same number
 // of steps with the device-resident integrator; prints both results' rho error
 // against the exact advected vortex and their difference.
 //
@@ -122,20 +123,36 @@ int main(int argc, char** argv) {
         dgcu::StageRunner::get().scheme = &Godunov;
         dgcu::StageRunner::get().dt = dt;
         // the reference's loop: two solveEquation stages and the SSP average
+        dgcu::dgScalarField rho1(rho), Ener1(Ener);
+        dgcu::dgVectorField rhoU1(rhoU);
         for (int n = 0; n < steps; n++) {
-            dgcu::dgScalarField rho1 = rho, Ener1 = Ener;
-            dgcu::dgVectorField rhoU1 = rhoU;
+            rho1 = rho;
+            rhoU1 = rhoU;
+            Ener1 = Ener;
             for (int stage = 0; stage < 2; stage++) {
-                Godunov.update(rho1, rhoU1, Ener1);
-                dgcu::dg::solveEquation(dgcu::dgm::ddt(rho1) + dgcu::dgc::div(Godunov.fluxRho()));
-                dgcu::dg::solveEquation(dgcu::dgm::ddt(rhoU1) + dgcu::dgc::div(Godunov.fluxRhoU()) + dgcu::dgc::grad());
-                dgcu::dg::solveEquation(dgcu::dgm::ddt(Ener1) + dgcu::dgc::div(Godunov.fluxEner()) + dgcu::dgc::divUp());
+                rho1.updateGaussField();
+                rhoU1.updateGaussField();
+                Ener1.updateGaussField();
+                dgcu::dgGaussVectorField gther_U = rhoU1.gaussField() / rho1.gaussField();
+                dgcu::dgGaussScalarField gther_p = dgcu::pressure(gamma, rho1.gaussField(), gther_U, Ener1.gaussField());
+                Godunov.update(gther_U, gther_p, gamma, rho1.gaussField(), rhoU1.gaussField(), Ener1.gaussField());
+                dgcu::dg::solveEquation(dgcu::dgm::ddt(rho1) + dgcu::dgc::div(gther_U, rho1, Godunov.fluxRho()));
+                dgcu::dg::solveEquation(dgcu::dgm::ddt(rhoU1) + dgcu::dgc::div(gther_U, rhoU1, Godunov.fluxRhoU()) +
+                                        dgcu::dgc::grad(gther_p));
+                dgcu::dg::solveEquation(dgcu::dgm::ddt(Ener1) + dgcu::dgc::div(gther_U, Ener1, Godunov.fluxEner()) +
+                                        dgcu::dgc::div(gther_U, gther_p));
             }
+            // rho = 0.5 rho + 0.5 rho1 (the stage results stay on the device until read here)
+            const dgcu::dgScalarField& r1 = rho1;
+            const dgcu::dgVectorField& ru1 = rhoU1;
+            const dgcu::dgScalarField& e1 = Ener1;
+            std::vector<double>&a = rho.component(0), &b = rhoU.component(0), &c = rhoU.component(1),
+                              &d = Ener.component(0);
             for (size_t i = 0; i < (size_t)K * Np; i++) {
-                rho.component(0)[i] = 0.5 * rho.component(0)[i] + 0.5 * rho1.component(0)[i];
-                rhoU.component(0)[i] = 0.5 * rhoU.component(0)[i] + 0.5 * rhoU1.component(0)[i];
-                rhoU.component(1)[i] = 0.5 * rhoU.component(1)[i] + 0.5 * rhoU1.component(1)[i];
-                Ener.component(0)[i] = 0.5 * Ener.component(0)[i] + 0.5 * Ener1.component(0)[i];
+                a[i] = 0.5 * a[i] + 0.5 * r1.component(0)[i];
+                b[i] = 0.5 * b[i] + 0.5 * ru1.component(0)[i];
+                c[i] = 0.5 * c[i] + 0.5 * ru1.component(1)[i];
+                d[i] = 0.5 * d[i] + 0.5 * e1.component(0)[i];
             }
         }
         // the same steps with the device-resident integrator

@@ -131,6 +131,25 @@ int dg_set_boundary_traces(dg_ctx* ctx, const double* traces_host);
  * DG/divSchemes/defaultDivScheme/defaultDivScheme.C:85-166. */
 int dg_euler_rhs(dg_ctx* ctx, int flux, int precision, double* rhs_host);
 
+/* Device-pointer, stream-ordered form of dg_euler_rhs: R(q) of the context's
+ * state into rhs_dev (4*K*Np doubles on the context's device, reference
+ * layout), queued on the context's stream; returns without synchronising.
+ * A bounded-wait timeout of the split-precision kernel is reported by the
+ * next dg_sync (or stepping call) on the context.  Wall and zero-gradient
+ * boundary slots take their traces from the state, as in every stage. */
+int dg_euler_rhs_device(dg_ctx* ctx, int flux, int precision, double* rhs_dev);
+
+/* One forward-Euler stage q <- q + dt M^-1 R_weak(q) of the context's state
+ * on the device, stream-ordered, no host synchronisation: the work of one
+ * dg::solveEquation(dgm::ddt(q) + dgc::div(...)) of the reference's three
+ * conserved equations together (Equation/Equation.C:39-75,
+ * DG/ddtSchemes/EulerDdtScheme/EulerDdtScheme.C:118-144). */
+int dg_forward_euler_stage(dg_ctx* ctx, double dt, int flux, int precision);
+
+/* Waits for the context's queued work; reports a bounded-wait timeout of a
+ * split-precision kernel queued by a stream-ordered call (DG_ERR_TIMEOUT). */
+int dg_sync(dg_ctx* ctx);
+
 /* nsteps low-storage RK4 steps (5 stages each, coefficients of
  * tutorials/DG/2D/isentropicVortex/dgEulerFoam/createFields.H:119-138). */
 int dg_lserk4_step(dg_ctx* ctx, double dt, int nsteps, int flux, int precision);
@@ -201,6 +220,12 @@ int dg_ipdg_set_mass(dg_ctx* ctx, double alpha);
 /* y = S x with S = -A (SPD sign of the reference operator A), matrix-free,
  * FP64; x, y host arrays of K*Np doubles in the reference node order. */
 int dg_ipdg_apply(dg_ctx* ctx, const double* x_host, double* y_host);
+/* Same on device vectors (K*Np doubles each, reference node order, on the
+ * context's device), stream-ordered: queued on the context's stream, no host
+ * synchronisation.  The matrix-free apply that replaces the assembled
+ * dgLduMatrix / PETSc MatMult of the pressure operator
+ * (defaultLaplacianScheme.C:63-288, dgMatrix.C:383-438). */
+int dg_ipdg_apply_device(dg_ctx* ctx, const double* x_dev, double* y_dev);
 
 /* Solves S x = b to ||b - S x|| <= rtol ||b|| with preconditioned CG
  * (replaces dgMatrix::solve -> KSPSolve, dgMatrices/dgMatrix/dgMatrix.C:162-283,
@@ -224,6 +249,14 @@ int dg_ipdg_apply(dg_ctx* ctx, const double* x_host, double* y_host);
  * reached (x_host still receives the last iterate). */
 int dg_pcg_solve(dg_ctx* ctx, const double* b_host, double* x_host, double rtol, int maxit, int pc, int precision,
                  dg_solve_stats* stats);
+/* Same on device vectors (K*Np doubles each, reference node order, on the
+ * context's device): b_dev is read, x_dev holds the initial guess and
+ * receives the solution, with no host staging.  The iteration count is not
+ * known in advance, so the call synchronises the context's stream between
+ * batches of iterations to test convergence (as KSPSolve returns only once
+ * converged, dgMatrixSolve.C:114-207), and once at the end. */
+int dg_pcg_solve_device(dg_ctx* ctx, const double* b_dev, double* x_dev, double rtol, int maxit, int pc, int precision,
+                        dg_solve_stats* stats);
 
 /* Learned element-block preconditioner for dg_pcg_solve (DG_PC_LEARNED).  No
  * counterpart in the reference (its KSP uses jacobi / LU, dgMatrix.C:199-222).
@@ -280,9 +313,13 @@ int dg_lpc_apply(dg_ctx* ctx, const double* r_host, double* z_host);
  * addition for callers that must not allocate device memory while they run
  * (inside a CUDA stream capture, under an application-owned memory pool, or
  * in a loop with a real-time budget).  Same result as dg_euler_rhs with
- * DG_PREC_FP64, but state and output are device arrays in the reference
- * layout (q_dev, rhs_dev: 4*K*Np doubles each, on the context's device, which
- * must be current) and the call makes no allocation: its scratch is a fixed
+ * DG_PREC_FP64 for the state q_dev, but state and output are device arrays in
+ * the reference layout (q_dev, rhs_dev: 4*K*Np doubles each, on the context's
+ * device, which must be current: DG_ERR_ARG otherwise).  Boundary traces:
+ * fixed-value slots use the traces set on the context; wall and zero-gradient
+ * slots are recomputed from q_dev into the context's trace buffer (as
+ * dg_euler_rhs does from the context's state).  The call makes no allocation:
+ * its scratch is a fixed
  * array in device global memory, 2 x DG_NOALLOC_MAX_VALUES doubles (8 MiB),
  * kept by every GPU that loads the library until the process exits.  Sizes
  * with 4*K*Np > DG_NOALLOC_MAX_VALUES are rejected with DG_ERR_ARG.  The

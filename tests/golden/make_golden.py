@@ -46,7 +46,9 @@ SLIDE18 = {
 
 
 def main():
-    root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    root = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("HOPEFOAM_REFERENCE_ROOT")
+    if not root:
+        sys.exit("usage: make_golden.py <reference root> (or set HOPEFOAM_REFERENCE_ROOT)")
     tut = os.path.join(root, "HopeFOAM-0.1", "tutorials", "DG", "2D", "isentropicVortex")
     for name in ["vortex0256", "vortex1024"]:
         m = read_fluent_msh(os.path.join(tut, name + ".msh"))

@@ -141,3 +141,26 @@ def test_errors_are_reported(gpu_lib):
     assert e.value.code == L.DG_ERR_ARG
     with pytest.raises(L.DGError):
         ctx.lserk4(-1.0, 1)
+
+
+def test_fp64_state_parity_at_configured_size(gpu_lib):
+    """The plain FP64 path against the oracle at the reference's CPU-sized
+    configuration itself: isentropic vortex, periodic 40x40x2 (K = 3200),
+    N = 3, LF flux, LSERK4 at CFL 0.5, 100 steps.  Round-off only, so the
+    fields agree to 1e-12 relative L2 after all 100 steps."""
+    from hopefoam_gb300 import _lib as L
+    from hopefoam_gb300 import euler
+    from hopefoam_gb300.mesh import periodic_square
+
+    N = 3
+    m = periodic_square(40, 40, 10.0, 10.0)
+    ctx, orc, x, y = _setup(m, N)
+    q = euler.isentropic_vortex(x, y, x0=5.0, y0=5.0)
+    ctx.upload(q)
+    dt = ctx.cfl_dt(0.5)
+    ctx.lserk4(dt, 100, flux=L.DG_FLUX_LF, precision=L.DG_PREC_FP64)
+    qg = ctx.download()
+    qo, _ = orc.lserk4(q.reshape(-1), dt, 100, flux=0)
+    err = rel_l2(qg.reshape(-1), qo)
+    print("K=3200 N=3, 100 LSERK4 steps: GPU FP64 vs oracle rel L2 %.3e" % err)
+    assert err < TOL_FP64

@@ -6,7 +6,8 @@ by the volume/face cancellation (~N^2, reduced by the delta formulation);
 on the coarse parity meshes below it is bounded at 2.5e-4 relative L2 and
 one LSERK4 step (5 stages) at 1e-8.  On the benchmark configuration itself
 (N = 5, 256x256x2, h = 10/256) one step must stay within 1e-9 relative L2
-of the FP64 path (the per-step target)."""
+of the FP64 path (the per-step target), and the right-hand side itself within
+1.5e-4 relative L2."""
 import numpy as np
 import pytest
 
@@ -17,6 +18,12 @@ pytestmark = pytest.mark.gpu
 TOL_RHS_SPLIT = 2.5e-4
 TOL_STEP_SPLIT = 1e-8
 TOL_STEP_C2 = 1e-9
+# on the benchmark configuration: the state after one step in Linf, and the
+# right-hand side itself (FP32 flux round-off times the volume / surface
+# cancellation; measured 6.8e-5 relative L2 on this workload)
+TOL_STEP_C2_LINF = 5e-8
+TOL_RHS_C2 = 1.5e-4
+TOL_RHS_C2_LINF = 2e-3
 # the shear layer starts from discontinuous data (density 1 | 2, u = -0.5 | +0.5
 # across |y - 0.5| = 0.25): elements on the interfaces carry O(1) variation, so
 # the delta formulation's round-off (eps32 times the in-element variation
@@ -136,8 +143,13 @@ def test_split_step_error_on_benchmark_config(gpu_lib):
     err_rhs = rel_l2(rsp, r64)
     err = rel_l2(qsp, q64)
     linf = np.abs(qsp - q64).max() / np.abs(q64).max()
-    print("benchmark config: split rhs rel L2 %.3e; one LSERK4 step state rel L2 %.3e Linf %.3e" % (err_rhs, err, linf))
+    rhs_linf = np.abs(rsp - r64).max() / np.abs(r64).max()
+    print("benchmark config: split rhs rel L2 %.3e Linf %.3e; one LSERK4 step state rel L2 %.3e Linf %.3e"
+          % (err_rhs, rhs_linf, err, linf))
     assert err < TOL_STEP_C2
+    assert linf < TOL_STEP_C2_LINF
+    assert err_rhs < TOL_RHS_C2
+    assert rhs_linf < TOL_RHS_C2_LINF
 
 
 def test_split_n7_roe_shear_layer_many_tiles(gpu_lib):

@@ -2,8 +2,10 @@
 may not allocate device memory while they run (stream capture, pool-owned
 device memory, real-time loops).  Checked through the C ABI against the
 existing entry point dg_euler_rhs (FP64), on two calls in a row with
-different states, within the FP64 path's tolerance; and the size limit of its
-fixed scratch array is enforced.  This file sorts last so that a run stopping
+different states, within the FP64 path's tolerance, on a periodic mesh and on
+the double-Mach mesh with reflective-wall slots (whose traces the call
+recomputes from the state it is given); and the size limit of its fixed
+scratch array is enforced.  This file sorts last so that a run stopping
 at the first failure has already run every other test."""
 import ctypes
 
@@ -64,3 +66,49 @@ def test_noalloc_rejects_sizes_beyond_its_scratch(gpu_lib):
     rc = lib.dg_euler_rhs_noalloc(ctx.h, ctypes.c_void_p(q_dev.data_ptr()), ctypes.c_void_p(out.data_ptr()), 0)
     assert rc == L.DG_ERR_ARG
     assert b"exceeds the fixed scratch" in lib.dg_last_error(ctx.h)
+
+
+def test_noalloc_rhs_with_wall_slots(gpu_lib):
+    """Reflective-wall boundary slots: the call recomputes their traces from
+    the state it is given, as dg_euler_rhs does from the context's state."""
+    import os
+
+    import torch
+
+    from conftest import GOLDEN
+    from hopefoam_gb300 import _lib as L
+    from hopefoam_gb300 import euler
+    from hopefoam_gb300.mesh import Mesh, connect
+    from hopefoam_gb300.shock import DoubleMach
+
+    lib = L.lib()
+    d = np.load(os.path.join(GOLDEN, "doublemach.npz"))
+    EToE, EToF, ROT, BC = connect(d["EToV"])
+    mesh = Mesh(d["EToV"], d["VXY"], EToE, EToF, ROT, BC, name="doubleMach", patch=d["patch"],
+                patch_names=tuple(str(x) for x in d["patch_names"]))
+    mesh.patch_first_face = d["patch_first_face"]
+    N = 4
+    dm = DoubleMach(mesh, N)
+    ctx = euler.EulerContext(mesh, N)
+    assert 4 * ctx.K * ctx.Np <= L.DG_NOALLOC_MAX_VALUES
+    ctx.set_boundary_traces(dm.bdata(0.0))
+    ctx.set_boundary_kinds(dm.kinds, dm.gref)
+    rng = np.random.default_rng(7)
+    for call in range(2):
+        q = dm.initial_state()
+        q = q * (1.0 + 0.05 * rng.uniform(-1.0, 1.0, size=q.shape))  # walls see a non-trivial interior trace
+        ctx.upload(q)
+        ref = ctx.rhs(flux=L.DG_FLUX_ROE, precision=L.DG_PREC_FP64)
+        q_dev = torch.from_numpy(q.reshape(-1).copy()).cuda()
+        out = torch.full_like(q_dev, float("nan"))
+        torch.cuda.synchronize()
+        rc = lib.dg_euler_rhs_noalloc(ctx.h, ctypes.c_void_p(q_dev.data_ptr()), ctypes.c_void_p(out.data_ptr()),
+                                      L.DG_FLUX_ROE)
+        assert rc == L.DG_OK, lib.dg_last_error(ctx.h)
+        torch.cuda.synchronize()
+        got = out.cpu().numpy().reshape(ref.shape)
+        err = np.linalg.norm(got - ref) / np.linalg.norm(ref)
+        print("wall slots, call %d: no-alloc rhs vs dg_euler_rhs rel L2 %.3e" % (call, err))
+        assert np.isfinite(got).all()
+        assert err < TOL
+    ctx.close()

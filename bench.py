@@ -257,10 +257,16 @@ def main():
     ap.add_argument("--no-ins", action="store_true", help="skip the incompressible (Chorin) step benchmark")
     ap.add_argument("--c5-study", action="store_true", help="500-step shear-layer accuracy study (reduced size)")
     ap.add_argument("--c5-study-n", type=int, default=128)
+    ap.add_argument("--profile-target", default=None, choices=sorted(PROFILE_TARGETS),
+                    help="run one workload of the line alone (the command the ncu summaries profile) and exit")
+    ap.add_argument("--profile-size", default="full", choices=["full", "small"],
+                    help="small: a reduced case of the same kernels for multi-pass ncu captures")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
         return run_reference(args)
+    if args.profile_target:
+        return profile_target(args.profile_target, args.profile_size == "small")
 
     import torch
 
@@ -964,6 +970,87 @@ def poisson_bench(with_cpu, n_interior=50000, order=4, tau_coef=1.0, rtol=1e-10)
                                          "iteration count"}
     ps.ctx.close()
     return out
+
+
+def _prof_pcg(small, pcs=("bj",)):
+    """The pressure system of the Poisson workload (Delaunay [0,2pi]^2, N = 4,
+    tau = (N+1)^2/h): a warm-up solve, then 64 iterations of each requested
+    preconditioner in mixed precision (block Jacobi also in FP64)."""
+    from hopefoam_gb300 import _lib as L
+    from hopefoam_gb300.mesh import delaunay_square
+    from hopefoam_gb300.poisson import PressureSolver, poisson_rhs
+
+    mesh = delaunay_square(12000 if small else 50000, seed=0)
+    ps = PressureSolver(mesh, 4, tau_coef=1.0)
+    b, _ = poisson_rhs(mesh, 4, seed=1)
+    out = {"K": mesh.K}
+    ps.solve(b, rtol=1e-4, precision=L.DG_PREC_SPLIT, raise_on_fail=False)  # warm-up
+    for name in pcs:
+        if name == "bj":
+            for pn, prec in (("bj_mixed", L.DG_PREC_SPLIT), ("bj_fp64", L.DG_PREC_FP64)):
+                _, st = ps.solve(b, rtol=1e-30, maxit=64, precision=prec, raise_on_fail=False)
+                out[pn] = {"iterations": st["iterations"], "ms": st["ms"]}
+        elif name == "multilevel":
+            ps.solve(b, rtol=1e-4, pc=L.DG_PC_MULTILEVEL, precision=L.DG_PREC_SPLIT, raise_on_fail=False)
+            _, st = ps.solve(b, rtol=1e-10, pc=L.DG_PC_MULTILEVEL, precision=L.DG_PREC_SPLIT, raise_on_fail=False)
+            out["multilevel"] = {"iterations": st["iterations"], "ms": st["ms"]}
+    ps.ctx.close()
+    return out
+
+
+def profile_target(name, small=False):
+    """One workload of the bench line on its own, for the ncu summaries (each
+    summary names the command it ran).  Prints one JSON line."""
+    import torch
+
+    torch.cuda.set_device(0)
+    from hopefoam_gb300 import _lib as L
+
+    out = {"profile_target": name, "size": "small" if small else "full"}
+    if name == "pcg":
+        out.update(_prof_pcg(small))
+    elif name == "multilevel":
+        out.update(_prof_pcg(small, pcs=("multilevel",)))
+    elif name == "learned":
+        from hopefoam_gb300.mesh import delaunay_square
+        from hopefoam_gb300.poisson import PressureSolver, poisson_rhs, train_learned_preconditioner
+
+        W1, W2, info = train_learned_preconditioner(4, tau_coef=1.0)
+        mesh = delaunay_square(12000 if small else 50000, seed=0)
+        ps = PressureSolver(mesh, 4, tau_coef=1.0)
+        ps.lpc_setup(hidden=info["hidden"], seed=0, capacity=0, form=info["form"])
+        ps.lpc_set_weights(W1, W2)
+        b, _ = poisson_rhs(mesh, 4, seed=1)
+        _, st = ps.solve(b, rtol=1e-30, maxit=64, pc=L.DG_PC_LEARNED_ONLY, precision=L.DG_PREC_SPLIT,
+                         raise_on_fail=False)
+        out.update({"K": mesh.K, "training": info, "iterations": st["iterations"], "ms": st["ms"]})
+        ps.ctx.close()
+    elif name == "ins":
+        out.update(ins_bench(n=64 if small else 128, steps=2, warmup=1, with_cpu=False))
+    elif name == "cylinder":
+        out.update(cylinder_bench(steps=3 if small else 8, warmup=0, with_cpu=False))
+    elif name == "limiter":
+        out.update(shock_bench(steps=10 if small else 50, warmup=2, with_cpu=False))
+    elif name == "batch":
+        prec = L.DG_PREC_SPLIT
+        out.update(batch_bench(prec, n_cases=32 if small else 512, nsteps=2 if small else 10))
+    elif name == "split":
+        from hopefoam_gb300 import euler
+
+        order = 5
+        mesh = workload(128 if small else 256, order)
+        q0, _, _ = initial_state(mesh, order)
+        ctx = euler.EulerContext(mesh, order)
+        ctx.upload(q0)
+        dt = host_cfl_dt(mesh, order, q0)
+        ctx.lserk4(dt, 2, flux=L.DG_FLUX_LF, precision=L.DG_PREC_SPLIT)
+        torch.cuda.synchronize()
+        out.update({"K": mesh.K, "steps": 2})
+        ctx.close()
+    print(json.dumps(out))
+
+
+PROFILE_TARGETS = ("pcg", "multilevel", "learned", "ins", "cylinder", "limiter", "batch", "split")
 
 
 def _split_ready(ctx):

@@ -23,6 +23,10 @@ struct SplitPlan {
     float* d_res32 = nullptr; // FP32 low-storage RK register
     int ctas_per_sm = 1;      // launch shape (persistent grid = SMs used x CTAs per SM)
     int sm_budget = 0;        // SMs the grid is sized for (0: all)
+    // kernel variant: tile-serial (every order) or software-pipelined across
+    // tiles (N <= 6, euler_split_pipe.cu)
+    enum { CLASSIC = 0, PIPE = 1 };
+    int variant = CLASSIC;
 };
 
 cudaError_t launch_euler_split(int N, const EulerArgs& a, const SplitPlan& plan, cudaStream_t s);

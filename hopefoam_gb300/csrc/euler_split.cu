@@ -976,10 +976,10 @@ static int setup_n(dg_ctx* c) {
         return DG_ERR_CUDA;
     if constexpr (!D::STREAM) {
         if (setup_split_pipe<N>() != cudaSuccess) return DG_ERR_CUDA;
-        c->split.variant = SplitPlan::CLASSIC;
-        // DGCU_SPLIT_VARIANT=pipe|classic selects the kernel variant (A/B measurements)
+        c->split.variant = SplitPlan::PIPE;
+        // DGCU_SPLIT_VARIANT=classic selects the tile-serial kernel (A/B measurements)
         const char* v = getenv("DGCU_SPLIT_VARIANT");
-        if (v && strcmp(v, "pipe") == 0) c->split.variant = SplitPlan::PIPE;
+        if (v && strcmp(v, "classic") == 0) c->split.variant = SplitPlan::CLASSIC;
     } else {
         c->split.variant = SplitPlan::CLASSIC;
     }

@@ -59,6 +59,7 @@ EulerArgs base_args(dg_ctx* c, int flux) {
     EulerArgs a;
     memset(&a, 0, sizeof(a));
     a.dtk = c->d_dtk;
+    a.dtk32 = c->d_dtk32;
     a.geo = c->d_geo;
     a.conn = c->d_conn;
     a.btrace = c->d_btrace;
@@ -281,7 +282,8 @@ const char* dg_last_error(const dg_ctx* c) { return c ? c->err.c_str() : "null c
 int dg_set_element_dt(dg_ctx* c, const double* dtk_host) {
     if (!c) return DG_ERR_ARG;
     if (!dtk_host) {
-        c->d_dtk = nullptr;  // the buffer stays allocated for a later call
+        c->d_dtk = nullptr;  // the buffers stay allocated for a later call
+        c->d_dtk32 = nullptr;
         return DG_OK;
     }
     for (int k = 0; k < c->K; k++)
@@ -292,6 +294,13 @@ int dg_set_element_dt(dg_ctx* c, const double* dtk_host) {
     }
     DG_CUDA(c, cudaMemcpy(c->dtk_buf, dtk_host, (size_t)c->K * sizeof(double), cudaMemcpyHostToDevice));
     c->d_dtk = c->dtk_buf;
+    if (!c->dtk32_buf) {
+        int rc = dmalloc(c, &c->dtk32_buf, (size_t)c->K);
+        if (rc) return rc;
+    }
+    std::vector<float> f32(dtk_host, dtk_host + c->K);
+    DG_CUDA(c, cudaMemcpy(c->dtk32_buf, f32.data(), (size_t)c->K * sizeof(float), cudaMemcpyHostToDevice));
+    c->d_dtk32 = c->dtk32_buf;
     return DG_OK;
 }
 

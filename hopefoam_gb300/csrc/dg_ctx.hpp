@@ -19,6 +19,7 @@ struct SplitPlan {
     void* d_ops = nullptr;    // operator images B1 | B2 (see euler_split.cu)
     size_t ops_bytes = 0;
     size_t b2_offset = 0;     // in floats
+    size_t if32_offset = 0;   // FP32 face interpolation table, in floats
     int* d_status = nullptr;  // bounded-wait timeout flag
     float* d_res32 = nullptr; // FP32 low-storage RK register
     int ctas_per_sm = 1;      // launch shape (persistent grid = SMs used x CTAs per SM)
@@ -60,6 +61,8 @@ struct dg_ctx {
     double *d_Vg = nullptr, *d_Sr = nullptr, *d_Ss = nullptr, *d_Lift = nullptr, *d_If = nullptr;
     double* d_dtk = nullptr;  // per-element time-step factors (dg_set_element_dt), null: none
     double* dtk_buf = nullptr;
+    float* d_dtk32 = nullptr;  // their FP32 copy (split-precision path)
+    float* dtk32_buf = nullptr;
     int cur = 0;
     bool btrace_set = false;
     dgk::SplitPlan split;

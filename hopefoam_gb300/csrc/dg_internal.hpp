@@ -51,6 +51,7 @@ struct EulerArgs {
     int mode;
     double gamma, dt, rka, rkb;
     const double* dtk;     // per-element time-step factors (null: 1); the step of element k is dt * dtk[k]
+    const float* dtk32;    // FP32 copy of dtk (the split-precision path)
 };
 
 // launchers (return cudaError_t of the launch)

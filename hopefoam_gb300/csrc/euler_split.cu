@@ -401,8 +401,8 @@ __global__ void __launch_bounds__(512, 1) euler_stage_split_kernel(SplitArgs sa)
 #pragma unroll
             for (int jn = 0; jn < Nfp; jn++) {
                 const int src = sbase + jn % FW;
-                const float w0 = (float)__ldg(a.ops.If + gi[0] * Nfp + jn);
-                const float w1 = (float)__ldg(a.ops.If + gi[1] * Nfp + jn);
+                const float w0 = __ldg(sa.If32 + gi[0] * Nfp + jn);
+                const float w1 = __ldg(sa.If32 + gi[1] * Nfp + jn);
 #pragma unroll
                 for (int v = 0; v < 4; v++) {
                     const float om = __shfl_sync(0xffffffffu, own[jn / FW][v], src);
@@ -519,7 +519,7 @@ __global__ void __launch_bounds__(512, 1) euler_stage_split_kernel(SplitArgs sa)
                 const int gi = i < Nfq ? i : 0;
 #pragma unroll
                 for (int jn = 0; jn < Nfp; jn++) {
-                    const float w = (float)__ldg(a.ops.If + gi * Nfp + jn);
+                    const float w = __ldg(sa.If32 + gi * Nfp + jn);
 #pragma unroll
                     for (int v = 0; v < 4; v++) {
                         if constexpr (D::PACKED) {
@@ -773,7 +773,7 @@ __global__ void __launch_bounds__(512, 1) euler_stage_split_kernel(SplitArgs sa)
         if (failed) break;
         // the epilogue's RK register values, loaded while the last MMAs run
         constexpr int EPI = D::EPI;
-        const bool first = (a.rka == 0.0);
+        const bool first = sa.first != 0;
         float resp[EPI];
         double q0v[EPI];  // N = 7, and N <= 6 with bulk tile copies: the stage input again (L2)
         {
@@ -837,11 +837,11 @@ __global__ void __launch_bounds__(512, 1) euler_stage_split_kernel(SplitArgs sa)
         }
         umma::fence_before_sync();
         __syncthreads();
-        if (a.mode == MODE_LSERK && !a.dtk) {
+        if (a.mode == MODE_LSERK && !sa.dtk32) {
             // the LSERK stage with one time step for all elements: straight-line
             // loads and stores (no early exit, no per-value mode dispatch)
             const size_t base = (size_t)k0 * 4 * Np;
-            const float rka = (float)a.rka, dtf0 = (float)a.dt, rkb = (float)a.rkb;
+            const float rka = sa.rkaf, dtf0 = sa.dtf, rkb = sa.rkbf;
             const int nv = ne * 4 * Np;
 #pragma unroll
             for (int j = 0; j < EPI; j++) {
@@ -858,7 +858,7 @@ __global__ void __launch_bounds__(512, 1) euler_stage_split_kernel(SplitArgs sa)
             }
         } else {
             const size_t base = (size_t)k0 * 4 * Np;
-            const float rka = (float)a.rka, dtf0 = (float)a.dt, rkb = (float)a.rkb;
+            const float rka = sa.rkaf, dtf0 = sa.dtf, rkb = sa.rkbf;
 #pragma unroll
             for (int j = 0; j < EPI; j++) {
                 const int i = tid + j * D::THREADS;
@@ -868,7 +868,7 @@ __global__ void __launch_bounds__(512, 1) euler_stage_split_kernel(SplitArgs sa)
                 if constexpr (D::STREAM) q0 = q0v[j];
                 else q0 = sa.qbulk ? q0v[j] : sQ64[i];
                 const size_t idx = base + i;
-                const float dtf = a.dtk ? (float)(a.dt * a.dtk[k0 + i / (4 * Np)]) : dtf0;
+                const float dtf = sa.dtk32 ? dtf0 * sa.dtk32[k0 + i / (4 * Np)] : dtf0;
                 switch (a.mode) {
                     case MODE_RHS: a.rhs[idx] = (double)R; break;
                     case MODE_LSERK: {
@@ -959,14 +959,17 @@ static int setup_n(dg_ctx* c) {
             return cc < 3 * Nfq ? o.dLift[(size_t)p * 3 * Nfq + cc] : 0.0;
         });
     }
-    size_t bytes = (b1.size() + b2.size()) * sizeof(float);
+    std::vector<float> if32(o.If.begin(), o.If.end());  // Nfq x Nfp
+    size_t bytes = (b1.size() + b2.size() + if32.size()) * sizeof(float);
     float* d = nullptr;
     if (cudaMalloc(&d, bytes) != cudaSuccess) return DG_ERR_NOMEM;
     cudaMemcpy(d, b1.data(), b1.size() * 4, cudaMemcpyHostToDevice);
     cudaMemcpy(d + b1.size(), b2.data(), b2.size() * 4, cudaMemcpyHostToDevice);
+    cudaMemcpy(d + b1.size() + b2.size(), if32.data(), if32.size() * 4, cudaMemcpyHostToDevice);
     c->split.d_ops = d;
     c->split.ops_bytes = bytes;
     c->split.b2_offset = b1.size();
+    c->split.if32_offset = b1.size() + b2.size();
     if (cudaMalloc(&c->split.d_status, sizeof(int)) != cudaSuccess) return DG_ERR_NOMEM;
     cudaMemset(c->split.d_status, 0, sizeof(int));
     if (cudaMalloc(&c->split.d_res32, (size_t)c->K * 4 * Np * sizeof(float)) != cudaSuccess) return DG_ERR_NOMEM;
@@ -1003,6 +1006,12 @@ static cudaError_t launch_split_n(const EulerArgs& a, const SplitPlan& plan, cud
     sa.b2 = static_cast<const float*>(plan.d_ops) + plan.b2_offset;
     sa.status = plan.d_status;
     sa.qbulk = (reinterpret_cast<uintptr_t>(a.qin) & 15u) == 0;
+    sa.If32 = static_cast<const float*>(plan.d_ops) + plan.if32_offset;
+    sa.dtk32 = a.dtk ? a.dtk32 : nullptr;
+    sa.rkaf = (float)a.rka;
+    sa.rkbf = (float)a.rkb;
+    sa.dtf = (float)a.dt;
+    sa.first = a.rka == 0.0;
     const int ntiles = (a.K + D::E - 1) / D::E;
     const int sms = (plan.sm_budget > 0 && plan.sm_budget < plan.sms) ? plan.sm_budget : plan.sms;
     const int want = sms * (plan.ctas_per_sm > 0 ? plan.ctas_per_sm : 1);

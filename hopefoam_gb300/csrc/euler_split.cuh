@@ -99,6 +99,13 @@ struct SplitArgs {
     const float* b2;     // device image of B2
     int* status;         // nonzero on a bounded-wait timeout
     int qbulk;           // N <= 6: the state is 16-byte aligned, tiles arrive by bulk copy
+    // FP32 forms of the stage's scalars and tables, prepared on the host so
+    // that no thread converts them (FP64 <-> FP32 conversions occupy the FP64
+    // pipe, two thread-operations per clock per SM on GB300)
+    const float* If32;   // face interpolation Nfq x Nfp
+    const float* dtk32;  // per-element time-step factors (null: none)
+    float rkaf, rkbf, dtf;
+    int first;           // LSERK stage with a = 0 (the register is not read)
 };
 
 constexpr uint32_t kWaitLimit = 1u << 22;

@@ -324,8 +324,8 @@ __global__ void __launch_bounds__(512, 1) euler_stage_split_pipe_kernel(SplitArg
 #pragma unroll
             for (int jn = 0; jn < Nfp; jn++) {
                 const int src = sbase + jn % FW;
-                const float w0 = (float)__ldg(a.ops.If + gi[0] * Nfp + jn);
-                const float w1 = (float)__ldg(a.ops.If + gi[1] * Nfp + jn);
+                const float w0 = __ldg(sa.If32 + gi[0] * Nfp + jn);
+                const float w1 = __ldg(sa.If32 + gi[1] * Nfp + jn);
 #pragma unroll
                 for (int v = 0; v < 4; v++) {
                     const float om = __shfl_sync(0xffffffffu, own[jn / FW][v], src);
@@ -426,7 +426,7 @@ __global__ void __launch_bounds__(512, 1) euler_stage_split_pipe_kernel(SplitArg
                 const int gi = i < Nfq ? i : 0;
 #pragma unroll
                 for (int jn = 0; jn < Nfp; jn++) {
-                    const float w = (float)__ldg(a.ops.If + gi * Nfp + jn);
+                    const float w = __ldg(sa.If32 + gi * Nfp + jn);
 #pragma unroll
                     for (int v = 0; v < 4; v++) {
                         if constexpr (S::PACKED) {
@@ -711,7 +711,7 @@ __global__ void __launch_bounds__(512, 1) euler_stage_split_pipe_kernel(SplitArg
         }
         // the epilogue's RK register values and stage input (L2), loaded while the last MMAs run
         constexpr int EPI = S::EPI;
-        const bool first = (a.rka == 0.0);
+        const bool first = sa.first != 0;
         const double* qtile = a.qin + (size_t)k0 * 4 * Np;
         float resp[EPI];
         double q0v[EPI];
@@ -763,9 +763,9 @@ __global__ void __launch_bounds__(512, 1) euler_stage_split_pipe_kernel(SplitArg
         // ---- epilogue of t
         {
             const size_t base = (size_t)k0 * 4 * Np;
-            const float rka = (float)a.rka, dtf0 = (float)a.dt, rkb = (float)a.rkb;
+            const float rka = sa.rkaf, dtf0 = sa.dtf, rkb = sa.rkbf;
             const int nv = ne * 4 * Np;
-            if (a.mode == MODE_LSERK && !a.dtk) {
+            if (a.mode == MODE_LSERK && !sa.dtk32) {
 #pragma unroll
                 for (int j = 0; j < EPI; j++) {
                     const int i = tid + j * S::THREADS;
@@ -784,7 +784,7 @@ __global__ void __launch_bounds__(512, 1) euler_stage_split_pipe_kernel(SplitArg
                     const float R = sRS[i];
                     const double q0 = q0v[j];
                     const size_t idx = base + i;
-                    const float dtf = a.dtk ? (float)(a.dt * a.dtk[k0 + i / (4 * Np)]) : dtf0;
+                    const float dtf = sa.dtk32 ? dtf0 * sa.dtk32[k0 + i / (4 * Np)] : dtf0;
                     switch (a.mode) {
                         case MODE_RHS: a.rhs[idx] = (double)R; break;
                         case MODE_LSERK: {

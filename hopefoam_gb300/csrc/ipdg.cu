@@ -273,6 +273,161 @@ __global__ void __launch_bounds__(256, 4) ipdg_apply_kernel(IpdgArgs a, const do
     }
 }
 
+// Element-per-lane SIPG apply for the FP32 iterations of the PCG (N <= 5):
+// one thread holds one element's input offsets, its output rows and, face by
+// face, its neighbour's offsets in registers, and every reference table entry
+// is a kernel-parameter (constant-bank) operand of the FMA that uses it, so
+// the apply is FMAs plus the element's own loads.  The neighbour is read in
+// its relabelled numbering (the shared face is its face 0, traversed in this
+// element's direction: IpLaneTab::perm), so its face-0 tables serve every
+// face; the face coefficients fcl carry its gradients in that frame.  Same
+// operator, staging (p = z + beta p_old, offsets from the FP32 mirrors, FP64
+// offset differences across faces) and outputs as ipdg_apply_kernel; the sums
+// run in another order, so results agree to FP32 round-off.
+template <int N>
+__global__ void __launch_bounds__(128, N <= 3 ? 4 : (N == 4 ? 3 : 2)) ipdg_apply_lane_kernel(IpdgArgs a, const __grid_constant__ IpLaneTab<N> T,
+                                                             const double* __restrict__ u, double* __restrict__ y,
+                                                             ApplyPcg pc) {
+    using L = IpLaneTab<N>;
+    constexpr int Np = L::Np, Nfp = L::Nfp, Nfq = L::Nfq, NB = 3 * N;
+    double beta = 0.0;
+    if (pc.S) {
+        if (pc.S->done) return;
+        beta = pc.S->beta;
+    }
+    const bool has_beta = beta != 0.0;
+    const float betaf = (float)beta;
+    const double* __restrict__ p_old = pc.p_old;
+    const float* __restrict__ dzv = pc.dz;
+    const float* __restrict__ dpo = pc.dp_old;
+    const bool mass = a.mass_coef != 0.0;
+    double dot = 0.0;
+    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < a.K; k += gridDim.x * blockDim.x) {
+        const size_t base = (size_t)k * Np;
+        // own input: p = z + beta p_old (FP64, written out), FP32 offsets from the mirrors
+        float us[Np];
+        double pd0 = 0.0;
+#pragma unroll
+        for (int p = 0; p < Np; p++) {
+            const size_t i = base + p;
+            const double vp = has_beta ? fma(beta, p_old[i], u[i]) : u[i];
+            if (pc.p_new) pc.p_new[i] = vp;
+            if (p == 0) pd0 = vp;
+            float d = dzv[i];
+            if (has_beta) d = fmaf(betaf, dpo[i], d);
+            us[p] = d;
+            pc.dp_new[i] = d;
+        }
+        const float ub0 = (float)pd0;
+        // volume term J (c_rr Srr + c_rs Srs2 + c_ss Sss) u
+        const float* vc = a.o32.vc + (size_t)k * 3;
+        const float vrr = vc[0], vrs = vc[1], vss = vc[2];
+        float v[Np];
+#pragma unroll
+        for (int i = 0; i < Np; i++) {
+            float A = 0.f, B = 0.f, C = 0.f;
+#pragma unroll
+            for (int p = 0; p < Np; p++) {
+                A = fmaf(T.Srr[i][p], us[p], A);
+                B = fmaf(T.Srs2[i][p], us[p], B);
+                C = fmaf(T.Sss[i][p], us[p], C);
+            }
+            v[i] = vrr * A + vrs * B + vss * C;
+        }
+        if (mass) {
+            const float mc = (float)(a.mass_coef * a.J[k]);
+#pragma unroll
+            for (int i = 0; i < Np; i++) {
+                float m = T.mrow[i] * ub0;
+#pragma unroll
+                for (int p = 0; p < Np; p++) m = fmaf(T.Mr[i][p], us[p], m);
+                v[i] = fmaf(mc, m, v[i]);
+            }
+        }
+        // faces
+#pragma unroll
+        for (int f = 0; f < 3; f++) {
+            const int c = a.conn[(size_t)k * 3 + f];
+            const float2* fcp = reinterpret_cast<const float2*>(a.fcl + ((size_t)k * 3 + f) * kFaceCoef);
+            const float2 f01 = fcp[0], f23 = fcp[1], f45 = fcp[2];
+            const bool interior = c >= 0;
+            float nb[Np];
+            float dc = 0.f;
+            if (interior) {
+                const int nbk = c >> 3, pid = 2 * (c & 3) + ((c >> 2) & 1);
+                const size_t nbase = (size_t)nbk * Np;
+#pragma unroll
+                for (int p = 0; p < Np; p++) {
+                    const size_t j = nbase + T.perm[pid][p];
+                    float d = dzv[j];
+                    if (has_beta) d = fmaf(betaf, dpo[j], d);
+                    nb[p] = d;
+                }
+                dc = (float)(pd0 - (has_beta ? fma(beta, p_old[nbase], u[nbase]) : u[nbase]));
+            } else {
+#pragma unroll
+                for (int p = 0; p < Np; p++) nb[p] = 0.f;
+            }
+#pragma unroll
+            for (int g = 0; g < Nfq; g++) {
+                const int fg = f * Nfq + g;
+                float ur = 0.f, usd = 0.f, um = 0.f;
+#pragma unroll
+                for (int p = 0; p < Np; p++) {
+                    ur = fmaf(T.DrfT[p][fg], us[p], ur);
+                    usd = fmaf(T.DsfT[p][fg], us[p], usd);
+                }
+#pragma unroll
+                for (int j = 0; j < Nfp; j++) um = fmaf(T.If[g][j], us[(f * N + j) % NB], um);
+                const float dm = f01.x * ur + f01.y * usd;
+                float jump, dp;
+                if (interior) {
+                    float vr = 0.f, vs = 0.f, up = 0.f;
+#pragma unroll
+                    for (int p = 0; p < Np; p++) {
+                        vr = fmaf(T.DrfT[p][g], nb[p], vr);
+                        vs = fmaf(T.DsfT[p][g], nb[p], vs);
+                    }
+#pragma unroll
+                    for (int j = 0; j < Nfp; j++) up = fmaf(T.If[g][j], nb[j], up);
+                    dp = f23.x * vr + f23.y * vs;
+                    jump = (um - up) + dc;
+                } else {
+                    // Dirichlet face: u+ = -u-, so [u] = 2 u- (offset included)
+                    jump = 2.f * (um + ub0);
+                    dp = dm;
+                }
+                const float wJ = f45.y * T.fw[g];
+                const float sigma = 0.5f * (dm + dp);
+                const float cc2 = -0.5f * wJ * jump;
+                const float c1 = wJ * (f45.x * jump - sigma);
+                const float c2r = cc2 * f01.x, c2s = cc2 * f01.y;
+#pragma unroll
+                for (int i = 0; i < Np; i++) v[i] = fmaf(c2r, T.DrfT[i][fg], fmaf(c2s, T.DsfT[i][fg], v[i]));
+#pragma unroll
+                for (int d = 0; d <= N; d++) v[(f * N + d) % NB] = fmaf(c1, T.If[g][d], v[(f * N + d) % NB]);
+            }
+        }
+#pragma unroll
+        for (int i = 0; i < Np; i++) {
+            const double out = (double)v[i];
+            y[base + i] = out;
+            const double pv = pc.p_new ? pc.p_new[base + i] : (has_beta ? fma(beta, p_old[base + i], u[base + i])
+                                                                        : u[base + i]);
+            dot += out * pv;
+        }
+    }
+    if (pc.S) {
+        double val[1] = {dot}, tot[1];
+        if (grid_sum<1>(val, pc.part, gridDim.x, &pc.S->counter, tot) && threadIdx.x == 0) {
+            const double pap = tot[0];
+            pc.S->pap = pap;
+            pc.S->alpha = pc.S->rz / pap;
+            if (!(pap > 0.0) || !(pc.S->alpha == pc.S->alpha)) pc.S->done = 2;
+        }
+    }
+}
+
 // diagonal blocks S_kk (column j = S_kk e_j with neighbours zero), FP64
 template <int N>
 __global__ void ipdg_diag_kernel(IpdgArgs a, double* __restrict__ blocks) {
@@ -394,6 +549,24 @@ struct RowDims {
 __device__ __forceinline__ float fma_t(float a, float b, float c) { return fmaf(a, b, c); }
 __device__ __forceinline__ double fma_t(double a, double b, double c) { return fma(a, b, c); }
 
+// this thread's row of its element's inverse block (grouped layout), loaded
+// ahead of the residual it multiplies
+template <int NP, typename PT>
+__device__ __forceinline__ void bj_row_load(const PT* __restrict__ P, int grp, PT (&row)[NP]) {
+    constexpr int EBNP = RowDims<NP>::EB * NP;
+    const PT* col = P + (size_t)grp * NP * EBNP + threadIdx.x;
+#pragma unroll
+    for (int j = 0; j < NP; j++) row[j] = __ldg(col + j * EBNP);
+}
+
+template <int NP, typename PT, typename RT>
+__device__ __forceinline__ double bj_row_apply(const PT (&row)[NP], const RT* rs) {
+    PT s = 0;
+#pragma unroll
+    for (int j = 0; j < NP; j++) s = fma_t(row[j], (PT)rs[j], s);
+    return (double)s;
+}
+
 template <int NP, typename PT, typename RT>
 __device__ __forceinline__ double bj_rowg(const PT* __restrict__ P, const RT* rs, int grp) {
     constexpr int EBNP = RowDims<NP>::EB * NP;
@@ -494,6 +667,9 @@ __global__ void __launch_bounds__(RowDims<NP>::THREADS) pcg_update_kernel(PcgVec
         const bool act = e < EB && k < K;
         const size_t idx = (size_t)k * NP + i;
         double ri = 0, z = 0;
+        // the FP32 block row is loaded with the vectors (one memory phase per group)
+        float prow[NP];
+        if (act && !v.P64) bj_row_load<NP>(v.P32, grp, prow);
         if (act) {
             v.x[idx] += alpha * p[idx];
             ri = v.r[idx] - alpha * v.Ap[idx];
@@ -503,7 +679,7 @@ __global__ void __launch_bounds__(RowDims<NP>::THREADS) pcg_update_kernel(PcgVec
         }
         __syncthreads();
         if (act) {
-            z = v.P64 ? bj_rowg<NP>(v.P64, rs[e], grp) : bj_rowg<NP>(v.P32, rs32[e], grp);
+            z = v.P64 ? bj_rowg<NP>(v.P64, rs[e], grp) : bj_row_apply<NP>(prow, rs32[e]);
             rr += ri * ri;
             if (v.r32) v.r32[idx] = rs32[e][i];
             if (v.zb) {
@@ -602,6 +778,14 @@ template <int N>
 static cudaError_t apply_n(const IpdgArgs& a, bool fp32, const double* u, double* y, const ApplyPcg& pc,
                            cudaStream_t s) {
     using D = IpDims<N>;
+    if constexpr (N <= 5) {
+        if (fp32 && pc.dz && pc.S && a.lane_tab && a.fcl) {
+            const int grid = std::max(1, std::min((a.K + 127) / 128, pcg_max_grid(a.K, N, a.sms)));
+            ipdg_apply_lane_kernel<N>
+                <<<grid, 128, 0, s>>>(a, *static_cast<const IpLaneTab<N>*>(a.lane_tab), u, y, pc);
+            return cudaGetLastError();
+        }
+    }
     const int grid = apply_grid<N>(a);
     if (fp32) ipdg_apply_kernel<N, float><<<grid, D::THREADS, 0, s>>>(a, u, y, pc);
     else ipdg_apply_kernel<N, double><<<grid, D::THREADS, 0, s>>>(a, u, y, pc);

@@ -34,9 +34,33 @@ struct IpdgArgs {
     double mass_coef;    // S + mass_coef M (Helmholtz form); 0: the Laplacian alone
     IpdgOps<double> o64;
     IpdgOps<float> o32;
+    // element-per-lane apply (N <= 5, FP32 PCG iterations): the face
+    // coefficients with each neighbour's gradient terms taken in its
+    // relabelled frame (face shared with this element = its face 0, Gauss
+    // points in this element's order), and the host copy of the reference
+    // tables passed to that kernel by value (IpLaneTab<N>; null: not built)
+    const float* fcl;
+    const void* lane_tab;
 };
 
 constexpr int kFaceCoef = 6;
+
+// reference tables of the element-per-lane apply, FP32, ring order; passed
+// as a kernel parameter so that every table read is a constant-bank operand
+template <int N>
+struct IpLaneTab {
+    static constexpr int Np = (N + 1) * (N + 2) / 2, Nfp = N + 1, Nfq = N + 2, NF = 3 * Nfq;
+    float DrfT[Np][NF];  // d/dr of basis function p at face Gauss point fg
+    float DsfT[Np][NF];
+    float If[Nfq][Nfp];
+    float fw[Nfq];
+    float Srr[Np][Np], Srs2[Np][Np], Sss[Np][Np];
+    float Mr[Np][Np];
+    float mrow[Np];
+    // ring position, in the neighbour's own numbering, of the node at ring
+    // position p of its relabelled numbering; index 2 fn + rot
+    unsigned char perm[6][Np];
+};
 
 // device-side CG state; the kernels read and update it, the host reads it
 // every few iterations

@@ -81,6 +81,18 @@ __device__ __forceinline__ const IpdgOps<float>& ops_of<float>(const IpdgArgs& a
 // Persistent CTAs (a few per SM) stride over the tiles; in the PCG each CTA's
 // share of p.Ap enters one deterministic grid-wide sum whose last CTA also
 // forms alpha (one arrival per CTA, not per tile).
+struct ApplyPcg {
+    const double* p_old;  // previous search direction (read when beta != 0)
+    double* p_new;        // this direction, written for each element's rows
+    PcgScalars* S;        // beta in, pap / alpha out; null outside the PCG
+    double* part;
+    // FP32 offset mirrors (element value minus the element's first-node
+    // value) of z and of the search directions; used by the FP32 apply in the
+    // PCG so that staging needs no FP64 arithmetic per node
+    const float* dz;
+    const float* dp_old;
+    float* dp_new;
+};
 
 template <int N, typename T>
 __global__ void __launch_bounds__(256, 4) ipdg_apply_kernel(IpdgArgs a, const double* __restrict__ u,
@@ -766,12 +778,8 @@ template <int N>
 static cudaError_t apply_n(const IpdgArgs& a, bool fp32, const double* u, double* y, const ApplyPcg& pc,
                            cudaStream_t s) {
     using D = IpDims<N>;
-    if constexpr (N <= 4) {
-        if (fp32 && pc.dz && pc.S && a.tc_b && a.fcl && a.apply_variant == IPDG_APPLY_TC)
-            return launch_ipdg_apply_tc(a, u, y, pc, s);
-    }
     if constexpr (N <= 5) {
-        if (fp32 && pc.dz && pc.S && a.lane_tab && a.fcl && a.apply_variant != IPDG_APPLY_TILE) {
+        if (fp32 && pc.dz && pc.S && a.lane_tab && a.fcl) {
             const int grid = std::max(1, std::min((a.K + 127) / 128, pcg_max_grid(a.K, N, a.sms)));
             ipdg_apply_lane_kernel<N>
                 <<<grid, 128, 0, s>>>(a, *static_cast<const IpLaneTab<N>*>(a.lane_tab), u, y, pc);

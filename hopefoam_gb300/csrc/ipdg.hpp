@@ -3,8 +3,6 @@
 
 #include <cuda_runtime.h>
 
-#include <vector>
-
 namespace dgk {
 
 // reference operators in the arithmetic type of the apply (ring order)
@@ -43,18 +41,7 @@ struct IpdgArgs {
     // tables passed to that kernel by value (IpLaneTab<N>; null: not built)
     const float* fcl;
     const void* lane_tab;
-    // the neighbour relabelling of the element-per-lane and tensor-core
-    // applies: ring position, in the neighbour's own numbering, of the node at
-    // ring position p of its relabelled numbering; index 2 fn + rot (N <= 4)
-    unsigned char nperm[6][16];
-    const float* tc_b;   // tensor-core apply: B1 | B2 | B3 operand images (hi | lo each); null: not built
-    int* tc_status;      // its bounded-wait timeout flag
-    int apply_variant;   // IPDG_APPLY_* for the FP32 PCG iterations
 };
-
-// the SIPG apply used by the FP32 PCG iterations: tensor cores (N <= 4),
-// element per lane (N <= 5), or the tiled SIMT kernel (every order)
-enum { IPDG_APPLY_TC = 0, IPDG_APPLY_LANE = 1, IPDG_APPLY_TILE = 2 };
 
 constexpr int kFaceCoef = 6;
 
@@ -117,29 +104,6 @@ int pcg_max_grid(int K, int N, int sms);
 // of the padded storage, and the conversion from row-major blocks
 size_t grouped_blocks_size(int K, int Np);
 cudaError_t launch_group_blocks(const IpdgArgs& a, const double* blocks, double* P64, float* P32, cudaStream_t s);
-
-// PCG hooks of the apply: p = z + beta p_old formed in the apply, p.Ap and
-// alpha on the device (see ipdg.cu)
-struct ApplyPcg {
-    const double* p_old;  // previous search direction (read when beta != 0)
-    double* p_new;        // this direction, written for each element's rows
-    PcgScalars* S;        // beta in, pap / alpha out; null outside the PCG
-    double* part;
-    // FP32 offset mirrors (element value minus the element's first-node
-    // value) of z and of the search directions; used by the FP32 apply in the
-    // PCG so that staging needs no FP64 arithmetic per node
-    const float* dz;
-    const float* dp_old;
-    float* dp_new;
-};
-
-cudaError_t launch_ipdg_apply_tc(const IpdgArgs& a, const double* u, double* y, const ApplyPcg& pc, cudaStream_t s);
-cudaError_t setup_ipdg_tc(int N);
-// tensor-core apply operand images for order N (empty when N > 4)
-std::vector<float> ipdg_tc_images(int N, const std::vector<double>& DrfT, const std::vector<double>& DsfT,
-                                  const std::vector<double>& If, const std::vector<double>& Srr,
-                                  const std::vector<double>& Srs2, const std::vector<double>& Sss,
-                                  const std::vector<double>& Mr);
 
 // y = S u (standalone)
 cudaError_t launch_ipdg_apply(const IpdgArgs& a, bool fp32, const double* u, double* y, cudaStream_t s);

@@ -1,7 +1,6 @@
 // ipdg_api.cu -- C ABI of the SIPG pressure operator and its PCG solve.
 #include <algorithm>
 #include <cmath>
-#include <cstdlib>
 #include <cstring>
 #include <string>
 #include <type_traits>
@@ -677,31 +676,6 @@ int dg_ipdg_setup(dg_ctx* c, double tau_coef) {
     a.o32 = o32;
     a.fcl = s->d_fcl;
     a.lane_tab = s->lane_tab.empty() ? nullptr : s->lane_tab.data();
-    // neighbour relabelling shared by the element-per-lane and tensor-core applies
-    memset(a.nperm, 0, sizeof(a.nperm));
-    if (Np <= 16)
-        for (int fn = 0; fn < 3; fn++)
-            for (int rot = 0; rot < 2; rot++) {
-                int sig[3];
-                neighbour_relabelling(fn, rot, sig);
-                const std::vector<int> perm = relabel_perm(c->ops, sig);
-                for (int p = 0; p < Np; p++) a.nperm[2 * fn + rot][p] = (unsigned char)perm[p];
-            }
-    a.tc_b = nullptr;
-    a.tc_status = s->d_status;
-    if (c->N <= 4) {
-        const std::vector<float> img = ipdg_tc_images(c->N, DrfT, DsfT, Ifh, Srr, Srs2, Sss, Mr);
-        float* d = nullptr;
-        if (iupload(c, s, &d, img)) return DG_ERR_NOMEM;
-        if (setup_ipdg_tc(c->N) != cudaSuccess) return ifail(c, DG_ERR_CUDA, "tensor-core apply setup");
-        a.tc_b = d;
-    }
-    // DGCU_IPDG_APPLY=tc|lane|tile selects the FP32 apply of the PCG (A/B measurements)
-    a.apply_variant = IPDG_APPLY_TC;
-    if (const char* v = getenv("DGCU_IPDG_APPLY")) {
-        if (strcmp(v, "lane") == 0) a.apply_variant = IPDG_APPLY_LANE;
-        if (strcmp(v, "tile") == 0) a.apply_variant = IPDG_APPLY_TILE;
-    }
     rc = build_blocks(c);
     if (rc) return rc;
     s->ready = true;

@@ -568,21 +568,23 @@ __global__ void __launch_bounds__(512, 1) euler_stage_split_pipe_kernel(SplitArg
                 for (int v = 0; v < 4; v++) fr[v] = fs[v] = 0.f;
             }
         };
+        // this thread's slots in a chunk operand: rows g2row(my_e, v) are one
+        // 8-row group apart per v (KC * 8 floats), the Fs columns CH / 4 core
+        // matrices after the Fr ones, so every store is a fixed offset from one base
+        float* const sAC0 =
+            reinterpret_cast<float*>(smem + D::OFF_AC) + (umma::kmajor_offset(g2row(my_e, 0), sub * 4 + my_v, KC) >> 2);
         auto store_chunk = [&](int buf, const float* fr, const float* fs) {
-            float* sAC = reinterpret_cast<float*>(smem + D::OFF_AC + buf * STRIDE_AC);
-            const int gl = sub * 4 + my_v;
+            constexpr int VSTR = KC * 8, FSO = CH * 8, LO = LO_AC / 4;
+            float* const b = sAC0 + buf * (STRIDE_AC / 4);
 #pragma unroll
             for (int v = 0; v < 4; v++) {
-                const int r = g2row(my_e, v);
                 float hi, lo;
                 umma::split_tf32(fr[v], hi, lo);
-                uint32_t off = umma::kmajor_offset(r, gl, KC) >> 2;
-                sAC[off] = hi;
-                sAC[off + LO_AC / 4] = lo;
+                b[v * VSTR] = hi;
+                b[v * VSTR + LO] = lo;
                 umma::split_tf32(fs[v], hi, lo);
-                off = umma::kmajor_offset(r, CH + gl, KC) >> 2;
-                sAC[off] = hi;
-                sAC[off + LO_AC / 4] = lo;
+                b[v * VSTR + FSO] = hi;
+                b[v * VSTR + FSO + LO] = lo;
             }
         };
         auto issue_mma = [&](int ch, int buf) {

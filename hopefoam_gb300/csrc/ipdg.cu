@@ -301,23 +301,36 @@ __global__ void __launch_bounds__(128, N <= 3 ? 4 : (N == 4 ? 3 : 2)) ipdg_apply
     const float* __restrict__ dzv = pc.dz;
     const float* __restrict__ dpo = pc.dp_old;
     const bool mass = a.mass_coef != 0.0;
+    double* __restrict__ p_new = pc.p_new;
+    float* __restrict__ dp_new = pc.dp_new;
+    // the tile's own values pass through shared memory so that every global
+    // access of the element's own rows is coalesced: p (FP64) for the first
+    // node and p.Ap, the FP32 offsets in, the outputs out
+    __shared__ double sp[128 * Np];
+    __shared__ float sd[128 * Np];
     double dot = 0.0;
-    for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < a.K; k += gridDim.x * blockDim.x) {
-        const size_t base = (size_t)k * Np;
-        // own input: p = z + beta p_old (FP64, written out), FP32 offsets from the mirrors
-        float us[Np];
-        double pd0 = 0.0;
-#pragma unroll
-        for (int p = 0; p < Np; p++) {
-            const size_t i = base + p;
+    const int ntiles = (a.K + 127) / 128;
+    for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        const int k0 = tile * 128, ne = min(128, a.K - k0);
+        const size_t g0 = (size_t)k0 * Np;
+        for (int t = threadIdx.x; t < ne * Np; t += 128) {
+            const size_t i = g0 + t;
             const double vp = has_beta ? fma(beta, p_old[i], u[i]) : u[i];
-            if (pc.p_new) pc.p_new[i] = vp;
-            if (p == 0) pd0 = vp;
+            if (p_new) p_new[i] = vp;
+            sp[t] = vp;
             float d = dzv[i];
             if (has_beta) d = fmaf(betaf, dpo[i], d);
-            us[p] = d;
-            pc.dp_new[i] = d;
+            dp_new[i] = d;
+            sd[t] = d;
         }
+        __syncthreads();
+        const int e = threadIdx.x;
+        const int k = k0 + e;
+        if (e < ne) {
+        float us[Np];
+#pragma unroll
+        for (int p = 0; p < Np; p++) us[p] = sd[e * Np + p];
+        const double pd0 = sp[e * Np];
         const float ub0 = (float)pd0;
         // volume term J (c_rr Srr + c_rs Srs2 + c_ss Sss) u
         const float* vc = a.o32.vc + (size_t)k * 3;
@@ -408,14 +421,17 @@ __global__ void __launch_bounds__(128, N <= 3 ? 4 : (N == 4 ? 3 : 2)) ipdg_apply
                 for (int d = 0; d <= N; d++) v[(f * N + d) % NB] = fmaf(c1, T.If[g][d], v[(f * N + d) % NB]);
             }
         }
+        // this element's outputs over its own input row (read only by this thread)
 #pragma unroll
-        for (int i = 0; i < Np; i++) {
-            const double out = (double)v[i];
-            y[base + i] = out;
-            const double pv = pc.p_new ? pc.p_new[base + i] : (has_beta ? fma(beta, p_old[base + i], u[base + i])
-                                                                        : u[base + i]);
-            dot += out * pv;
+        for (int i = 0; i < Np; i++) sd[e * Np + i] = v[i];
         }
+        __syncthreads();
+        for (int t = threadIdx.x; t < ne * Np; t += 128) {
+            const double out = (double)sd[t];
+            y[g0 + t] = out;
+            dot += out * sp[t];
+        }
+        __syncthreads();  // the next tile rewrites sp and sd
     }
     if (pc.S) {
         double val[1] = {dot}, tot[1];
@@ -540,11 +556,32 @@ __device__ __forceinline__ void block_sum1(double a, double* oa) {
 // g and column j the EB x Np entries (element, row) are contiguous,
 //   Pg[((g Np + j) EB + e) Np + i] = P_{g EB + e}[i][j],
 // so the CTA's loads for one column form a single contiguous read.
+//
+// Up to Np = 32 (N <= 6) an element's rows never straddle a warp: each warp
+// holds EW = 32 / Np whole elements (WA), so the rows of an element exchange
+// their values by warp shuffles and the kernels need no CTA barrier per
+// group.  N = 7 (Np = 36) keeps one shared-memory exchange per group.
 template <int NP>
 struct RowDims {
-    static constexpr int EB = 256 / NP;
-    static constexpr int THREADS = (EB * NP + 31) / 32 * 32;  // extra lanes idle but join the reductions
+    static constexpr bool WA = NP <= 32;
+    static constexpr int EW = WA ? 32 / NP : 0;  // elements per warp
+    static constexpr int EB = WA ? 8 * EW : 256 / NP;
+    static constexpr int THREADS = WA ? 256 : (EB * NP + 31) / 32 * 32;  // extra lanes idle but join the reductions
 };
+
+// this thread's (element in the group, row) and its slot in the grouped layout
+template <int NP>
+__device__ __forceinline__ void row_of(int& e, int& i) {
+    if constexpr (RowDims<NP>::WA) {
+        const int lane = threadIdx.x & 31;
+        e = (threadIdx.x >> 5) * RowDims<NP>::EW + lane / NP;
+        i = lane % NP;
+        if (lane >= RowDims<NP>::EW * NP) e = RowDims<NP>::EB;  // idle lane
+    } else {
+        e = threadIdx.x / NP;
+        i = threadIdx.x - e * NP;
+    }
+}
 
 __device__ __forceinline__ float fma_t(float a, float b, float c) { return fmaf(a, b, c); }
 __device__ __forceinline__ double fma_t(double a, double b, double c) { return fma(a, b, c); }
@@ -554,7 +591,9 @@ __device__ __forceinline__ double fma_t(double a, double b, double c) { return f
 template <int NP, typename PT>
 __device__ __forceinline__ void bj_row_load(const PT* __restrict__ P, int grp, PT (&row)[NP]) {
     constexpr int EBNP = RowDims<NP>::EB * NP;
-    const PT* col = P + (size_t)grp * NP * EBNP + threadIdx.x;
+    int e, i;
+    row_of<NP>(e, i);
+    const PT* col = P + (size_t)grp * NP * EBNP + e * NP + i;
 #pragma unroll
     for (int j = 0; j < NP; j++) row[j] = __ldg(col + j * EBNP);
 }
@@ -570,7 +609,9 @@ __device__ __forceinline__ double bj_row_apply(const PT (&row)[NP], const RT* rs
 template <int NP, typename PT, typename RT>
 __device__ __forceinline__ double bj_rowg(const PT* __restrict__ P, const RT* rs, int grp) {
     constexpr int EBNP = RowDims<NP>::EB * NP;
-    const PT* col = P + (size_t)grp * NP * EBNP + threadIdx.x;
+    int e, i;
+    row_of<NP>(e, i);
+    const PT* col = P + (size_t)grp * NP * EBNP + e * NP + i;
     PT s = 0;
 #pragma unroll
     for (int j = 0; j < NP; j++) s = fma_t(col[j * EBNP], (PT)rs[j], s);
@@ -583,39 +624,83 @@ __device__ __forceinline__ double bj_rowg(const PT* __restrict__ P, const RT* rs
 template <int NP>
 __global__ void __launch_bounds__(RowDims<NP>::THREADS) pcg_init_kernel(PcgVecs v, int K, int mode) {
     constexpr int EB = RowDims<NP>::EB;
-    __shared__ double rs[EB][NP];
-    __shared__ float rs32[EB][NP];
-    __shared__ double zs0[EB];
-    const int e = threadIdx.x / NP, i = threadIdx.x - e * NP;
+    int e, i;
+    row_of<NP>(e, i);
     const int ngroups = (K + EB - 1) / EB;
     double rz = 0, rr = 0;
-    for (int grp = blockIdx.x; grp < ngroups; grp += gridDim.x) {
-        const int k = grp * EB + e;
-        const bool act = e < EB && k < K;
-        const size_t idx = (size_t)k * NP + i;
-        double ri = 0, z = 0;
-        if (act) {
-            ri = v.r[idx];
-            rs[e][i] = ri;
-            rs32[e][i] = (float)ri;
-        }
-        __syncthreads();
-        if (act) {
-            z = v.P64 ? bj_rowg<NP>(v.P64, rs[e], grp) : bj_rowg<NP>(v.P32, rs32[e], grp);
-            if (v.zb) v.zb[idx] = z;
-            else {
-                v.z[idx] = z;
-                rz += ri * z;
+    if constexpr (RowDims<NP>::WA) {
+        const int lb = (threadIdx.x & 31) - i;  // lane of the element's row 0
+        for (int grp = blockIdx.x; grp < ngroups; grp += gridDim.x) {
+            const int k = grp * EB + e;
+            const bool act = e < EB && k < K;
+            const size_t idx = (size_t)k * NP + i;
+            const double ri = act ? v.r[idx] : 0.0;
+            const float r32 = (float)ri;
+            double z = 0;
+            if (v.P64) {
+                double s = 0;
+                const double* col = v.P64 + (size_t)grp * NP * EB * NP + e * NP + i;
+#pragma unroll
+                for (int j = 0; j < NP; j++) {
+                    const double rj = __shfl_sync(0xffffffffu, ri, lb + j);
+                    if (act) s = fma(__ldg(col + (size_t)j * EB * NP), rj, s);
+                }
+                z = s;
+            } else {
+                float prow[NP];
+                if (act) bj_row_load<NP>(v.P32, grp, prow);
+                float s = 0.f;
+#pragma unroll
+                for (int j = 0; j < NP; j++) {
+                    const float rj = __shfl_sync(0xffffffffu, r32, lb + j);
+                    if (act) s = fmaf(prow[j], rj, s);
+                }
+                z = (double)s;
             }
-            if (i == 0) zs0[e] = z;
-            if (v.r32) v.r32[idx] = rs32[e][i];
-            rr += ri * ri;
+            const double z0 = __shfl_sync(0xffffffffu, z, lb);
+            if (act) {
+                if (v.zb) v.zb[idx] = z;
+                else {
+                    v.z[idx] = z;
+                    rz += ri * z;
+                }
+                if (v.r32) v.r32[idx] = r32;
+                if (v.dz) v.dz[idx] = (float)(z - z0);  // learned mode: the mirror of P r
+                rr += ri * ri;
+            }
         }
-        if (v.dz) {  // learned mode: the mirror of P r, completed by the learned kernel
+    } else {
+        __shared__ double rs[EB][NP];
+        __shared__ float rs32[EB][NP];
+        __shared__ double zs0[EB];
+        for (int grp = blockIdx.x; grp < ngroups; grp += gridDim.x) {
+            const int k = grp * EB + e;
+            const bool act = e < EB && k < K;
+            const size_t idx = (size_t)k * NP + i;
+            double ri = 0, z = 0;
+            if (act) {
+                ri = v.r[idx];
+                rs[e][i] = ri;
+                rs32[e][i] = (float)ri;
+            }
             __syncthreads();
-            if (act) v.dz[idx] = (float)(z - zs0[e]);
+            if (act) {
+                z = v.P64 ? bj_rowg<NP>(v.P64, rs[e], grp) : bj_rowg<NP>(v.P32, rs32[e], grp);
+                if (v.zb) v.zb[idx] = z;
+                else {
+                    v.z[idx] = z;
+                    rz += ri * z;
+                }
+                if (i == 0) zs0[e] = z;
+                if (v.r32) v.r32[idx] = rs32[e][i];
+                rr += ri * ri;
+            }
+            if (v.dz) {  // learned mode: the mirror of P r, completed by the learned kernel
+                __syncthreads();
+                if (act) v.dz[idx] = (float)(z - zs0[e]);
+            }
+            __syncthreads();
         }
-        __syncthreads();
     }
     double val[2] = {rz, rr}, tot[2];
     if (grid_sum<2>(val, v.part, gridDim.x, &v.S->counter, tot) && threadIdx.x == 0) {
@@ -634,16 +719,35 @@ __global__ void __launch_bounds__(RowDims<NP>::THREADS) bj_kernel(const float* _
                                                                   const double* __restrict__ r,
                                                                   double* __restrict__ z, int K) {
     constexpr int EB = RowDims<NP>::EB;
-    __shared__ float rs32[EB][NP];
-    const int e = threadIdx.x / NP, i = threadIdx.x - e * NP;
+    int e, i;
+    row_of<NP>(e, i);
     const int ngroups = (K + EB - 1) / EB;
-    for (int grp = blockIdx.x; grp < ngroups; grp += gridDim.x) {
-        const int k = grp * EB + e;
-        const bool act = e < EB && k < K;
-        if (act) rs32[e][i] = (float)r[(size_t)k * NP + i];
-        __syncthreads();
-        if (act) z[(size_t)k * NP + i] = bj_rowg<NP>(P32, rs32[e], grp);
-        __syncthreads();
+    if constexpr (RowDims<NP>::WA) {
+        const int lb = (threadIdx.x & 31) - i;
+        for (int grp = blockIdx.x; grp < ngroups; grp += gridDim.x) {
+            const int k = grp * EB + e;
+            const bool act = e < EB && k < K;
+            const float r32 = act ? (float)r[(size_t)k * NP + i] : 0.f;
+            float prow[NP];
+            if (act) bj_row_load<NP>(P32, grp, prow);
+            float s = 0.f;
+#pragma unroll
+            for (int j = 0; j < NP; j++) {
+                const float rj = __shfl_sync(0xffffffffu, r32, lb + j);
+                if (act) s = fmaf(prow[j], rj, s);
+            }
+            if (act) z[(size_t)k * NP + i] = (double)s;
+        }
+    } else {
+        __shared__ float rs32[EB][NP];
+        for (int grp = blockIdx.x; grp < ngroups; grp += gridDim.x) {
+            const int k = grp * EB + e;
+            const bool act = e < EB && k < K;
+            if (act) rs32[e][i] = (float)r[(size_t)k * NP + i];
+            __syncthreads();
+            if (act) z[(size_t)k * NP + i] = bj_rowg<NP>(P32, rs32[e], grp);
+            __syncthreads();
+        }
     }
 }
 
@@ -654,52 +758,99 @@ template <int NP>
 __global__ void __launch_bounds__(RowDims<NP>::THREADS) pcg_update_kernel(PcgVecs v, int K, int parity) {
     constexpr int EB = RowDims<NP>::EB;
     if (v.S->done) return;
-    __shared__ double rs[EB][NP];
-    __shared__ float rs32[EB][NP];
-    __shared__ double zs0[EB];
     const double alpha = v.S->alpha;
     const double* __restrict__ p = v.p[parity ^ 1];
-    const int e = threadIdx.x / NP, i = threadIdx.x - e * NP;
+    int e, i;
+    row_of<NP>(e, i);
     const int ngroups = (K + EB - 1) / EB;
     double rz = 0, rr = 0, rzo = 0;
-    for (int grp = blockIdx.x; grp < ngroups; grp += gridDim.x) {
-        const int k = grp * EB + e;
-        const bool act = e < EB && k < K;
-        const size_t idx = (size_t)k * NP + i;
-        double ri = 0, z = 0;
-        // the FP32 block row is loaded with the vectors (one memory phase per group)
-        float prow[NP];
-        if (act && !v.P64) bj_row_load<NP>(v.P32, grp, prow);
-        if (act) {
-            v.x[idx] += alpha * p[idx];
-            ri = v.r[idx] - alpha * v.Ap[idx];
-            v.r[idx] = ri;
-            if (v.P64) rs[e][i] = ri;
-            if (!v.P64 || v.r32) rs32[e][i] = (float)ri;
-        }
-        __syncthreads();
-        if (act) {
-            z = v.P64 ? bj_rowg<NP>(v.P64, rs[e], grp) : bj_row_apply<NP>(prow, rs32[e]);
-            rr += ri * ri;
-            if (v.r32) v.r32[idx] = rs32[e][i];
-            if (v.zb) {
-                v.zb[idx] = z;  // the learned kernel forms z and finishes the iteration
-                if (i == 0) zs0[e] = z;
+    if constexpr (RowDims<NP>::WA) {
+        // no CTA barrier: the element's residual reaches its rows by shuffles
+        const int lb = (threadIdx.x & 31) - i;
+        for (int grp = blockIdx.x; grp < ngroups; grp += gridDim.x) {
+            const int k = grp * EB + e;
+            const bool act = e < EB && k < K;
+            const size_t idx = (size_t)k * NP + i;
+            // the block row is loaded with the vectors (one memory phase per group)
+            float prow[NP];
+            if (act && !v.P64) bj_row_load<NP>(v.P32, grp, prow);
+            double ri = 0;
+            if (act) {
+                v.x[idx] += alpha * p[idx];
+                ri = v.r[idx] - alpha * v.Ap[idx];
+                v.r[idx] = ri;
+            }
+            const float r32 = (float)ri;
+            double z = 0;
+            if (v.P64) {
+                double s = 0;
+                const double* col = v.P64 + (size_t)grp * NP * EB * NP + e * NP + i;
+#pragma unroll
+                for (int j = 0; j < NP; j++) {
+                    const double rj = __shfl_sync(0xffffffffu, ri, lb + j);
+                    if (act) s = fma(__ldg(col + (size_t)j * EB * NP), rj, s);
+                }
+                z = s;
             } else {
-                // block Jacobi is a fixed linear preconditioner: the standard
-                // (Fletcher-Reeves) beta needs no r.z_old, and skipping the
-                // z_old read measured 40% faster per iteration at equal
-                // iteration counts
-                v.z[idx] = z;
-                rz += ri * z;
-                if (i == 0) zs0[e] = z;
+                float s = 0.f;
+#pragma unroll
+                for (int j = 0; j < NP; j++) {
+                    const float rj = __shfl_sync(0xffffffffu, r32, lb + j);
+                    if (act) s = fmaf(prow[j], rj, s);
+                }
+                z = (double)s;
+            }
+            const double z0 = __shfl_sync(0xffffffffu, z, lb);
+            if (act) {
+                rr += ri * ri;
+                if (v.r32) v.r32[idx] = r32;
+                if (v.zb) {
+                    v.zb[idx] = z;  // the learned kernel forms z and finishes the iteration
+                } else {
+                    // block Jacobi is a fixed linear preconditioner: the standard
+                    // (Fletcher-Reeves) beta needs no r.z_old
+                    v.z[idx] = z;
+                    rz += ri * z;
+                }
+                if (v.dz) v.dz[idx] = (float)(z - z0);  // learned mode: the mirror of P r
             }
         }
-        if (v.dz) {  // learned mode: the mirror of P r, completed by the learned kernel
+    } else {
+        __shared__ double rs[EB][NP];
+        __shared__ float rs32[EB][NP];
+        __shared__ double zs0[EB];
+        for (int grp = blockIdx.x; grp < ngroups; grp += gridDim.x) {
+            const int k = grp * EB + e;
+            const bool act = e < EB && k < K;
+            const size_t idx = (size_t)k * NP + i;
+            double ri = 0, z = 0;
+            float prow[NP];
+            if (act && !v.P64) bj_row_load<NP>(v.P32, grp, prow);
+            if (act) {
+                v.x[idx] += alpha * p[idx];
+                ri = v.r[idx] - alpha * v.Ap[idx];
+                v.r[idx] = ri;
+                if (v.P64) rs[e][i] = ri;
+                if (!v.P64 || v.r32) rs32[e][i] = (float)ri;
+            }
             __syncthreads();
-            if (act) v.dz[idx] = (float)(z - zs0[e]);
+            if (act) {
+                z = v.P64 ? bj_rowg<NP>(v.P64, rs[e], grp) : bj_row_apply<NP>(prow, rs32[e]);
+                rr += ri * ri;
+                if (v.r32) v.r32[idx] = rs32[e][i];
+                if (v.zb) v.zb[idx] = z;
+                else {
+                    v.z[idx] = z;
+                    rz += ri * z;
+                }
+                if (i == 0) zs0[e] = z;
+            }
+            if (v.dz) {
+                __syncthreads();
+                if (act) v.dz[idx] = (float)(z - zs0[e]);
+            }
+            __syncthreads();
         }
-        __syncthreads();
     }
     double val[3] = {rz, rr, rzo}, tot[3];
     if (grid_sum<3>(val, v.part, gridDim.x, &v.S->counter, tot) && threadIdx.x == 0) {

@@ -257,6 +257,7 @@ def main():
     ap.add_argument("--no-ins", action="store_true", help="skip the incompressible (Chorin) step benchmark")
     ap.add_argument("--c5-study", action="store_true", help="500-step shear-layer accuracy study (reduced size)")
     ap.add_argument("--c5-study-n", type=int, default=128)
+    ap.add_argument("--c5-study-only", action="store_true", help="run only the shear-layer accuracy study and exit")
     ap.add_argument("--profile-target", default=None, choices=sorted(PROFILE_TARGETS),
                     help="run one workload of the line alone (the command the ncu summaries profile) and exit")
     ap.add_argument("--profile-size", default="full", choices=["full", "small"],
@@ -267,6 +268,12 @@ def main():
         return run_reference(args)
     if args.profile_target:
         return profile_target(args.profile_target, args.profile_size == "small")
+    if args.c5_study_only:
+        import torch
+
+        torch.cuda.set_device(0)
+        print(json.dumps({"c5_study": c5_study(n=args.c5_study_n)}))
+        return
 
     import torch
 

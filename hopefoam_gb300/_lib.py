@@ -39,7 +39,8 @@ class Info(ctypes.Structure):
 
 
 class BatchTuning(ctypes.Structure):
-    _fields_ = [("concurrent", ctypes.c_int32), ("ms_sequential", ctypes.c_double), ("ms_concurrent", ctypes.c_double)]
+    _fields_ = [("concurrent", ctypes.c_int32), ("ms_sequential", ctypes.c_double), ("ms_concurrent", ctypes.c_double),
+                ("ms_fused", ctypes.c_double)]
 
 
 class SolveStats(ctypes.Structure):
@@ -115,6 +116,7 @@ SIGNATURES = {
     "dg_batch_tune": (ctypes.c_int, [_vp, ctypes.c_double, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                      ctypes.POINTER(BatchTuning)]),
     "dg_batch_get_shape": (ctypes.c_int, [_vp, ctypes.c_int, _ip, _ip, _ip]),
+    "dg_batch_set_schedule": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int]),
     "dg_batch_run": (ctypes.c_int, [_vp, ctypes.c_double, ctypes.c_int, ctypes.c_int, ctypes.c_int, _dp]),
 }
 DG_NOALLOC_MAX_VALUES = 524288

@@ -108,7 +108,12 @@ class EulerBatch:
                                                     ctypes.byref(conc)))
             shapes.append(dict(order=self.groups[g]["order"], ctas_per_sm=cps.value, sm_budget=smb.value))
         return dict(concurrent=t.concurrent, ms_sequential=t.ms_sequential, ms_concurrent=t.ms_concurrent,
-                    groups=shapes)
+                    ms_fused=t.ms_fused, groups=shapes)
+
+    def set_schedule(self, schedule, precision=L.DG_PREC_SPLIT):
+        """0: groups one after another, 1: side by side on streams, 2: one
+        mixed-order launch per stage."""
+        self._check(self.lib.dg_batch_set_schedule(self.h, int(schedule), int(precision)))
 
     def run(self, nsteps, flux=L.DG_FLUX_LF, precision=L.DG_PREC_SPLIT):
         """Advances every case nsteps LSERK4 steps (one graph launch);

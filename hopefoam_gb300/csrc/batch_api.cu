@@ -12,6 +12,7 @@
 
 #include "../../include/dgcu.h"
 #include "dg_ctx.hpp"
+#include "euler_split.cuh"
 
 struct dg_batch {
     std::vector<dg_ctx*> groups;
@@ -21,7 +22,10 @@ struct dg_batch {
     cudaEvent_t fork = nullptr;
     std::vector<cudaEvent_t> joins;
     // schedule
-    int concurrent = 0;              // 0: groups one after another on the whole GPU; 1: side by side
+    // 0: groups one after another on the whole GPU; 1: side by side on
+    // streams; 2: every stage of every group in one launch (the mixed-order
+    // kernel, each group on its share of the SMs)
+    int concurrent = 0;
     std::vector<int> ctas_per_sm;    // per group
     std::vector<int> sm_budget;      // per group (concurrent schedule)
     // captured graph
@@ -49,7 +53,7 @@ int bfail(dg_batch* b, int code, const std::string& m) {
 void apply_shape(dg_batch* b) {
     for (size_t g = 0; g < b->groups.size(); g++) {
         b->groups[g]->split.ctas_per_sm = b->ctas_per_sm[g];
-        b->groups[g]->split.sm_budget = b->concurrent ? b->sm_budget[g] : 0;
+        b->groups[g]->split.sm_budget = b->concurrent == 1 ? b->sm_budget[g] : 0;
     }
 }
 
@@ -59,9 +63,48 @@ void drop_graph(dg_batch* b) {
     b->g_steps = -1;
 }
 
+// the mixed-order single launch per stage needs split precision, orders
+// 1..6 on the pipelined body, 16-byte aligned states and no per-stage
+// boundary-trace refresh
+bool fused_ok(const dg_batch* b, int precision) {
+    if (precision != DG_PREC_SPLIT || b->groups.size() > (size_t)dgk::SplitBatchArgs::MAXG) return false;
+    for (const dg_ctx* c : b->groups) {
+        if (c->N > 6 || !c->split.ready || c->split.variant == dgk::SplitPlan::CLASSIC) return false;
+        if (has_dynamic_traces(c)) return false;
+        if ((reinterpret_cast<uintptr_t>(c->d_q[0]) & 15u) || (reinterpret_cast<uintptr_t>(c->d_q[1]) & 15u))
+            return false;
+    }
+    return true;
+}
+
+int issue_steps_fused(dg_batch* b, double dt, int nsteps, int flux) {
+    const int G = (int)b->groups.size();
+    for (int s = 0; s < nsteps; s++)
+        for (int k = 0; k < 5; k++) {
+            dgk::SplitBatchArgs P;
+            memset(&P, 0, sizeof(P));
+            P.ngroups = G;
+            int acc = 0;
+            for (int g = 0; g < G; g++) {
+                dg_ctx* c = b->groups[g];
+                dgk::EulerArgs a;
+                lserk_stage_args(c, dt, k, flux, &a);
+                dgk::split_fill_args(a, c->split, &P.sa[g]);
+                P.order[g] = c->N;
+                const int ntiles = (c->K + dgk::SplitDims<1>::E - 1) / dgk::SplitDims<1>::E;
+                acc += std::max(1, std::min(ntiles, b->sm_budget[g]));
+                P.cta_end[g] = acc;
+            }
+            B_CUDA(b, dgk::launch_split_batch(P, b->main));
+            for (int g = 0; g < G; g++) b->groups[g]->cur ^= 1;
+        }
+    return DG_OK;
+}
+
 // issues nsteps LSERK4 steps of every group into the batch streams
 int issue_steps(dg_batch* b, double dt, int nsteps, int flux, int precision) {
     const int G = (int)b->groups.size();
+    if (b->concurrent == 2) return issue_steps_fused(b, dt, nsteps, flux);
     B_CUDA(b, cudaEventRecord(b->fork, b->main));
     for (int g = 0; g < G; g++) {
         cudaStream_t st = b->concurrent ? b->streams[g] : b->main;
@@ -258,14 +301,29 @@ int dg_batch_tune(dg_batch* b, double dt, int flux, int precision, int steps_per
         apply_shape(b);
         rc = time_steps(b, dt, steps_per_trial, flux, precision, &t_conc);
     }
+    float t_fused = 1e30f;
+    if (!rc && fused_ok(b, precision)) {
+        // one launch per stage, each group on its share of the SMs
+        b->sm_budget = budget;
+        b->concurrent = 2;
+        apply_shape(b);
+        rc = time_steps(b, dt, steps_per_trial, flux, precision, &t_fused);
+    }
     if (!rc) {
-        b->concurrent = (G > 1 && t_conc < t_seq) ? 1 : 0;
+        b->concurrent = 0;
+        float best = t_seq;
+        if (G > 1 && t_conc < best) {
+            b->concurrent = 1;
+            best = t_conc;
+        }
+        if (t_fused < best) b->concurrent = 2;
         b->sm_budget = budget;
         apply_shape(b);
         if (result) {
             result->concurrent = b->concurrent;
             result->ms_sequential = t_seq / steps_per_trial;
             result->ms_concurrent = G > 1 ? t_conc / steps_per_trial : t_seq / steps_per_trial;
+            result->ms_fused = t_fused < 1e29f ? t_fused / steps_per_trial : 0.0;
         }
     }
     // restore the states
@@ -281,10 +339,36 @@ int dg_batch_tune(dg_batch* b, double dt, int flux, int precision, int steps_per
     return rc;
 }
 
+int dg_batch_set_schedule(dg_batch* b, int schedule, int precision) {
+    if (!b || schedule < 0 || schedule > 2) return DG_ERR_ARG;
+    if (schedule == 2 && !fused_ok(b, precision))
+        return bfail(b, DG_ERR_UNSUPPORTED, "one launch per stage needs split precision, orders <= 6, <= 8 groups");
+    const int G = (int)b->groups.size();
+    if (schedule != 0 && b->sm_budget.size() == (size_t)G) {
+        // SM shares in proportion to the groups' element-node counts unless tuned before
+        int sum = 0;
+        for (int v : b->sm_budget) sum += v;
+        if (sum != b->sms) {
+            double tot = 0;
+            for (const dg_ctx* c : b->groups) tot += (double)c->K * c->Np;
+            int used = 0;
+            for (int g = 0; g < G; g++) {
+                b->sm_budget[g] = std::max(1, (int)std::floor(b->sms * (double)b->groups[g]->K * b->groups[g]->Np / tot));
+                used += b->sm_budget[g];
+            }
+            for (int g = 0; used < b->sms; g = (g + 1) % G, used++) b->sm_budget[g]++;
+        }
+    }
+    drop_graph(b);
+    b->concurrent = schedule;
+    apply_shape(b);
+    return DG_OK;
+}
+
 int dg_batch_get_shape(const dg_batch* b, int group, int* ctas_per_sm, int* sm_budget, int* concurrent) {
     if (!b || group < 0 || group >= (int)b->groups.size()) return DG_ERR_ARG;
     if (ctas_per_sm) *ctas_per_sm = b->ctas_per_sm[group];
-    if (sm_budget) *sm_budget = b->concurrent ? b->sm_budget[group] : b->sms;
+    if (sm_budget) *sm_budget = b->concurrent ? b->sm_budget[group] : b->sms;  // schedules 1 and 2: its share
     if (concurrent) *concurrent = b->concurrent;
     return DG_OK;
 }

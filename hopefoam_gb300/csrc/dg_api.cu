@@ -118,6 +118,19 @@ int euler_stage_mode(dg_ctx* c, const double* qin, double* qout, const double* q
     return run_stage(c, a, precision);
 }
 
+int lserk_stage_args(dg_ctx* c, double dt, int stage, int flux, EulerArgs* out) {
+    EulerArgs a = base_args(c, flux);
+    a.res = c->d_res;
+    a.mode = MODE_LSERK;
+    a.dt = dt;
+    a.qin = c->d_q[c->cur];
+    a.qout = c->d_q[c->cur ^ 1];
+    a.rka = kRk4a[stage];
+    a.rkb = kRk4b[stage];
+    *out = a;
+    return DG_OK;
+}
+
 int lserk_stage(dg_ctx* c, double dt, int stage, int flux, int precision) {
     EulerArgs a = base_args(c, flux);
     a.res = c->d_res;

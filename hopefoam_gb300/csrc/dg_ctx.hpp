@@ -78,6 +78,11 @@ void split_teardown(dg_ctx* c);
 // one LSERK4 stage (0..4) of a context on c->stream, no host synchronisation
 // (usable inside a stream capture); flips c->cur
 int lserk_stage(dg_ctx* c, double dt, int stage, int flux, int precision);
+// the arguments of that stage (from the context's current buffer parity),
+// without launching or flipping anything
+int lserk_stage_args(dg_ctx* c, double dt, int stage, int flux, dgk::EulerArgs* out);
+// true when wall / zero-gradient slots need their traces refreshed per stage
+bool has_dynamic_traces(const dg_ctx* c);
 // validates flux / precision / boundary state for stepping
 int check_run_args(dg_ctx* c, int flux, int precision);
 // reads and clears the split kernel's timeout flag (synchronises c->stream)

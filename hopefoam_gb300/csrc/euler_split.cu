@@ -979,6 +979,7 @@ static int setup_n(dg_ctx* c) {
         return DG_ERR_CUDA;
     if constexpr (!D::STREAM) {
         if (setup_split_pipe<N>() != cudaSuccess) return DG_ERR_CUDA;
+        if (setup_split_batch() != cudaSuccess) return DG_ERR_CUDA;
         c->split.variant = SplitPlan::PIPE;
         // DGCU_SPLIT_VARIANT=classic selects the tile-serial kernel (A/B measurements)
         const char* v = getenv("DGCU_SPLIT_VARIANT");
@@ -995,23 +996,28 @@ static int setup_n(dg_ctx* c) {
     return DG_OK;
 }
 
+int split_fill_args(const EulerArgs& a, const SplitPlan& plan, SplitArgs* sa) {
+    sa->e = a;
+    sa->res32 = plan.d_res32;
+    sa->res32_out = plan.d_res32;
+    sa->b1 = static_cast<const float*>(plan.d_ops);
+    sa->b2 = static_cast<const float*>(plan.d_ops) + plan.b2_offset;
+    sa->status = plan.d_status;
+    sa->qbulk = (reinterpret_cast<uintptr_t>(a.qin) & 15u) == 0;
+    sa->If32 = static_cast<const float*>(plan.d_ops) + plan.if32_offset;
+    sa->dtk32 = a.dtk ? a.dtk32 : nullptr;
+    sa->rkaf = (float)a.rka;
+    sa->rkbf = (float)a.rkb;
+    sa->dtf = (float)a.dt;
+    sa->first = a.rka == 0.0;
+    return DG_OK;
+}
+
 template <int N>
 static cudaError_t launch_split_n(const EulerArgs& a, const SplitPlan& plan, cudaStream_t s) {
     using D = SplitDims<N>;
     SplitArgs sa;
-    sa.e = a;
-    sa.res32 = plan.d_res32;
-    sa.res32_out = plan.d_res32;
-    sa.b1 = static_cast<const float*>(plan.d_ops);
-    sa.b2 = static_cast<const float*>(plan.d_ops) + plan.b2_offset;
-    sa.status = plan.d_status;
-    sa.qbulk = (reinterpret_cast<uintptr_t>(a.qin) & 15u) == 0;
-    sa.If32 = static_cast<const float*>(plan.d_ops) + plan.if32_offset;
-    sa.dtk32 = a.dtk ? a.dtk32 : nullptr;
-    sa.rkaf = (float)a.rka;
-    sa.rkbf = (float)a.rkb;
-    sa.dtf = (float)a.dt;
-    sa.first = a.rka == 0.0;
+    split_fill_args(a, plan, &sa);
     const int ntiles = (a.K + D::E - 1) / D::E;
     const int sms = (plan.sm_budget > 0 && plan.sm_budget < plan.sms) ? plan.sm_budget : plan.sms;
     const int want = sms * (plan.ctas_per_sm > 0 ? plan.ctas_per_sm : 1);

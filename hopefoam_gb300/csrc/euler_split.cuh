@@ -116,6 +116,21 @@ constexpr uint32_t kWaitLimit = 1u << 22;
 // stores are free of bank conflicts.  GEMM1 keeps r = 4 e + v.
 __device__ __forceinline__ int g2row(int e, int v) { return ((e >> 3) << 5) | (v << 3) | (e & 7); }
 
+// one stage of several contexts (orders 1..6, pipelined body) in one launch:
+// group g runs on blocks [cta_end[g-1], cta_end[g])
+struct SplitBatchArgs {
+    static constexpr int MAXG = 8;
+    SplitArgs sa[MAXG];
+    int order[MAXG];
+    int cta_end[MAXG];
+    int ngroups;
+};
+cudaError_t setup_split_batch();
+cudaError_t launch_split_batch(const SplitBatchArgs& P, cudaStream_t s);
+
+// the stage's kernel arguments from the context-level ones (FP32 scalars, tables)
+int split_fill_args(const EulerArgs& a, const SplitPlan& plan, SplitArgs* sa);
+
 // the pipelined variant of the stage (euler_split_pipe.cu) for N <= 6: the
 // next tile's staging runs under this tile's volume phase and its face phase
 // under this tile's epilogue

@@ -28,6 +28,7 @@
 // is re-read from L2 in the epilogue.  Every mbarrier wait is bounded; a
 // timeout sets the status word, and the CTA waits for its copies and MMAs in
 // flight before it frees tensor memory and returns.
+#include <algorithm>
 #include <cstdio>
 
 #include "../../include/dgcu.h"
@@ -69,8 +70,11 @@ struct PipeDims {
     static constexpr int DQ_PER = (NDQ + DQ_SLICES - 1) / DQ_SLICES;
 };
 
+// The stage for the tiles bid, bid + nblk, ... of one context (a CTA of 512
+// threads); the single-context kernel runs it with its own block index and
+// grid size, the mixed-order batch kernel with its share of the grid.
 template <int N>
-__global__ void __launch_bounds__(512, 1) euler_stage_split_pipe_kernel(SplitArgs sa) {
+__device__ __forceinline__ void pipe_body(const SplitArgs& sa, const int bid, const int nblk) {
     using S = SplitDims<N>;
     using D = PipeDims<N>;
     constexpr int Np = S::Np, Ng = S::Ng, Nfp = S::Nfp, Nfq = S::Nfq, E = S::E;
@@ -102,7 +106,7 @@ __global__ void __launch_bounds__(512, 1) euler_stage_split_pipe_kernel(SplitArg
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int ntiles = (a.K + E - 1) / E;
     const float gamma = (float)a.gamma;
-    const int G = (int)gridDim.x;
+    const int G = nblk;
 
     uint32_t pq = 0;       // bq phase parity
     bool qpend = false;    // a tile copy in flight (thread 0)
@@ -207,7 +211,7 @@ __global__ void __launch_bounds__(512, 1) euler_stage_split_pipe_kernel(SplitArg
         for (int i = tid; i < S::SZ_A1 / 4; i += blockDim.x) sA1[i] = 0.f;
         for (int i = tid; i < S::SZ_AF / 4; i += blockDim.x) sAF[i] = 0.f;
     }
-    const int t0 = blockIdx.x;
+    const int t0 = bid;
     if (tid == 0) {
         umma::mbar_init(bar1, 1);
         for (int b = 0; b < S::NBUF; b++) umma::mbar_init(bar2 + b, 1);
@@ -813,6 +817,59 @@ __global__ void __launch_bounds__(512, 1) euler_stage_split_pipe_kernel(SplitArg
     umma::fence_before_sync();
     __syncthreads();
     if (warp == 0) umma::tmem_dealloc(tmem, S::TMEM_COLS);
+}
+
+template <int N>
+__global__ void __launch_bounds__(512, 1) euler_stage_split_pipe_kernel(SplitArgs sa) {
+    pipe_body<N>(sa, blockIdx.x, gridDim.x);
+}
+
+// One stage of several contexts of orders 1..6 in one launch: blocks
+// [cta_end[g-1], cta_end[g]) run group g's tiles with its order's body.
+__global__ void __launch_bounds__(512, 1) euler_stage_split_batch_kernel(const __grid_constant__ SplitBatchArgs P) {
+    int g = 0;
+    while (g + 1 < P.ngroups && (int)blockIdx.x >= P.cta_end[g]) g++;
+    const int begin = g ? P.cta_end[g - 1] : 0;
+    const int bid = (int)blockIdx.x - begin, nblk = P.cta_end[g] - begin;
+    switch (P.order[g]) {
+        case 1: pipe_body<1>(P.sa[g], bid, nblk); break;
+        case 2: pipe_body<2>(P.sa[g], bid, nblk); break;
+        case 3: pipe_body<3>(P.sa[g], bid, nblk); break;
+        case 4: pipe_body<4>(P.sa[g], bid, nblk); break;
+        case 5: pipe_body<5>(P.sa[g], bid, nblk); break;
+        case 6: pipe_body<6>(P.sa[g], bid, nblk); break;
+        default: break;
+    }
+}
+
+static int batch_smem(int N) {
+    switch (N) {
+        case 1: return PipeDims<1>::SMEM;
+        case 2: return PipeDims<2>::SMEM;
+        case 3: return PipeDims<3>::SMEM;
+        case 4: return PipeDims<4>::SMEM;
+        case 5: return PipeDims<5>::SMEM;
+        case 6: return PipeDims<6>::SMEM;
+        default: return 0;
+    }
+}
+
+cudaError_t setup_split_batch() {
+    int smax = 0;
+    for (int n = 1; n <= 6; n++) smax = std::max(smax, batch_smem(n));
+    return cudaFuncSetAttribute(euler_stage_split_batch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smax);
+}
+
+cudaError_t launch_split_batch(const SplitBatchArgs& P, cudaStream_t s) {
+    if (P.ngroups < 1 || P.ngroups > SplitBatchArgs::MAXG) return cudaErrorInvalidValue;
+    int smax = 0;
+    for (int g = 0; g < P.ngroups; g++) {
+        const int sm = batch_smem(P.order[g]);
+        if (sm == 0) return cudaErrorInvalidValue;
+        smax = std::max(smax, sm);
+    }
+    euler_stage_split_batch_kernel<<<P.cta_end[P.ngroups - 1], 512, smax, s>>>(P);
+    return cudaGetLastError();
 }
 
 template <int N>

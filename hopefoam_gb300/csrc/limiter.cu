@@ -395,6 +395,8 @@ int reflect(dg_ctx* c, const double* q, double* bnd) {
 // (the unlimited steppers call this before every stage, as the reference
 // corrects its boundary conditions after every equation solve,
 // dgMatrixSolve.C:209); no work when no slot is of those kinds
+bool has_dynamic_traces(const dg_ctx* c) { return c->lim && c->lim->ready && c->lim->dynamic; }
+
 int refresh_boundary_traces(dg_ctx* c, const double* q) {
     if (!c->lim || !c->lim->ready || !c->lim->dynamic) return DG_OK;
     return reflect(c, q, c->d_btrace);

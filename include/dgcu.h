@@ -177,21 +177,29 @@ int dg_set_element_dt(dg_ctx* ctx, const double* dtk_host);
  * every group nsteps LSERK4 steps in one CUDA-graph launch (captured on the
  * first run with these arguments, replayed after).  dg_batch_tune measures
  * launch shapes on the live state (restored afterwards): CTAs per SM of the
- * split kernel where two fit, and the groups run one after another on the
- * whole GPU or side by side on SM shares proportional to their measured cost;
- * the fastest is kept.  No counterpart in the reference.  The groups must not
+ * split kernel where two fit, and three schedules: the groups one after
+ * another on the whole GPU, side by side on streams with SM shares
+ * proportional to their measured cost, or (split precision, orders <= 6, up
+ * to 8 groups) every stage of every group in one persistent mixed-order
+ * launch, each group on its SM share; the fastest is kept.  No counterpart in the reference.  The groups must not
  * be used on their own streams while a dg_batch_run is in flight. */
 typedef struct dg_batch dg_batch;
 typedef struct dg_batch_tuning {
-    int32_t concurrent;      /* 1: groups side by side */
+    int32_t concurrent;      /* schedule kept: 0 groups one after another, 1 side by side on streams,
+                                2 one mixed-order launch per stage */
     double ms_sequential;    /* per step */
     double ms_concurrent;    /* per step */
+    double ms_fused;         /* per step (0: schedule 2 not possible for this batch) */
 } dg_batch_tuning;
 int dg_batch_create(dg_ctx* const* groups, int n_groups, dg_batch** out);
 int dg_batch_destroy(dg_batch* batch);
 const char* dg_batch_last_error(const dg_batch* batch);
 int dg_batch_tune(dg_batch* batch, double dt, int flux, int precision, int steps_per_trial, dg_batch_tuning* result);
 int dg_batch_get_shape(const dg_batch* batch, int group, int* ctas_per_sm, int* sm_budget, int* concurrent);
+/* Fixes the schedule (0, 1 or 2 as in dg_batch_tuning.concurrent) without
+ * measuring; SM shares from the last tuning, else in proportion to each
+ * group's element nodes.  DG_ERR_UNSUPPORTED when schedule 2 is not possible. */
+int dg_batch_set_schedule(dg_batch* batch, int schedule, int precision);
 int dg_batch_run(dg_batch* batch, double dt, int nsteps, int flux, int precision, double* ms);
 
 /* Symmetric interior-penalty Laplacian of the pressure equation on the

@@ -63,7 +63,8 @@ def test_batch_split_tuned_and_replayed(gpu_lib):
     b1.close()
     b2 = EulerBatch(cases)
     shape = b2.tune(precision=L.DG_PREC_SPLIT, steps_per_trial=1)
-    assert shape["concurrent"] in (0, 1) and len(shape["groups"]) == len({c["order"] for c in cases})
+    assert shape["concurrent"] in (0, 1, 2) and len(shape["groups"]) == len({c["order"] for c in cases})
+    assert shape["ms_fused"] > 0  # the one-launch-per-stage schedule was measured
     b2.run(4, precision=L.DG_PREC_SPLIT)
     s2 = b2.states()
     b2.close()
@@ -74,3 +75,37 @@ def test_batch_split_tuned_and_replayed(gpu_lib):
         # the split path's per-step bound on small meshes (TOL_STEP_SPLIT of
         # test_split_gpu.py) over the 4 steps
         assert err < 4e-8, (i, err)
+
+
+@pytest.mark.parametrize("schedule", [1, 2])
+def test_batch_schedules_bit_identical(gpu_lib, schedule):
+    """Side by side on streams (1) and one mixed-order launch per stage (2)
+    give every case the bits of the groups run one after another (0): each
+    tile's arithmetic does not depend on which launch or CTA runs it."""
+    from hopefoam_gb300 import _lib as L
+    from hopefoam_gb300.batch import EulerBatch
+
+    cases = _cases()
+    ref = EulerBatch(cases)
+    ref.set_schedule(0)
+    ref.run(3, precision=L.DG_PREC_SPLIT)
+    s0 = ref.states()
+    ref.close()
+    b = EulerBatch(cases)
+    b.set_schedule(schedule)
+    b.run(2, precision=L.DG_PREC_SPLIT)
+    b.run(1, precision=L.DG_PREC_SPLIT)  # a second graph (another step count) continues the trajectory
+    s1 = b.states()
+    b.close()
+    for i in range(len(cases)):
+        assert np.array_equal(s0[i], s1[i]), i
+
+
+def test_batch_fused_rejected_in_fp64(gpu_lib):
+    from hopefoam_gb300 import _lib as L
+    from hopefoam_gb300.batch import EulerBatch
+
+    b = EulerBatch(_cases())
+    with pytest.raises(L.DGError):
+        b.set_schedule(2, precision=L.DG_PREC_FP64)
+    b.close()

@@ -98,4 +98,23 @@ F64S_HD float minus_f32(double q, float b) {
     return (qh - b) + ql;
 }
 
+// x widened to FP64 exactly, from its bits (the FP32 -> FP64 conversion
+// instruction occupies the FP64 pipe); zero, subnormal, infinite and NaN
+// inputs take the conversion instruction
+F64S_HD double widen(float x) {
+    const uint32_t u = f_bits(x);
+    const uint32_t e = (u >> 23) & 0xFFu;
+    if (e == 0u || e == 255u) return (double)x;
+    const uint32_t hi = (u & 0x80000000u) | ((e + 896u) << 20) | ((u & 0x7FFFFFu) >> 3);
+    const uint32_t lo = u << 29;
+#ifdef __CUDA_ARCH__
+    return __hiloint2double((int)hi, (int)lo);
+#else
+    const uint64_t b = ((uint64_t)hi << 32) | lo;
+    double d;
+    memcpy(&d, &b, 8);
+    return d;
+#endif
+}
+
 }  // namespace f64s

@@ -24,6 +24,9 @@ extern "C" void minus_batch(const double* q, const float* b, float* out, int n) 
 extern "C" void trunc_batch(const double* q, float* out, int n) {
     for (int i = 0; i < n; i++) out[i] = f64s::trunc_f32(q[i]);
 }
+extern "C" void widen_batch(const float* x, double* out, int n) {
+    for (int i = 0; i < n; i++) out[i] = f64s::widen(x[i]);
+}
 '''
 
 
@@ -83,3 +86,19 @@ def test_trunc_f32(f64split_lib):
     o = out.astype(np.float64)
     assert np.all(np.abs(o) <= np.abs(q))  # toward zero
     assert np.all(np.abs(q - o) < np.spacing(np.abs(out)).astype(np.float64))  # less than one FP32 ulp
+
+
+def test_widen_exact(f64split_lib):
+    """FP32 -> FP64 from the bits: identical to the conversion for normal,
+    zero, subnormal, infinite values (NaN stays NaN)."""
+    rng = np.random.default_rng(11)
+    x = np.concatenate([(rng.standard_normal(20000) * 10.0 ** rng.uniform(-30, 30, 20000)).astype(np.float32),
+                        np.array([0.0, -0.0, 1e-45, -3e-40, 3.4e38, np.inf, -np.inf], np.float32)])
+    out = np.empty(x.size, np.float64)
+    f64split_lib.widen_batch(_p(x), _p(out), x.size)
+    ref = x.astype(np.float64)
+    assert np.array_equal(out.view(np.uint64), ref.view(np.uint64))
+    nan = np.array([np.nan], np.float32)
+    o = np.empty(1, np.float64)
+    f64split_lib.widen_batch(_p(nan), _p(o), 1)
+    assert np.isnan(o[0])

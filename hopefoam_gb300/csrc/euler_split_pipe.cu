@@ -65,7 +65,10 @@ struct PipeDims {
     // volume passes (two chunks per pass where there are two chunk buffers)
     static constexpr int NPASS = S::PAIR ? (S::NCH + 1) / 2 : S::NCH;
     // FP32 deltas of a tile per thread, and how they are spread over the passes
-    static constexpr int NDQ = (S::E * 4 * S::Np + S::THREADS - 1) / S::THREADS;
+    // one core matrix of the GEMM1 operand per warp and step: warp w holds
+    // rows 8w .. 8w + 7, lane = 4 (row % 8) + (k % 4), KP1 / 4 steps along K
+    static constexpr int NDQ = S::KP1 / 4;
+    static_assert(S::THREADS == 512 && S::ROWS == 128, "16 warps x 8 rows");
     static constexpr int DQ_SLICES = NPASS > 1 ? NPASS - 1 : 1;
     static constexpr int DQ_PER = (NDQ + DQ_SLICES - 1) / DQ_SLICES;
 };
@@ -180,22 +183,24 @@ __device__ __forceinline__ void pipe_body(const SplitArgs& sa, const int bid, co
     // stage, part 2: FP32 deltas (this thread's items j0 <= j < j1) into sQF and
     // their TF32 hi / lo into the GEMM1 operand
     constexpr uint32_t LO_A1 = 128 * KP1 * 4;
+    // the rows and K offsets of this thread in the core-matrix mapping
+    const int cm_r = 8 * warp + (lane >> 2), cm_k = lane & 3;
     auto stage_dq = [&](int t, int b, int j0, int j1) {
         const int net = min(E, a.K - t * E);
-        const double* qd = qbd(b);
+        if (cm_r >= 4 * net) return;  // rows of a missing element (tail tile)
+        const double qr = qbd(b)[cm_r];
+        const double* src = sQ64 + cm_r * Np + cm_k;
+        float* qf = sQF + cm_r * Np + cm_k;
+        float* dst = sA1 + (warp * (KP1 / 4)) * 32 + lane;
 #pragma unroll
         for (int j = j0; j < j1; j++) {
-            const int i = tid + j * S::THREADS;
-            if (j < D::NDQ && i < net * 4 * Np) {
-                const int e = i / (4 * Np), rem = i - e * 4 * Np, v = rem / Np, p = rem - v * Np;
-                const int r = 4 * e + v;
-                const float d = (float)(sQ64[i] - qd[r]);
-                sQF[i] = d;
+            if (j < D::NDQ && 4 * j + cm_k < Np) {
+                const float d = (float)(src[4 * j] - qr);
+                qf[4 * j] = d;
                 float hi, lo;
                 umma::split_tf32(d, hi, lo);
-                const uint32_t off = umma::kmajor_offset(r, p, KP1) >> 2;
-                sA1[off] = hi;
-                sA1[off + LO_A1 / 4] = lo;
+                dst[32 * j] = hi;
+                dst[32 * j + LO_A1 / 4] = lo;
             }
         }
     };

@@ -258,6 +258,7 @@ def main():
     ap.add_argument("--c5-study", action="store_true", help="500-step shear-layer accuracy study (reduced size)")
     ap.add_argument("--c5-study-n", type=int, default=128)
     ap.add_argument("--c5-study-only", action="store_true", help="run only the shear-layer accuracy study and exit")
+    ap.add_argument("--c5-study-cfl", type=float, default=0.5)
     ap.add_argument("--profile-target", default=None, choices=sorted(PROFILE_TARGETS),
                     help="run one workload of the line alone (the command the ncu summaries profile) and exit")
     ap.add_argument("--profile-size", default="full", choices=["full", "small"],
@@ -272,7 +273,7 @@ def main():
         import torch
 
         torch.cuda.set_device(0)
-        print(json.dumps({"c5_study": c5_study(n=args.c5_study_n)}))
+        print(json.dumps({"c5_study": c5_study(n=args.c5_study_n, cfl=args.c5_study_cfl)}))
         return
 
     import torch
@@ -641,7 +642,7 @@ def c5_bench(nsteps=None, order=7, n=708):
     return out
 
 
-def c5_study(order=7, n=128, checkpoints=(100, 250, 500), n_full=708):
+def c5_study(order=7, n=128, checkpoints=(100, 250, 500), n_full=708, cfl=0.5):
     """The shear layer's accuracy study at reduced size (n x n x 2 elements,
     the full-size workload's setup otherwise) and at the full-size
     workload's time step (its CFL-0.5 step on the n_full grid, so that 500
@@ -659,7 +660,7 @@ def c5_study(order=7, n=128, checkpoints=(100, 250, 500), n_full=708):
     csp = euler.EulerContext(mesh, order)
     c64.upload(q0)
     csp.upload(q0)
-    dt = c64.cfl_dt(0.5) * n / n_full  # min h scales with 1/n on this grid family
+    dt = c64.cfl_dt(cfl) * n / n_full  # min h scales with 1/n on this grid family
     rows, done, ms64, mssp = [], 0, 0.0, 0.0
     for cp in checkpoints:
         ms64 += _timed_lserk4(c64, dt, cp - done, L.DG_FLUX_ROE, L.DG_PREC_FP64)
@@ -673,7 +674,7 @@ def c5_study(order=7, n=128, checkpoints=(100, 250, 500), n_full=708):
     c64.close()
     csp.close()
     return {"workload": "Kelvin-Helmholtz, periodic %dx%dx2 (K=%d), N=7, Roe, LSERK4 at the %dx%dx2 grid's "
-                        "CFL-0.5 step, %d steps" % (n, n, mesh.K, n_full, n_full, checkpoints[-1]),
+                        "CFL-%g step, %d steps" % (n, n, mesh.K, n_full, n_full, cfl, checkpoints[-1]),
             "dt": dt, "density_error_split_vs_fp64": rows, "ms_per_step_fp64": ms64 / checkpoints[-1],
             "ms_per_step_split": mssp / checkpoints[-1]}
 

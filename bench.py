@@ -1042,6 +1042,14 @@ def profile_target(name, small=False):
     elif name == "batch":
         prec = L.DG_PREC_SPLIT
         out.update(batch_bench(prec, n_cases=32 if small else 512, nsteps=2 if small else 10))
+        # the one-launch-per-stage schedule as well, whatever the tuner kept
+        from hopefoam_gb300.batch import EulerBatch, batch_cases
+
+        b = EulerBatch(batch_cases(32 if small else 512, seed=0))
+        b.set_schedule(2, precision=prec)
+        b.run(2, precision=prec)
+        out["fused_ms_2_steps"] = b.run(2, precision=prec)
+        b.close()
     elif name == "split":
         from hopefoam_gb300 import euler
 

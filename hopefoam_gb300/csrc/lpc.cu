@@ -444,17 +444,32 @@ __global__ void __launch_bounds__(SchwarzLocalDims<NP, H>::THREADS, SchwarzLocal
     }
 }
 
-// z_k = zb_k + (G^T U)_k, one thread per element row in element-aligned
-// CTAs (EB = 256 / Np elements); the FP32 offset mirror of z is that of zb
-// (written by the PCG update) plus c - c0 in FP32; partial sums of r.z for the
-// CG scalars (M is linear SPD: the standard beta applies)
+// z_k = zb_k + (G^T U)_k, one thread per element row; the FP32 offset mirror
+// of z is that of zb (written by the PCG update) plus c - c0 in FP32; partial
+// sums of r.z for the CG scalars (M is linear SPD: the standard beta
+// applies).  Up to Np = 32 each warp holds whole elements (32 / Np of them)
+// and an element's c0 reaches its rows by a shuffle; beyond that, element
+// groups of 256 / Np rows exchange it through shared memory.
 __global__ void schwarz_collect_kernel(SchwarzArgs a, const double* __restrict__ zb, const float* __restrict__ U,
                                        const double* __restrict__ r, double* __restrict__ z, float* __restrict__ dz,
                                        int mode, PcgScalars* S, double* part) {
     __shared__ float c0s[256];
     if (mode == LPC_PCG_ITERATION && S->done) return;
-    const int Np = a.Np, F = 4 * Np, EB = 256 / Np;
-    const int e = threadIdx.x / Np, q = threadIdx.x - e * Np;
+    const int Np = a.Np, F = 4 * Np;
+    const bool wa = Np <= 32;
+    const int lane = threadIdx.x & 31;
+    const int EW = wa ? 32 / Np : 0;
+    const int EB = wa ? 8 * EW : 256 / Np;
+    int e, q;
+    if (wa) {
+        e = (threadIdx.x >> 5) * EW + lane / Np;
+        q = lane % Np;
+        if (lane >= EW * Np) e = EB;  // idle lane
+    } else {
+        e = threadIdx.x / Np;
+        q = threadIdx.x - e * Np;
+    }
+    const int lb = lane - q;  // lane of the element's row 0 (warp-aligned layout)
     const int ngroups = (a.K + EB - 1) / EB;
     double rz = 0;
     for (int grp = blockIdx.x; grp < ngroups; grp += gridDim.x) {
@@ -472,16 +487,22 @@ __global__ void schwarz_collect_kernel(SchwarzArgs a, const double* __restrict__
             const double zv = zb[t] + (double)c;
             z[t] = zv;
             if (r) rz += r[t] * zv;
-            if (q == 0) c0s[e] = c;
         }
         if (dz) {
             // dz enters as the offset mirror of zb: z - z0 = (zb - zb0) + (c - c0)
-            __syncthreads();
+            float c0;
+            if (wa) {
+                c0 = __shfl_sync(0xffffffffu, c, lb);
+            } else {
+                if (act && q == 0) c0s[e] = c;
+                __syncthreads();
+                c0 = act ? c0s[e] : 0.f;
+                __syncthreads();
+            }
             if (act) {
                 const size_t t = (size_t)k * Np + q;
-                dz[t] = dz[t] + (c - c0s[e]);
+                dz[t] = dz[t] + (c - c0);
             }
-            __syncthreads();
         }
     }
     if (mode == LPC_APPLY) return;
@@ -596,8 +617,9 @@ cudaError_t launch_schwarz_local(const SchwarzArgs& a, const double* r, const fl
 
 cudaError_t launch_schwarz_collect(const SchwarzArgs& a, const double* zb, const float* U, const double* r,
                                    double* z, float* dz, int mode, PcgScalars* S, double* part, cudaStream_t st) {
-    const int EB = 256 / a.Np;
-    const int threads = (EB * a.Np + 31) / 32 * 32;
+    const bool wa = a.Np <= 32;
+    const int EB = wa ? 8 * (32 / a.Np) : 256 / a.Np;
+    const int threads = wa ? 256 : (EB * a.Np + 31) / 32 * 32;
     const int ngroups = (a.K + EB - 1) / EB;
     const int grid = ngroups < 8 * a.sms ? ngroups : 8 * a.sms;
     schwarz_collect_kernel<<<grid, threads, 0, st>>>(a, zb, U, r, z, dz, mode, S, part);

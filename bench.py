@@ -97,8 +97,8 @@ def alg_bytes_per_elem_stage(order, split=True):
 
 
 # dram__bytes_read.sum + dram__bytes_write.sum of one split-stage launch at
-# the headline workload (one ncu capture of euler_stage_split_kernel<5>)
-SPLIT_STAGE_TRAFFIC_N5 = 222.0e6
+# the headline workload (one ncu capture of euler_stage_split_pipe_kernel<5>)
+SPLIT_STAGE_TRAFFIC_N5 = 220.8e6
 
 
 class ClockSampler:

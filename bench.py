@@ -410,7 +410,8 @@ def main():
                      "traffic": SPLIT_STAGE_TRAFFIC_N5 if (prec_name == "split" and order == 5 and args.nx == 256)
                      else None, "peak_kind": peak_kind, "bytes_per_elem_stage": bpe,
                      "frac_at_fp64_register_bytes": bpe_survey * mesh.K / per_launch_s / 1e9 / peak,
-                     "kernel": "euler_stage_%s_kernel<%d>" % (prec_name, order)},
+                     "kernel": ("euler_stage_split_pipe_kernel<%d>" % order if prec_name == "split" and order <= 6
+                                else "euler_stage_%s_kernel<%d>" % (prec_name, order))},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": n * 8, "d2h_bytes_per_step": n * 8},
         "gpu_launches": launches,
         "clocks": ck,
@@ -963,6 +964,12 @@ def poisson_bench(with_cpu, n_interior=50000, order=4, tau_coef=1.0, rtol=1e-10)
     except Exception as exc:
         out["learned"] = out.get("learned", {"error": str(exc)})
         out["learned_multilevel"] = {"error": str(exc)}
+    # the two-layer network of width 128 (tied weights, relu, BF16 tensor-core
+    # training and inference kernels) in the same Schwarz form, flexible PCG
+    try:
+        out["learned_mlp"] = learned_mlp_solve(mesh, order, b, tau_coef, rtol, st["ms"])
+    except Exception as exc:
+        out["learned_mlp"] = {"error": str(exc)}
     if with_cpu:
         from hopefoam_gb300.mesh import load_cubature
         from oracle import oracle
@@ -978,6 +985,30 @@ def poisson_bench(with_cpu, n_interior=50000, order=4, tau_coef=1.0, rtol=1e-10)
                                          "iteration count"}
     ps.ctx.close()
     return out
+
+
+def learned_mlp_solve(mesh, order, b, tau_coef, rtol, ms_block_jacobi):
+    """Trains the two-layer Schwarz form on a small mesh, transfers it, and
+    solves S x = b with it (learned alone, then with the block-Jacobi
+    fallback)."""
+    from hopefoam_gb300 import _lib as L
+    from hopefoam_gb300.poisson import PressureSolver, train_learned_preconditioner
+
+    W, _, info = train_learned_preconditioner(order, tau_coef=tau_coef, form="mlp", hidden=128)
+    ps = PressureSolver(mesh, order, tau_coef=tau_coef)
+    try:
+        ps.lpc_setup(hidden=128, seed=0, capacity=0, form="mlp")
+        ps.lpc_set_weights(W)
+        _, stl = ps.solve(b, rtol=rtol, maxit=20000, pc=L.DG_PC_LEARNED_ONLY, precision=L.DG_PREC_SPLIT,
+                          raise_on_fail=False)
+        _, stf = ps.solve(b, rtol=rtol, maxit=20000, pc=L.DG_PC_LEARNED, precision=L.DG_PREC_SPLIT,
+                          raise_on_fail=False)
+    finally:
+        ps.ctx.close()
+    return {"training": info, "ms": stf["ms"], "iterations": stf["iterations"], "rel_residual": stf["rel_residual"],
+            "learned_only": {"ms": stl["ms"], "iterations": stl["iterations"], "rel_residual": stl["rel_residual"],
+                             "converged": stl["status"] == L.DG_OK},
+            "speedup_vs_block_jacobi": ms_block_jacobi / stf["ms"] if stf["ms"] else None}
 
 
 def _prof_pcg(small, pcs=("bj",)):

@@ -14,7 +14,7 @@ DG_FLUX_LF, DG_FLUX_ROE = 0, 1
 DG_PREC_FP64, DG_PREC_SPLIT = 0, 1
 DG_PC_NONE, DG_PC_BLOCK_JACOBI, DG_PC_LEARNED, DG_PC_LEARNED_ONLY, DG_PC_MULTILEVEL = 0, 1, 2, 3, 4
 DG_PC_LEARNED_MULTILEVEL = 5
-DG_LPC_RELU, DG_LPC_LINEAR, DG_LPC_SCHWARZ = 0, 1, 2
+DG_LPC_RELU, DG_LPC_LINEAR, DG_LPC_SCHWARZ, DG_LPC_SCHWARZ_MLP = 0, 1, 2, 3
 
 _dp = ctypes.POINTER(ctypes.c_double)
 _ip = ctypes.POINTER(ctypes.c_int32)
@@ -102,6 +102,7 @@ SIGNATURES = {
     "dg_euler_rhs_noalloc": (ctypes.c_int, [_vp, _vp, _vp, ctypes.c_int]),
     "dg_lpc_setup": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_ulonglong, ctypes.c_int, ctypes.c_int]),
     "dg_lpc_add_residual": (ctypes.c_int, [_vp, _dp]),
+    "dg_lpc_set_slope": (ctypes.c_int, [_vp, ctypes.c_double]),
     "dg_lpc_train": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_double, ctypes.c_ulonglong, _dp, _dp]),
     "dg_lpc_loss": (ctypes.c_int, [_vp, _dp, _dp, _dp]),
     "dg_lpc_energy_gradients": (ctypes.c_int, [_vp, _dp, _fp, _fp, _dp]),

@@ -18,7 +18,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-O3", "-I" + CSRC,
           "-I" + os.path.join(HERE, "..", "include")]
 
-SOURCES = ["dg_api.cu", "euler_fp64.cu", "euler_split.cu", "euler_split_pipe.cu", "euler_noalloc.cu", "ipdg.cu", "ipdg_api.cu", "lpc.cu", "schwarz_tc.cu", "batch_api.cu", "ins.cu", "mg.cu", "limiter.cu",
+SOURCES = ["dg_api.cu", "euler_fp64.cu", "euler_split.cu", "euler_split_pipe.cu", "euler_noalloc.cu", "ipdg.cu", "ipdg_api.cu", "lpc.cu", "schwarz_tc.cu", "schwarz_mlp.cu", "batch_api.cu", "ins.cu", "mg.cu", "limiter.cu",
            "dg_basis.cpp"]
 
 

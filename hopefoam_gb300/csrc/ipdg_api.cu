@@ -61,6 +61,7 @@ struct IpdgState {
     float *d_Xs = nullptr, *d_As = nullptr, *d_C = nullptr;  // training: gathered rows, F x F cross term
     double* d_gvec = nullptr;         // training: output-gradient vector
     int* d_tcstatus = nullptr;        // timeout flag of the tensor-core local stage
+    float* d_wpart = nullptr;         // two-layer form: per-CTA weight-gradient partials
     float *d_W1 = nullptr, *d_W2 = nullptr, *d_m1 = nullptr, *d_v1 = nullptr, *d_m2 = nullptr, *d_v2 = nullptr;
     float *d_g1 = nullptr, *d_g2 = nullptr;
     __nv_bfloat16 *d_W1b = nullptr, *d_W2b = nullptr;
@@ -126,6 +127,9 @@ int dot_host(dg_ctx* c, const double* x, const double* y, double* out) {
     return DG_OK;
 }
 
+// the additive-Schwarz forms: one tied weight matrix W (H x 4 Np)
+bool schwarz_form(int form) { return form == DG_LPC_SCHWARZ || form == DG_LPC_SCHWARZ_MLP; }
+
 // runs PCG iterations on S e = r (vectors in v) until S->done or `limit`
 // iterations; returns the iterations taken and the stop code
 void lpc_descr(dg_ctx* c, LpcNet& net, LpcFeatArgs& fa) {
@@ -137,7 +141,7 @@ void lpc_descr(dg_ctx* c, LpcNet& net, LpcFeatArgs& fa) {
     net.W1 = s->d_W1b;
     net.W2 = s->d_W2b;
     net.perm = s->d_perm;
-    if (s->lpc_form == DG_LPC_SCHWARZ) {
+    if (schwarz_form(s->lpc_form)) {
         net.sw = &s->sw;
         net.U = s->d_U;
     }
@@ -759,7 +763,7 @@ static int pcg_solve_impl(dg_ctx* c, const double* b_host, double* x_host, doubl
     const bool mgm = pc == DG_PC_MULTILEVEL || pc == DG_PC_LEARNED_MULTILEVEL;
     if (learned && !c->ipdg->lpc_ready) return ifail(c, DG_ERR_ARG, "dg_lpc_setup not called");
     if (pc == DG_PC_LEARNED_MULTILEVEL && c->ipdg->lpc_form != DG_LPC_SCHWARZ)
-        return ifail(c, DG_ERR_ARG, "learned + multilevel needs the learned Schwarz form");
+        return ifail(c, DG_ERR_ARG, "learned + multilevel needs the linear learned Schwarz form");
     if (mgm && !c->ipdg->mg_ready) {
         const int rcm = mg_setup(c);
         if (rcm) return rcm;
@@ -799,7 +803,7 @@ static int pcg_solve_impl(dg_ctx* c, const double* b_host, double* x_host, doubl
     v.dz = mirrors ? s->d_dz : nullptr;
     v.dp[0] = mirrors ? s->d_dp : nullptr;
     v.dp[1] = mirrors ? s->d_dp2 : nullptr;
-    v.r32 = (learned && s->lpc_form == DG_LPC_SCHWARZ) ? s->d_r32 : nullptr;
+    v.r32 = (learned && schwarz_form(s->lpc_form)) ? s->d_r32 : nullptr;
     int total_it = 0, stop = 0;
     double rel = 0;
     if (bb == 0.0) {
@@ -1001,7 +1005,7 @@ int lpc_forward_vec(dg_ctx* c, const double* r, bool with_bj_loss) {
         IP_CUDA(c, launch_dot(r, s->d_zb, n, s->d_lpart + 2 * s->G, s->G, c->stream));
         IP_CUDA(c, launch_dot(s->d_zb, s->d_w, n, s->d_lpart + 3 * s->G, s->G, c->stream));
     }
-    if (s->lpc_form == DG_LPC_SCHWARZ) {
+    if (schwarz_form(s->lpc_form)) {
         IP_CUDA(c, launch_schwarz_local(s->sw, r, nullptr, s->d_U, nullptr, c->stream));
         IP_CUDA(c, launch_schwarz_collect(s->sw, s->d_zb, s->d_U, nullptr, s->d_zt, nullptr, LPC_APPLY, nullptr,
                                           nullptr, c->stream));
@@ -1020,7 +1024,17 @@ int lpc_forward_vec(dg_ctx* c, const double* r, bool with_bj_loss) {
 // gradients of L(r) into s->d_g1 / d_g2
 int lpc_backward_vec(dg_ctx* c, const double* r) {
     IpdgState* s = c->ipdg;
-    if (s->lpc_form == DG_LPC_SCHWARZ) {
+    if (s->lpc_form == DG_LPC_SCHWARZ_MLP) {
+        // dL/dW = (2a/b) sum_m h_m a_m^T + (D_m W a_m) x_m^T, x_m = G_m r, a_m = G_m g,
+        // g = (a/b) S z - r: per-CTA partials on the tensor cores, then their sum
+        const size_t n = (size_t)c->K * c->Np;
+        IP_CUDA(c, launch_schwarz_outgrad(r, s->d_w, s->d_lpart, s->d_lpart + s->G, s->G, n, s->d_gvec, c->stream));
+        IP_CUDA(c, launch_schwarz_mlp_wgrad(s->sw, r, s->d_gvec, s->d_wpart, s->d_tcstatus, c->stream));
+        IP_CUDA(c, launch_schwarz_mlp_wreduce(s->d_wpart, schwarz_mlp_wgrad_ctas(s->sw), s->H, s->F, s->d_lpart,
+                                              s->d_lpart + s->G, s->G, s->d_g1, c->stream));
+        return DG_OK;
+    }
+    if (schwarz_form(s->lpc_form)) {
         // dL/dW = (2a/b) W (X^T A + A^T X), X = G r, A = G g, g = (a/b) S z - r
         const size_t n = (size_t)c->K * c->Np;
         IP_CUDA(c, launch_schwarz_outgrad(r, s->d_w, s->d_lpart, s->d_lpart + s->G, s->G, n, s->d_gvec, c->stream));
@@ -1068,7 +1082,7 @@ int lpc_losses(dg_ctx* c, double* loss, double* loss_bj) {
 
 int lpc_adam_step(dg_ctx* c, double lr) {
     IpdgState* s = c->ipdg;
-    const int n1 = s->H * s->F, n2 = s->lpc_form == DG_LPC_SCHWARZ ? 0 : c->Np * s->H;
+    const int n1 = s->H * s->F, n2 = schwarz_form(s->lpc_form) ? 0 : c->Np * s->H;
     s->adam_step++;
     IP_CUDA(c, launch_lpc_adam(s->d_W1, s->d_m1, s->d_v1, s->d_g1, s->d_W1b, n1, (float)lr, 0.9f, 0.999f, 1e-8f,
                                s->adam_step, 1.f, c->stream));
@@ -1082,7 +1096,7 @@ int lpc_adam_step(dg_ctx* c, double lr) {
 // learning rate only converts)
 int lpc_refresh_bf16(dg_ctx* c) {
     IpdgState* s = c->ipdg;
-    const int n1 = s->H * s->F, n2 = s->lpc_form == DG_LPC_SCHWARZ ? 0 : c->Np * s->H;
+    const int n1 = s->H * s->F, n2 = schwarz_form(s->lpc_form) ? 0 : c->Np * s->H;
     IP_CUDA(c, cudaMemsetAsync(s->d_g1, 0, n1 * sizeof(float), c->stream));
     IP_CUDA(c, launch_lpc_adam(s->d_W1, s->d_m1, s->d_v1, s->d_g1, s->d_W1b, n1, 0.f, 0.9f, 0.999f, 1e-8f, 1, 1.f,
                                c->stream));
@@ -1111,15 +1125,18 @@ extern "C" {
 
 int dg_lpc_setup(dg_ctx* c, int hidden, unsigned long long seed, int capacity, int form) {
     if (!c || hidden < 8 || hidden > 256 || capacity < 0) return DG_ERR_ARG;
-    if (form != DG_LPC_RELU && form != DG_LPC_LINEAR && form != DG_LPC_SCHWARZ) return DG_ERR_ARG;
+    if (form != DG_LPC_RELU && form != DG_LPC_LINEAR && form != DG_LPC_SCHWARZ && form != DG_LPC_SCHWARZ_MLP)
+        return DG_ERR_ARG;
     if (!c->ipdg || !c->ipdg->ready) return ifail(c, DG_ERR_ARG, "dg_ipdg_setup not called");
     IpdgState* s = c->ipdg;
     if (s->lpc_ready) return ifail(c, DG_ERR_ARG, "learned preconditioner already set up");
     const int Np = c->Np, K = c->K;
-    const bool schwarz = form == DG_LPC_SCHWARZ;
+    const bool schwarz = schwarz_form(form), mlp = form == DG_LPC_SCHWARZ_MLP;
     if (Np > 36) return ifail(c, DG_ERR_UNSUPPORTED, "learned preconditioner supports N <= 7");
-    if (schwarz && (Np > 28 || (hidden != 32 && hidden != 64)))
+    if (form == DG_LPC_SCHWARZ && (Np > 28 || (hidden != 32 && hidden != 64)))
         return ifail(c, DG_ERR_UNSUPPORTED, "the Schwarz form supports N <= 6 and hidden width 32 or 64");
+    if (mlp && (Np > 28 || Np < 3 || hidden != kSchwarzMlpH))
+        return ifail(c, DG_ERR_UNSUPPORTED, "the two-layer Schwarz form supports N = 1..6 and hidden width 128");
     s->H = hidden;
     s->F = schwarz ? 4 * Np : 4 * Np + 4;
     s->lpc_form = form;
@@ -1152,10 +1169,15 @@ int dg_lpc_setup(dg_ctx* c, int hidden, unsigned long long seed, int capacity, i
     if (schwarz) {
         rc |= iupload(c, s, &s->d_iperm, iperm);
         rc |= ialloc(c, s, &s->d_U, (size_t)K * s->F);
-        rc |= ialloc(c, s, &s->d_Xs, (size_t)K * s->F);
-        rc |= ialloc(c, s, &s->d_As, (size_t)K * s->F);
-        rc |= ialloc(c, s, &s->d_C, (size_t)s->F * s->F);
         rc |= ialloc(c, s, &s->d_gvec, n);
+        if (mlp) {
+            const int nctas = std::min((K + 127) / 128, s->sms);
+            rc |= ialloc(c, s, &s->d_wpart, (size_t)nctas * s->H * s->F);
+        } else {
+            rc |= ialloc(c, s, &s->d_Xs, (size_t)K * s->F);
+            rc |= ialloc(c, s, &s->d_As, (size_t)K * s->F);
+            rc |= ialloc(c, s, &s->d_C, (size_t)s->F * s->F);
+        }
     } else {
         rc |= iupload(c, s, &s->d_W2, W2);
         rc |= ialloc(c, s, &s->d_m2, n2);
@@ -1180,7 +1202,10 @@ int dg_lpc_setup(dg_ctx* c, int hidden, unsigned long long seed, int capacity, i
     s->sw.perm = s->d_perm;
     s->sw.iperm = s->d_iperm;
     s->sw.tc_status = nullptr;
-    if (schwarz && s->H == 32) {
+    s->sw.mlp = mlp ? 1 : 0;
+    s->sw.flex = mlp ? 1 : 0;  // M(r) is not linear: flexible beta in the PCG
+    s->sw.slope = 0.f;
+    if ((form == DG_LPC_SCHWARZ && s->H == 32) || mlp) {
         if (ialloc(c, s, &s->d_tcstatus, 1)) return DG_ERR_NOMEM;
         IP_CUDA(c, cudaMemsetAsync(s->d_tcstatus, 0, sizeof(int), c->stream));
         s->sw.tc_status = s->d_tcstatus;  // the tensor-core local stage
@@ -1197,6 +1222,16 @@ int dg_lpc_setup(dg_ctx* c, int hidden, unsigned long long seed, int capacity, i
     s->count = 0;
     s->adam_step = 0;
     s->lpc_ready = true;
+    return DG_OK;
+}
+
+int dg_lpc_set_slope(dg_ctx* c, double slope) {
+    if (!c || !(slope >= 0.0 && slope <= 1.0)) return DG_ERR_ARG;
+    if (!lpc_ok(c)) return ifail(c, DG_ERR_ARG, "dg_lpc_setup not called");
+    IpdgState* s = c->ipdg;
+    if (s->lpc_form != DG_LPC_SCHWARZ_MLP) return ifail(c, DG_ERR_ARG, "the slope belongs to the two-layer Schwarz form");
+    s->sw.slope = (float)slope;
+    s->sw.flex = slope < 1.0 ? 1 : 0;  // slope 1: linear and symmetric, the standard beta applies
     return DG_OK;
 }
 
@@ -1272,7 +1307,7 @@ int dg_lpc_loss(dg_ctx* c, const double* r_host, double* loss, double* loss_bj) 
 
 int dg_lpc_energy_gradients(dg_ctx* c, const double* r_host, float* gW1, float* gW2, double* loss) {
     if (!c || !r_host || !gW1) return DG_ERR_ARG;
-    if (c->ipdg && c->ipdg->lpc_form != DG_LPC_SCHWARZ && !gW2) return DG_ERR_ARG;
+    if (c->ipdg && !schwarz_form(c->ipdg->lpc_form) && !gW2) return DG_ERR_ARG;
     if (!lpc_ok(c)) return ifail(c, DG_ERR_ARG, "dg_lpc_setup not called");
     IpdgState* s = c->ipdg;
     int rc = lpc_upload_residual(c, r_host, s->d_r);
@@ -1281,7 +1316,7 @@ int dg_lpc_energy_gradients(dg_ctx* c, const double* r_host, float* gW1, float* 
     if (!rc) rc = lpc_losses(c, loss, nullptr);
     if (rc) return rc;
     IP_CUDA(c, cudaMemcpyAsync(gW1, s->d_g1, (size_t)s->H * s->F * sizeof(float), cudaMemcpyDeviceToHost, c->stream));
-    if (s->lpc_form != DG_LPC_SCHWARZ)
+    if (!schwarz_form(s->lpc_form))
         IP_CUDA(c, cudaMemcpyAsync(gW2, s->d_g2, (size_t)c->Np * s->H * sizeof(float), cudaMemcpyDeviceToHost,
                                    c->stream));
     IP_CUDA(c, cudaStreamSynchronize(c->stream));
@@ -1292,7 +1327,7 @@ int dg_lpc_get_weights(dg_ctx* c, float* W1, float* W2) {
     if (!c || !W1) return DG_ERR_ARG;
     if (!lpc_ok(c)) return ifail(c, DG_ERR_ARG, "dg_lpc_setup not called");
     IpdgState* s = c->ipdg;
-    const bool two = s->lpc_form != DG_LPC_SCHWARZ;
+    const bool two = !schwarz_form(s->lpc_form);
     if (two && !W2) return DG_ERR_ARG;
     IP_CUDA(c, cudaMemcpyAsync(W1, s->d_W1, (size_t)s->H * s->F * sizeof(float), cudaMemcpyDeviceToHost, c->stream));
     if (two)
@@ -1306,7 +1341,7 @@ int dg_lpc_set_weights(dg_ctx* c, const float* W1, const float* W2) {
     if (!c || !W1) return DG_ERR_ARG;
     if (!lpc_ok(c)) return ifail(c, DG_ERR_ARG, "dg_lpc_setup not called");
     IpdgState* s = c->ipdg;
-    const bool two = s->lpc_form != DG_LPC_SCHWARZ;
+    const bool two = !schwarz_form(s->lpc_form);
     if (two && !W2) return DG_ERR_ARG;
     const int n1 = s->H * s->F, n2 = two ? c->Np * s->H : 0;
     IP_CUDA(c, cudaMemcpyAsync(s->d_W1, W1, n1 * sizeof(float), cudaMemcpyHostToDevice, c->stream));
@@ -1329,7 +1364,7 @@ int dg_lpc_gradients(dg_ctx* c, const float* X_host, const float* T_host, int B,
     if (!c || !X_host || !T_host || B < 1 || !gW1 || !gW2) return DG_ERR_ARG;
     if (!lpc_ok(c)) return ifail(c, DG_ERR_ARG, "dg_lpc_setup not called");
     IpdgState* s = c->ipdg;
-    if (s->lpc_form == DG_LPC_SCHWARZ)
+    if (schwarz_form(s->lpc_form))
         return ifail(c, DG_ERR_UNSUPPORTED, "batch gradients are defined for the two-layer forms");
     const int Np = c->Np;
     float *Xf = nullptr, *Td = nullptr, *Hs = nullptr, *dY = nullptr;
@@ -1381,7 +1416,7 @@ int dg_lpc_apply(dg_ctx* c, const double* r_host, double* z_host) {
     LpcFeatArgs fa;
     lpc_descr(c, net, fa);
     IP_CUDA(c, cudaMemsetAsync(s->d_z, 0, n * sizeof(double), c->stream));
-    if (s->lpc_form == DG_LPC_SCHWARZ) {
+    if (schwarz_form(s->lpc_form)) {
         IP_CUDA(c, launch_schwarz_local(s->sw, s->d_r, nullptr, s->d_U, nullptr, c->stream));
         IP_CUDA(c, launch_schwarz_collect(s->sw, s->d_zb, s->d_U, nullptr, s->d_z, nullptr, LPC_APPLY, nullptr,
                                           nullptr, c->stream));

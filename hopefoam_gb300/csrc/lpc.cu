@@ -446,8 +446,9 @@ __global__ void __launch_bounds__(SchwarzLocalDims<NP, H>::THREADS, SchwarzLocal
 
 // z_k = zb_k + (G^T U)_k, one thread per element row; the FP32 offset mirror
 // of z is that of zb (written by the PCG update) plus c - c0 in FP32; partial
-// sums of r.z for the CG scalars (M is linear SPD: the standard beta
-// applies).  Up to Np = 32 each warp holds whole elements (32 / Np of them)
+// sums of r.z for the CG scalars (the linear form is SPD: the standard beta
+// applies; the two-layer form (a.flex) also sums r.z_old, read from z before
+// it is overwritten, for the flexible beta).  Up to Np = 32 each warp holds whole elements (32 / Np of them)
 // and an element's c0 reaches its rows by a shuffle; beyond that, element
 // groups of 256 / Np rows exchange it through shared memory.
 __global__ void schwarz_collect_kernel(SchwarzArgs a, const double* __restrict__ zb, const float* __restrict__ U,
@@ -471,7 +472,8 @@ __global__ void schwarz_collect_kernel(SchwarzArgs a, const double* __restrict__
     }
     const int lb = lane - q;  // lane of the element's row 0 (warp-aligned layout)
     const int ngroups = (a.K + EB - 1) / EB;
-    double rz = 0;
+    const bool flex = a.flex && mode == LPC_PCG_ITERATION;
+    double rz = 0, rzo = 0;
     for (int grp = blockIdx.x; grp < ngroups; grp += gridDim.x) {
         const int k = grp * EB + e;
         const bool act = e < EB && k < a.K;
@@ -485,6 +487,7 @@ __global__ void schwarz_collect_kernel(SchwarzArgs a, const double* __restrict__
                 if (cn >= 0) c += U[(size_t)(cn >> 3) * F + ((cn & 3) + 1) * Np + a.iperm[f * Np + q]];
             }
             const double zv = zb[t] + (double)c;
+            if (flex) rzo += r[t] * z[t];
             z[t] = zv;
             if (r) rz += r[t] * zv;
         }
@@ -506,9 +509,9 @@ __global__ void schwarz_collect_kernel(SchwarzArgs a, const double* __restrict__
         }
     }
     if (mode == LPC_APPLY) return;
-    double val[1] = {rz}, tot[1];
-    if (grid_sum<1>(val, part, gridDim.x, &S->counter, tot) && threadIdx.x == 0) {
-        if (mode == LPC_PCG_ITERATION) pcg_finish(S, tot[0], 0.0, S->rr);
+    double val[2] = {rz, rzo}, tot[2];
+    if (grid_sum<2>(val, part, gridDim.x, &S->counter, tot) && threadIdx.x == 0) {
+        if (mode == LPC_PCG_ITERATION) pcg_finish(S, tot[0], tot[1], S->rr);
         else S->rz = tot[0];
     }
 }
@@ -603,6 +606,7 @@ static cudaError_t schwarz_local_np(const SchwarzArgs& a, const double* r, const
 
 cudaError_t launch_schwarz_local(const SchwarzArgs& a, const double* r, const float* r32, float* U, const int* done,
                                  cudaStream_t st) {
+    if (a.mlp) return launch_schwarz_mlp_local(a, r, r32, U, done, a.tc_status, st);
     if (a.tc_status && a.H == 32) return launch_schwarz_local_tc(a, r, r32, U, done, a.tc_status, st);
     switch (a.Np) {
         case 3: return schwarz_local_np<3>(a, r, r32, U, done, st);

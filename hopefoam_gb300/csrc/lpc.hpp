@@ -59,15 +59,20 @@ enum { LPC_APPLY = 0, LPC_PCG_INIT = 1, LPC_PCG_REFRESH = 2, LPC_PCG_ITERATION =
 cudaError_t launch_lpc_precond(const LpcNet& n, const LpcFeatArgs& fa, const double* r, double* z, int mode,
                                PcgScalars* S, double* part, float* dz, cudaStream_t st);
 
-// learned additive-Schwarz form: M r = P r + sum_m G_m^T W^T W G_m r
+// learned additive-Schwarz form: M r = P r + sum_m G_m^T W^T W G_m r, or with
+// mlp = 1 the two-layer network with tied weights M r = P r + sum_m G_m^T W^T relu(W G_m r)
 constexpr int kSchwarzMaxH = 128;
+constexpr int kSchwarzMlpH = 128;
 struct SchwarzArgs {
     int K, Np, H, sms;
     const __nv_bfloat16* W;  // H x 4 Np
     const int* conn;         // packed neighbours
     const int* perm;         // 3 x Np: node permutation that rotates a neighbour's face fn onto face 0
     const int* iperm;        // 3 x Np: inverse of perm
-    int* tc_status;          // non-null: run the local stage on the tensor cores (H = 32); timeout flag
+    int* tc_status;          // non-null: run the local stage on the tensor cores (H = 32, or mlp); timeout flag
+    int mlp;                 // 1: (leaky) relu between the two layers (H = 128, BF16 tensor-core kernels)
+    int flex;                // 1: the collect step also forms r.z_old (flexible beta: M is not linear)
+    float slope;             // mlp: activation max(h, slope h), slope in [0, 1] (0: relu)
 };
 // tensor-core local stage (schwarz_tc.cu); cudaErrorNotSupported when H != 32 or N > 6
 cudaError_t launch_schwarz_local_tc(const SchwarzArgs& a, const double* r, const float* r32, float* U,
@@ -83,6 +88,18 @@ cudaError_t launch_schwarz_gather_rows(const SchwarzArgs& a, const double* v, fl
 cudaError_t launch_schwarz_cross(const float* X, const float* A, int K, int F, float* C, cudaStream_t st);
 cudaError_t launch_schwarz_wgrad(const float* W, const float* C, int H, int F, const double* part_a,
                                  const double* part_b, int G, float* gW, cudaStream_t st);
+// two-layer (mlp) form on the tensor cores (schwarz_mlp.cu): the local stage
+// U_m = W^T relu(W G_m r) (BF16 hi + lo operands, FP32 accumulation), and the
+// energy-loss weight gradient: per CTA a partial sum over its patches of
+// h a^T + (D W a) x^T (x = G_m r, a = G_m g, h = relu(W x), D its 0/1 mask),
+// then gW = (2 a / b) times the sum over the CTAs
+cudaError_t launch_schwarz_mlp_local(const SchwarzArgs& a, const double* r, const float* r32, float* U,
+                                     const int* done, int* status, cudaStream_t st);
+int schwarz_mlp_wgrad_ctas(const SchwarzArgs& a);
+cudaError_t launch_schwarz_mlp_wgrad(const SchwarzArgs& a, const double* r, const double* g, float* part,
+                                     int* status, cudaStream_t st);
+cudaError_t launch_schwarz_mlp_wreduce(const float* part, int nparts, int H, int F, const double* part_a,
+                                       const double* part_b, int G, float* gW, cudaStream_t st);
 cudaError_t launch_schwarz_outgrad(const double* r, const double* w, const double* part_a, const double* part_b,
                                    int G, size_t n, double* g, cudaStream_t st);
 

@@ -1,7 +1,7 @@
 // umma.cuh -- minimal sm_100-family tensor-core (tcgen05) building blocks in
 // inline PTX: tensor-memory allocation, shared-memory matrix descriptors
-// (no-swizzle K-major canonical layout), the TF32 MMA with FP32 accumulation
-// in TMEM, commit to an mbarrier, bounded mbarrier waits, and TMEM loads.
+// (no-swizzle K-major canonical layout), the TF32 and BF16 MMAs with FP32
+// accumulation in TMEM, commit to an mbarrier, bounded mbarrier waits, and TMEM loads.
 //
 // Canonical no-swizzle K-major operand layout used throughout: the matrix is
 // tiled in "core matrices" of 8 rows x 16 bytes (8 x 4 TF32).  Element
@@ -45,6 +45,35 @@ __host__ __device__ __forceinline__ uint32_t idesc_tf32(int M, int N) {
     d |= (uint32_t)((N >> 3) & 0x3F) << 17;
     d |= (uint32_t)((M >> 4) & 0x1F) << 24;
     return d;
+}
+
+// byte offset of element (r, k) in the same canonical layout for 2-byte
+// elements (core matrices of 8 rows x 8 BF16): one K = 16 MMA step also
+// consumes two core matrices along K (base + s * 256 B); SBO = (KP / 8) * 128 B
+__host__ __device__ __forceinline__ uint32_t kmajor_offset_b16(int r, int k, int KP) {
+    return (uint32_t)((((r >> 3) * (KP >> 3) + (k >> 3)) << 7) + ((r & 7) << 4) + ((k & 7) << 1));
+}
+
+// 32-bit instruction descriptor for kind::f16 with BF16 operands: D = F32,
+// A = B = BF16, both K-major, dense
+__host__ __device__ __forceinline__ uint32_t idesc_bf16(int M, int N) {
+    uint32_t d = 0;
+    d |= 1u << 4;                        // D format F32
+    d |= 1u << 7;                        // A format BF16
+    d |= 1u << 10;                       // B format BF16
+    d |= (uint32_t)((N >> 3) & 0x3F) << 17;
+    d |= (uint32_t)((M >> 4) & 0x1F) << 24;
+    return d;
+}
+
+// D[tmem] (+)= A[smem] * B[smem]^T, BF16 operands (K = 16 per instruction)
+__device__ __forceinline__ void mma_bf16(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc, uint32_t acc) {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "setp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(d_tmem),
+        "l"(adesc), "l"(bdesc), "r"(idesc), "r"(acc)
+        : "memory");
 }
 
 // D[tmem] (+)= A[smem] * B[smem]^T  (both K-major), issued by one thread

@@ -75,23 +75,31 @@ class PressureSolver:
     # ------------------------------------------------------------------
     # learned element-block preconditioner (DG_PC_LEARNED)
 
-    FORMS = {"relu": L.DG_LPC_RELU, "linear": L.DG_LPC_LINEAR, "schwarz": L.DG_LPC_SCHWARZ}
+    FORMS = {"relu": L.DG_LPC_RELU, "linear": L.DG_LPC_LINEAR, "schwarz": L.DG_LPC_SCHWARZ,
+             "mlp": L.DG_LPC_SCHWARZ_MLP}
+    SCHWARZ_FORMS = ("schwarz", "mlp")
 
     def lpc_setup(self, hidden=None, seed=0, capacity=0, form="schwarz", linear=False):
         """Allocates the learned preconditioner and room for `capacity`
         training residual vectors on the device.  form "schwarz" (default):
         M = P + sum_m G_m^T W^T W G_m, SPD by construction, W hidden x 4 Np
-        (hidden 32 or 64); "relu" / "linear": the two-layer correction of the
-        block-Jacobi output (hidden default 128).  linear=True selects
+        (hidden 32 or 64); "mlp": M = P + sum_m G_m^T W^T relu(W G_m), the
+        two-layer network with tied weights, hidden 128, BF16 tensor-core
+        kernels, flexible PCG; "relu" / "linear": the two-layer correction of
+        the block-Jacobi output (hidden default 128).  linear=True selects
         "linear"."""
         if linear:
             form = "linear"
         self.lpc_form = form
         self.lpc_hidden = int(hidden if hidden is not None else (32 if form == "schwarz" else 128))
-        self.lpc_F = 4 * self.Np + (0 if form == "schwarz" else 4)
+        self.lpc_F = 4 * self.Np + (0 if form in self.SCHWARZ_FORMS else 4)
         self.lpc_linear = form == "linear"
         _check(self.ctx.h, self.ctx.lib.dg_lpc_setup(self.ctx.h, self.lpc_hidden, int(seed), int(capacity),
                                                      self.FORMS[form]))
+
+    def lpc_set_slope(self, slope):
+        """Activation max(h, slope h) of the "mlp" form (0: relu, 1: linear)."""
+        _check(self.ctx.h, self.ctx.lib.dg_lpc_set_slope(self.ctx.h, float(slope)))
 
     def lpc_add_residual(self, r):
         r = np.ascontiguousarray(r, np.float64).reshape(-1)
@@ -130,7 +138,7 @@ class PressureSolver:
     def lpc_energy_gradients(self, r):
         r = np.ascontiguousarray(r, np.float64).reshape(-1)
         gW1 = np.zeros((self.lpc_hidden, self.lpc_F), np.float32)
-        gW2 = None if self.lpc_form == "schwarz" else np.zeros((self.Np, self.lpc_hidden), np.float32)
+        gW2 = None if self.lpc_form in self.SCHWARZ_FORMS else np.zeros((self.Np, self.lpc_hidden), np.float32)
         loss = ctypes.c_double(0.0)
         fp = ctypes.POINTER(ctypes.c_float)
         _check(self.ctx.h, self.ctx.lib.dg_lpc_energy_gradients(
@@ -139,10 +147,10 @@ class PressureSolver:
         return gW1, gW2, loss.value
 
     def lpc_weights(self):
-        """(W1, W2); W2 is None for the Schwarz form (one tied weight matrix)."""
+        """(W1, W2); W2 is None for the Schwarz forms (one tied weight matrix)."""
         fp = ctypes.POINTER(ctypes.c_float)
         W1 = np.zeros((self.lpc_hidden, self.lpc_F), np.float32)
-        if self.lpc_form == "schwarz":
+        if self.lpc_form in self.SCHWARZ_FORMS:
             _check(self.ctx.h, self.ctx.lib.dg_lpc_get_weights(self.ctx.h, W1.ctypes.data_as(fp), None))
             return W1, None
         W2 = np.zeros((self.Np, self.lpc_hidden), np.float32)
@@ -154,7 +162,7 @@ class PressureSolver:
         W1 = np.ascontiguousarray(W1, np.float32)
         if W1.shape != (self.lpc_hidden, self.lpc_F):
             raise ValueError("weight shapes do not match the network")
-        if self.lpc_form == "schwarz":
+        if self.lpc_form in self.SCHWARZ_FORMS:
             _check(self.ctx.h, self.ctx.lib.dg_lpc_set_weights(self.ctx.h, W1.ctypes.data_as(fp), None))
             return
         W2 = np.ascontiguousarray(W2, np.float32)
@@ -187,11 +195,11 @@ class PressureSolver:
 
 def train_learned_preconditioner(order, tau_coef=1.0, n_interior=2000, n_rhs=16, epochs=(15, 10), lr=(1e-3, 3e-4),
                                  snapshots=(1, 2, 3, 5, 8, 13, 21, 34, 55, 89, 144, 233, 377), form="schwarz",
-                                 hidden=None, seed=11):
+                                 hidden=None, seed=11, slope=None):
     """Trains the learned preconditioner on a small seeded Delaunay mesh from
     residuals of this solver's own block-Jacobi PCG (the network is local,
     so the weights transfer to larger meshes).  Returns (W1, W2, info); W2 is
-    None for the Schwarz form."""
+    None for the Schwarz forms."""
     import time
 
     from .mesh import delaunay_square
@@ -200,6 +208,8 @@ def train_learned_preconditioner(order, tau_coef=1.0, n_interior=2000, n_rhs=16,
     mesh = delaunay_square(n_interior, seed=seed)
     ps = PressureSolver(mesh, order, tau_coef=tau_coef)
     ps.lpc_setup(hidden=hidden, seed=0, capacity=n_rhs * len(snapshots), form=form)
+    if slope is not None:
+        ps.lpc_set_slope(slope)
     rhs = [poisson_rhs(mesh, order, seed=100 + i)[0] for i in range(n_rhs)]
     n = ps.lpc_collect(rhs, snapshots=snapshots)
     losses = []
@@ -208,5 +218,7 @@ def train_learned_preconditioner(order, tau_coef=1.0, n_interior=2000, n_rhs=16,
     W1, W2 = ps.lpc_weights()
     info = {"train_K": ps.K, "residuals": n, "loss": losses[-1][0], "loss_block_jacobi": losses[-1][1],
             "seconds": time.perf_counter() - t0, "form": form, "hidden": ps.lpc_hidden}
+    if slope is not None:
+        info["slope"] = slope
     ps.ctx.close()
     return W1, W2, info

@@ -282,10 +282,16 @@ int dg_pcg_solve_device(dg_ctx* ctx, const double* b_dev, double* x_dev, double 
  *     additive-Schwarz preconditioner M r = P r + sum_m G_m^T W^T W G_m r, G_m
  *     the residual on element m and its rotated neighbours, W (hidden x 4 Np,
  *     hidden 32 or 64, N <= 6), SPD by construction (plain CG); the tensor
- *     cores run its local stage at hidden 32.  DG_LPC_RELU (the network above)
+ *     cores run its local stage at hidden 32.  DG_LPC_SCHWARZ_MLP: the same
+ *     gather with a two-layer network of tied weights between, M r = P r +
+ *     sum_m G_m^T W^T relu(W G_m r), W (128 x 4 Np, N <= 6) in BF16; every
+ *     term is >= 0 against r (r.M(r) > 0), M is not linear, and the solve
+ *     uses the flexible beta; its local stage and its training gradient run
+ *     as BF16 tensor-core (tcgen05) kernels.  DG_LPC_RELU (the network above)
  *     or DG_LPC_LINEAR (identity activation, no metric features) correct the
- *     block-Jacobi output instead; they are not SPD.  For DG_LPC_SCHWARZ the
- *     weights are W1 = W only (W2 / gW2 arguments may be NULL).
+ *     block-Jacobi output instead; they are not SPD.  For the two Schwarz
+ *     forms the weights are W1 = W only (W2 / gW2 arguments may be NULL);
+ *     DG_PC_LEARNED_MULTILEVEL takes DG_LPC_SCHWARZ only.
  *   dg_lpc_add_residual: one residual r = b - S x of the method's own PCG
  *     (host array, reference node order), stored scaled to r.P r = 1.
  *   dg_lpc_train: Adam epochs, one step per stored residual, minimising the
@@ -304,8 +310,11 @@ int dg_pcg_solve_device(dg_ctx* ctx, const double* b_dev, double* x_dev, double 
  *     per output), a direct check of the backward kernels.
  *   dg_lpc_apply: z = M(r) once (host arrays of K*Np doubles, reference node
  *     order). */
-enum { DG_LPC_RELU = 0, DG_LPC_LINEAR = 1, DG_LPC_SCHWARZ = 2 };
+enum { DG_LPC_RELU = 0, DG_LPC_LINEAR = 1, DG_LPC_SCHWARZ = 2, DG_LPC_SCHWARZ_MLP = 3 };
 int dg_lpc_setup(dg_ctx* ctx, int hidden, unsigned long long seed, int capacity, int form);
+/* Activation of DG_LPC_SCHWARZ_MLP: max(h, slope h), slope in [0, 1]
+ * (default 0, relu; 1 makes M linear and symmetric). */
+int dg_lpc_set_slope(dg_ctx* ctx, double slope);
 int dg_lpc_add_residual(dg_ctx* ctx, const double* r_host);
 int dg_lpc_train(dg_ctx* ctx, int epochs, double lr, unsigned long long seed, double* final_loss,
                  double* final_loss_bj);

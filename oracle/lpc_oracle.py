@@ -1,8 +1,8 @@
 """CPU restatement of the learned element-block preconditioner (numpy).
 
 TEST INFRASTRUCTURE ONLY: the checker for the library's BF16 training and
-inference kernels (hopefoam_gb300/csrc/lpc.cu).  Nothing in the product path
-imports this module.
+inference kernels (hopefoam_gb300/csrc/lpc.cu, schwarz_tc.cu,
+schwarz_mlp.cu).  Nothing in the product path imports this module.
 
 The learned preconditioner has no counterpart in the reference (its pressure
 solve hands the assembled matrix to PETSc KSP with a jacobi / LU
@@ -239,3 +239,61 @@ def schwarz_energy_gradients(W, r_ring, zb_ring, EToE, EToF, perm, S_apply_ring)
     A = schwarz_gather(g, EToE, EToF, perm)
     C = X.T @ A + A.T @ X
     return (2 * a / b) * (W.astype(np.float64) @ C), -(a * a) / b
+
+
+# ---------------------------------------------------------------------------
+# Two-layer learned additive-Schwarz form (tied weights, leaky relu between):
+#     M(r) = P r + sum_m G_m^T W^T act(W G_m r),   W: 128 x 4 Np in BF16,
+#     act(h) = max(h, slope h), slope in [0, 1] (0: relu).
+# Every term is >= 0 against r, M is positively homogeneous but not linear.
+# The kernels compute the local stage with BF16 hi + lo operands (FP32
+# accuracy) and the training gradient with X = G r, A = G g, h = relu(X W^T)
+# and D (W a) rounded to BF16 once, FP32 accumulation.
+
+
+def _leaky(P, slope):
+    return np.maximum(P, slope * P)
+
+
+def schwarz_mlp_apply(W, r_ring, zb_ring, EToE, EToF, perm, exact=False, slope=0.0):
+    """M(r) in ring order; W rounded to BF16 unless exact."""
+    Wb = np.asarray(W, np.float64) if exact else bf16(W).astype(np.float64)
+    X = schwarz_gather(r_ring, EToE, EToF, perm)
+    U = _leaky(X @ Wb.T, slope) @ Wb
+    return zb_ring + schwarz_scatter(U, EToE, EToF, perm)
+
+
+def schwarz_mlp_loss(W, r_ring, zb_ring, EToE, EToF, perm, S_apply_ring, exact=True, slope=0.0):
+    """The energy loss -(r.z)|r.z| / (z.S z) of z = M(r)."""
+    z = schwarz_mlp_apply(W, r_ring, zb_ring, EToE, EToF, perm, exact=exact, slope=slope)
+    a = float((r_ring * z).sum())
+    b = float((z * S_apply_ring(z)).sum())
+    return -a * abs(a) / b
+
+
+def schwarz_mlp_energy_gradients(W, r_ring, zb_ring, EToE, EToF, perm, S_apply_ring, exact=False, slope=0.0):
+    """dL/dW = (2a/b) sum_m [h_m a_m^T + (D_m W a_m) x_m^T] with x_m = G_m r,
+    a_m = G_m g, g = (a/b) S z - r, h_m = act(W x_m), D_m = diag act'(W x_m)
+    (1 where W x_m > 0, else slope), and the loss -(a^2)/b.  exact=False
+    applies the kernels' rounding rules (W, X, A, h and D W a in BF16);
+    exact=True is the FP64 derivative."""
+    z = schwarz_mlp_apply(W, r_ring, zb_ring, EToE, EToF, perm, exact=exact, slope=slope)
+    w = S_apply_ring(z)
+    a = float((r_ring * z).sum())
+    b = float((z * w).sum())
+    g = (a / b) * w - r_ring
+    X = schwarz_gather(r_ring, EToE, EToF, perm)
+    A = schwarz_gather(g, EToE, EToF, perm)
+    if exact:
+        Wb = np.asarray(W, np.float64)
+    else:
+        Wb = bf16(W).astype(np.float64)
+        X = bf16(X.astype(np.float32)).astype(np.float64)
+        A = bf16(A.astype(np.float32)).astype(np.float64)
+    P = X @ Wb.T
+    h = _leaky(P, slope)
+    Bm = (A @ Wb.T) * np.where(P > 0, 1.0, slope)
+    if not exact:
+        h = bf16(h.astype(np.float32)).astype(np.float64)
+        Bm = bf16(Bm.astype(np.float32)).astype(np.float64)
+    return (2 * a / b) * (h.T @ A + Bm.T @ X), -(a * a) / b

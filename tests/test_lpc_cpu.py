@@ -89,3 +89,65 @@ def test_schwarz_scatter_is_the_transpose_of_gather():
         lhs = float((lo.schwarz_gather(v, mesh.EToE, mesh.EToF, perm) * Y).sum())
         rhs = float((v * lo.schwarz_scatter(Y, mesh.EToE, mesh.EToF, perm)).sum())
         assert abs(lhs - rhs) <= 1e-12 * max(1.0, abs(lhs))
+
+
+def _mlp_problem(seed=0, N=2):
+    from hopefoam_gb300.euler import reference_operators
+    from hopefoam_gb300.mesh import delaunay_square
+
+    mesh = delaunay_square(30, seed=seed)
+    ops = reference_operators(N)
+    ring = lo.ring_order(N)
+    perm = lo.rotation_perms(ops["r"], ops["s"], ring)
+    Np = ring.size
+    rng = np.random.default_rng(seed + 7)
+    n = mesh.K * Np
+    Q = rng.standard_normal((n, n)) / np.sqrt(n)
+    S = Q @ Q.T + np.eye(n)  # SPD stand-in for the SIPG operator
+
+    def S_ring(z):
+        return (S @ z.reshape(-1)).reshape(z.shape)
+
+    r = rng.standard_normal((mesh.K, Np))
+    zb = rng.standard_normal((mesh.K, Np)) * 0.3
+    W = rng.standard_normal((16, 4 * Np)) * 0.3
+    return mesh, perm, S_ring, r, zb, W
+
+
+@pytest.mark.parametrize("slope", [0.0, 0.3])
+def test_schwarz_mlp_exact_gradients_finite_differences(slope):
+    """dL/dW of the two-layer Schwarz form against central differences of its
+    energy loss (FP64, no rounding), relu and leaky activation."""
+    mesh, perm, S_ring, r, zb, W = _mlp_problem()
+    args = (r, zb, mesh.EToE, mesh.EToF, perm, S_ring)
+    g, L0 = lo.schwarz_mlp_energy_gradients(W, *args, exact=True, slope=slope)
+    assert abs(L0 - lo.schwarz_mlp_loss(W, *args, slope=slope)) <= 1e-12 * abs(L0)
+    rng = np.random.default_rng(3)
+    eps = 1e-6
+    for _ in range(16):
+        i = tuple(rng.integers(0, n) for n in W.shape)
+        old = W[i]
+        W[i] = old + eps
+        Lp = lo.schwarz_mlp_loss(W, *args, slope=slope)
+        W[i] = old - eps
+        Lm = lo.schwarz_mlp_loss(W, *args, slope=slope)
+        W[i] = old
+        fd = (Lp - Lm) / (2 * eps)
+        assert abs(fd - g[i]) <= 1e-5 * max(1.0, abs(fd)), (i, fd, g[i])
+
+
+def test_schwarz_mlp_positive_and_rounding_rules():
+    """r . (M(r) - P r) >= 0 for every r (tied weights), M(a r) = a M(r) for
+    a > 0, and the kernels' BF16 rules stay within 3 % of the exact gradient."""
+    mesh, perm, S_ring, r, zb, W = _mlp_problem(seed=1)
+    rng = np.random.default_rng(5)
+    for _ in range(5):
+        v = rng.standard_normal(r.shape)
+        corr = lo.schwarz_mlp_apply(W, v, np.zeros_like(v), mesh.EToE, mesh.EToF, perm, exact=True)
+        assert float((v * corr).sum()) >= 0.0
+        c2 = lo.schwarz_mlp_apply(W, 2.5 * v, np.zeros_like(v), mesh.EToE, mesh.EToF, perm, exact=True)
+        assert np.allclose(c2, 2.5 * corr, rtol=1e-12, atol=1e-12)
+    args = (r, zb, mesh.EToE, mesh.EToF, perm, S_ring)
+    g, _ = lo.schwarz_mlp_energy_gradients(W, *args, exact=True)
+    gb, _ = lo.schwarz_mlp_energy_gradients(W, *args, exact=False)
+    assert np.linalg.norm(gb - g) / np.linalg.norm(g) < 3e-2

@@ -195,3 +195,94 @@ def test_training_gains_and_solve(gpu_lib):
         assert stl["rel_residual"] <= 1e-10 and stl["iterations"] < st["iterations"]
         assert stl["iterations"] <= 1.2 * stm["iterations"]
         assert rel_l2(xl, xb) < 1e-8
+
+
+def _s_ring(orc, diag, off, ring, Np):
+    def S_ring(z_ring):
+        zr = np.empty_like(z_ring)
+        zr[:, ring] = z_ring
+        y = -orc.blk_apply(diag, off, zr.reshape(-1)).reshape(-1, Np)
+        return y[:, ring]
+    return S_ring
+
+
+@pytest.mark.parametrize("N,n_interior", [(1, 200), (3, 200), (4, 200), (6, 200), (4, 12000)])
+def test_schwarz_mlp_apply_matches_oracle(gpu_lib, N, n_interior):
+    """The tensor-core local stage of the two-layer form (BF16 hi + lo
+    operands, FP32 accumulation) against the FP64 restatement: rel L2 2e-5
+    of z and 1e-4 of the network's part (n_interior 12000: more tiles than
+    CTAs, so each CTA runs several tiles)."""
+    from oracle import lpc_oracle as lo
+
+    mesh, ps, _, diag, _ = _setup(n_interior=n_interior, N=N, form="mlp", hidden=128)
+    rng = np.random.default_rng(8 + N)
+    W = (rng.standard_normal((128, 4 * ps.Np)) * 0.1).astype(np.float32)
+    ps.lpc_set_weights(W)
+    ring, perm = _ring_tools(N)
+    r = rng.standard_normal(ps.K * ps.Np)
+    z = ps.lpc_apply(r).reshape(ps.K, ps.Np)
+    zb_ring = lo.block_jacobi32(-diag, r)[:, ring]
+    z_ring = lo.schwarz_mlp_apply(W, r.reshape(-1, ps.Np)[:, ring], zb_ring, mesh.EToE, mesh.EToF, perm)
+    z_ref = np.empty_like(z_ring)
+    z_ref[:, ring] = z_ring
+    zbr = np.empty_like(zb_ring)
+    zbr[:, ring] = zb_ring
+    assert rel_l2(z - zbr, z_ref - zbr) < 1e-4, rel_l2(z - zbr, z_ref - zbr)
+    assert rel_l2(z, z_ref) < 2e-5, rel_l2(z, z_ref)
+
+
+@pytest.mark.parametrize("N,n_interior,slope", [(3, 300, 0.0), (4, 300, 0.0), (4, 12000, 0.0), (4, 300, 0.5)])
+def test_schwarz_mlp_energy_gradients_match_oracle(gpu_lib, N, n_interior, slope):
+    """The BF16 tensor-core weight gradient against the restatement under the
+    same rounding rules (rel L2 5e-3: a BF16 rounding or a relu mask may fall
+    differently where the FP32 sums differ in the last bit) and against the
+    exact FP64 gradient (rel L2 3e-2); n_interior 12000: several tiles per
+    CTA."""
+    from oracle import lpc_oracle as lo
+
+    mesh, ps, orc, diag, off = _setup(n_interior=n_interior, N=N, form="mlp", hidden=128)
+    rng = np.random.default_rng(12 + N)
+    W = (rng.standard_normal((128, 4 * ps.Np)) * 0.05).astype(np.float32)
+    ps.lpc_set_weights(W)
+    ps.lpc_set_slope(slope)
+    ring, perm = _ring_tools(N)
+    r = rng.standard_normal(ps.K * ps.Np)
+    g1, g2, loss = ps.lpc_energy_gradients(r)
+    assert g2 is None
+    Np = ps.Np
+    S_ring = _s_ring(orc, diag, off, ring, Np)
+    zb_ring = lo.block_jacobi32(-diag, r)[:, ring]
+    args = (r.reshape(-1, Np)[:, ring], zb_ring, mesh.EToE, mesh.EToF, perm, S_ring)
+    o1, oloss = lo.schwarz_mlp_energy_gradients(W, *args, slope=slope)
+    e1, _ = lo.schwarz_mlp_energy_gradients(W, *args, exact=True, slope=slope)
+    assert rel_l2(g1, o1) < 5e-3, rel_l2(g1, o1)
+    assert rel_l2(g1, e1) < 3e-2, rel_l2(g1, e1)
+    assert abs(loss - oloss) <= 1e-4 * abs(oloss)
+
+
+def test_schwarz_mlp_training_and_solve(gpu_lib):
+    """The two-layer form trained on the solver's own residuals with the
+    tensor-core kernels: its energy loss ends below block Jacobi's, and its
+    flexible PCG reaches 1e-10 on its own in fewer iterations than
+    block-Jacobi PCG, at the same solution."""
+    from hopefoam_gb300 import _lib as L
+    from hopefoam_gb300.poisson import poisson_rhs
+
+    snaps = (1, 2, 3, 5, 8, 13, 21, 34, 55, 89, 144, 233)
+    mesh, ps, _, _, _ = _setup(n_interior=800, N=3, hidden=128, capacity=8 * len(snaps), form="mlp")
+    rhs = [poisson_rhs(mesh, 3, seed=40 + i)[0] for i in range(8)]
+    assert ps.lpc_collect(rhs, snapshots=snaps) == 8 * len(snaps)
+    ps.lpc_train(epochs=15, lr=1e-3, seed=0)
+    loss, loss_bj = ps.lpc_train(epochs=10, lr=3e-4, seed=1)
+    assert loss < 1.5 * loss_bj, (loss, loss_bj)
+    b = poisson_rhs(mesh, 3, seed=99)[0]
+    x, st = ps.solve(b, rtol=1e-10, pc=L.DG_PC_LEARNED_ONLY, maxit=5000)
+    xb, stb = ps.solve(b, rtol=1e-10, pc=L.DG_PC_BLOCK_JACOBI, maxit=5000)
+    print("two-layer learned %d, block Jacobi %d iterations; loss %.3f (block Jacobi %.3f)" %
+          (st["iterations"], stb["iterations"], loss, loss_bj))
+    assert st["rel_residual"] <= 1e-10 and st["iterations"] > 0
+    assert st["iterations"] < stb["iterations"], (st["iterations"], stb["iterations"])
+    assert rel_l2(x, xb) < 1e-8
+    # the coarse-space combination takes the linear form only
+    with pytest.raises(L.DGError):
+        ps.solve(b, rtol=1e-10, pc=L.DG_PC_LEARNED_MULTILEVEL, maxit=10)

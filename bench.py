@@ -1064,6 +1064,22 @@ def profile_target(name, small=False):
                          raise_on_fail=False)
         out.update({"K": mesh.K, "training": info, "iterations": st["iterations"], "ms": st["ms"]})
         ps.ctx.close()
+    elif name == "learned_solve":
+        # the learned iteration's kernels without the training phase: small
+        # random weights (the kernels' cost does not depend on their values)
+        from hopefoam_gb300.mesh import delaunay_square
+        from hopefoam_gb300.poisson import PressureSolver, poisson_rhs
+
+        mesh = delaunay_square(12000 if small else 50000, seed=0)
+        ps = PressureSolver(mesh, 4, tau_coef=1.0)
+        ps.lpc_setup(hidden=32, seed=0, capacity=0, form="schwarz")
+        W = np.random.default_rng(0).standard_normal((32, 4 * ps.Np)).astype(np.float32) * 1e-3
+        ps.lpc_set_weights(W)
+        b, _ = poisson_rhs(mesh, 4, seed=1)
+        _, st = ps.solve(b, rtol=1e-30, maxit=64, pc=L.DG_PC_LEARNED_ONLY, precision=L.DG_PREC_SPLIT,
+                         raise_on_fail=False)
+        out.update({"K": mesh.K, "iterations": st["iterations"], "ms": st["ms"]})
+        ps.ctx.close()
     elif name == "ins":
         out.update(ins_bench(n=64 if small else 128, steps=2, warmup=1, with_cpu=False))
     elif name == "cylinder":
@@ -1097,7 +1113,7 @@ def profile_target(name, small=False):
     print(json.dumps(out))
 
 
-PROFILE_TARGETS = ("pcg", "multilevel", "learned", "ins", "cylinder", "limiter", "batch", "split")
+PROFILE_TARGETS = ("pcg", "multilevel", "learned", "learned_solve", "ins", "cylinder", "limiter", "batch", "split")
 
 
 def _split_ready(ctx):

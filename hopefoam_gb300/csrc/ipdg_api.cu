@@ -183,8 +183,10 @@ int run_cg(dg_ctx* c, const PcgVecs& v, bool fp32, double tol2, int limit, const
     *stop = 0;
     *iters = 0;
     // learned mode: give up when the best residual has not halved over a window
-    // (the caller then falls back to block Jacobi instead of running to maxit)
-    const int STALL = 256;
+    // (the caller then falls back to block Jacobi instead of running to maxit);
+    // with a linear SPD learned form CG cannot break down and the residual norm
+    // may plateau for long stretches, so the window is wider
+    const int STALL = (schwarz_form(s->lpc_form) && !s->sw.flex) ? 2048 : 256;
     double best_rr = -1.0;
     int best_it = 0;
     // A batch of CHECK iterations is ~20 kernels per iteration; on small

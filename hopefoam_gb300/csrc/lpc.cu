@@ -445,12 +445,15 @@ __global__ void __launch_bounds__(SchwarzLocalDims<NP, H>::THREADS, SchwarzLocal
 }
 
 // z_k = zb_k + (G^T U)_k, one thread per element row; the FP32 offset mirror
-// of z is that of zb (written by the PCG update) plus c - c0 in FP32; partial
-// sums of r.z for the CG scalars (the linear form is SPD: the standard beta
-// applies; the two-layer form (a.flex) also sums r.z_old, read from z before
-// it is overwritten, for the flexible beta).  Up to Np = 32 each warp holds whole elements (32 / Np of them)
-// and an element's c0 reaches its rows by a shuffle; beyond that, element
-// groups of 256 / Np rows exchange it through shared memory.
+// of z is that of zb (written by the PCG update) plus c - c0 in FP32 (no FP64
+// operation: forming it from z itself costs two FP64-pipe slots per row);
+// partial sums of r.z for the CG scalars (the linear form is SPD: the
+// standard beta applies; the two-layer form (FLEX) also sums r.z_old, read
+// from z before it is overwritten, for the flexible beta).  Up to Np = 32
+// each warp holds whole elements (32 / Np of them) and an element's c0
+// reaches its rows by a shuffle; beyond that, element groups of 256 / Np
+// rows exchange it through shared memory.
+template <bool FLEX>
 __global__ void schwarz_collect_kernel(SchwarzArgs a, const double* __restrict__ zb, const float* __restrict__ U,
                                        const double* __restrict__ r, double* __restrict__ z, float* __restrict__ dz,
                                        int mode, PcgScalars* S, double* part) {
@@ -472,7 +475,7 @@ __global__ void schwarz_collect_kernel(SchwarzArgs a, const double* __restrict__
     }
     const int lb = lane - q;  // lane of the element's row 0 (warp-aligned layout)
     const int ngroups = (a.K + EB - 1) / EB;
-    const bool flex = a.flex && mode == LPC_PCG_ITERATION;
+    const bool flex = FLEX && mode == LPC_PCG_ITERATION;
     double rz = 0, rzo = 0;
     for (int grp = blockIdx.x; grp < ngroups; grp += gridDim.x) {
         const int k = grp * EB + e;
@@ -509,10 +512,18 @@ __global__ void schwarz_collect_kernel(SchwarzArgs a, const double* __restrict__
         }
     }
     if (mode == LPC_APPLY) return;
-    double val[2] = {rz, rzo}, tot[2];
-    if (grid_sum<2>(val, part, gridDim.x, &S->counter, tot) && threadIdx.x == 0) {
-        if (mode == LPC_PCG_ITERATION) pcg_finish(S, tot[0], tot[1], S->rr);
-        else S->rz = tot[0];
+    if (FLEX) {
+        double val[2] = {rz, rzo}, tot[2];
+        if (grid_sum<2>(val, part, gridDim.x, &S->counter, tot) && threadIdx.x == 0) {
+            if (mode == LPC_PCG_ITERATION) pcg_finish(S, tot[0], tot[1], S->rr);
+            else S->rz = tot[0];
+        }
+    } else {
+        double val[1] = {rz}, tot[1];
+        if (grid_sum<1>(val, part, gridDim.x, &S->counter, tot) && threadIdx.x == 0) {
+            if (mode == LPC_PCG_ITERATION) pcg_finish(S, tot[0], 0.0, S->rr);
+            else S->rz = tot[0];
+        }
     }
 }
 
@@ -626,7 +637,10 @@ cudaError_t launch_schwarz_collect(const SchwarzArgs& a, const double* zb, const
     const int threads = wa ? 256 : (EB * a.Np + 31) / 32 * 32;
     const int ngroups = (a.K + EB - 1) / EB;
     const int grid = ngroups < 8 * a.sms ? ngroups : 8 * a.sms;
-    schwarz_collect_kernel<<<grid, threads, 0, st>>>(a, zb, U, r, z, dz, mode, S, part);
+    if (a.flex)
+        schwarz_collect_kernel<true><<<grid, threads, 0, st>>>(a, zb, U, r, z, dz, mode, S, part);
+    else
+        schwarz_collect_kernel<false><<<grid, threads, 0, st>>>(a, zb, U, r, z, dz, mode, S, part);
     return cudaGetLastError();
 }
 

@@ -259,8 +259,10 @@ __global__ void __launch_bounds__(128, 1) schwarz_mlp_local_kernel(SchwarzArgs a
             umma::tmem_ld8(tD2 + lane_base + c8 * 8, u);
             umma::tmem_ld_wait();
 #pragma unroll
-            for (int q = 0; q < 8; q++)
-                if (c8 * 8 + q < F) sU[tid * F + c8 * 8 + q] = u[q];
+            for (int q4 = 0; q4 < 2; q4++)
+                if (c8 * 8 + 4 * q4 < F)
+                    *reinterpret_cast<float4*>(sU + tid * F + c8 * 8 + 4 * q4) =
+                        make_float4(u[4 * q4], u[4 * q4 + 1], u[4 * q4 + 2], u[4 * q4 + 3]);
         }
         umma::fence_before_sync();
         __syncthreads();

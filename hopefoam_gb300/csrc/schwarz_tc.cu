@@ -43,6 +43,39 @@ struct SchwarzTcDims {
     static_assert(SMEM <= 232448, "shared memory budget");
 };
 
+// X row of element m: the residual on the element and its three rotated
+// neighbours (zero for m >= K and across a boundary)
+template <int NP>
+__device__ __forceinline__ void tc_gather(const SchwarzArgs& a, const float* __restrict__ r32,
+                                          const double* __restrict__ r, int m, float* x) {
+    if (m >= a.K) {
+#pragma unroll
+        for (int i = 0; i < 4 * NP; i++) x[i] = 0.f;
+        return;
+    }
+    if (r32) {
+        const float* vm = r32 + (size_t)m * NP;
+#pragma unroll
+        for (int i = 0; i < NP; i++) x[i] = vm[i];
+    } else {
+        const double* vm = r + (size_t)m * NP;
+#pragma unroll
+        for (int i = 0; i < NP; i++) x[i] = (float)vm[i];
+    }
+#pragma unroll
+    for (int f = 0; f < 3; f++) {
+        const int c = a.conn[(size_t)m * 3 + f];
+        const int* pm = a.perm + (c & 3) * NP;
+        const size_t nb = (size_t)(c >= 0 ? (c >> 3) : 0) * NP;
+#pragma unroll
+        for (int i = 0; i < NP; i++) {
+            float v = 0.f;
+            if (c >= 0) v = r32 ? r32[nb + pm[i]] : (float)r[nb + pm[i]];
+            x[(f + 1) * NP + i] = v;
+        }
+    }
+}
+
 }  // namespace
 
 template <int NP>
@@ -96,45 +129,24 @@ __global__ void __launch_bounds__(128, 1) schwarz_local_tc_kernel(SchwarzArgs a,
     bool failed = false;
     const int ntiles = (a.K + 127) / 128;
 
+    // X rows are gathered one tile ahead: the next tile's loads are in flight
+    // while this tile's MMAs, activations and stores run
+    float x[F];
+    if (blockIdx.x < ntiles) tc_gather<NP>(a, r32, r, blockIdx.x * 128 + tid, x);
     for (int tile = blockIdx.x; tile < ntiles && !failed; tile += gridDim.x) {
-        const int m = tile * 128 + tid;
-        const bool act = m < a.K;
-        // (1) X row of element m: the residual on the element and its three rotated neighbours
+        // (1) X row of element tile * 128 + tid as TF32 hi + lo
         {
-            float x[F];
-            if (act) {
-                if (r32) {
-                    const float* vm = r32 + (size_t)m * NP;
+            // four consecutive k per 16-byte store: eight threads of a phase
+            // write 128 contiguous bytes (no bank conflicts)
 #pragma unroll
-                    for (int i = 0; i < NP; i++) x[i] = vm[i];
-                } else {
-                    const double* vm = r + (size_t)m * NP;
+            for (int i4 = 0; i4 < KP1 / 4; i4++) {
+                float hi[4] = {0.f, 0.f, 0.f, 0.f}, lo[4] = {0.f, 0.f, 0.f, 0.f};
 #pragma unroll
-                    for (int i = 0; i < NP; i++) x[i] = (float)vm[i];
-                }
-#pragma unroll
-                for (int f = 0; f < 3; f++) {
-                    const int c = a.conn[(size_t)m * 3 + f];
-                    const int* pm = a.perm + (c & 3) * NP;
-                    const size_t nb = (size_t)(c >= 0 ? (c >> 3) : 0) * NP;
-#pragma unroll
-                    for (int i = 0; i < NP; i++) {
-                        float v = 0.f;
-                        if (c >= 0) v = r32 ? r32[nb + pm[i]] : (float)r[nb + pm[i]];
-                        x[(f + 1) * NP + i] = v;
-                    }
-                }
-            } else {
-#pragma unroll
-                for (int i = 0; i < F; i++) x[i] = 0.f;
-            }
-#pragma unroll
-            for (int i = 0; i < KP1; i++) {
-                float hi = 0.f, lo = 0.f;
-                if (i < F) umma::split_tf32(x[i], hi, lo);
-                const uint32_t off = umma::kmajor_offset(tid, i, KP1) >> 2;
-                sA[off] = hi;
-                sA[off + LO1 / 4] = lo;
+                for (int q = 0; q < 4; q++)
+                    if (4 * i4 + q < F) umma::split_tf32(x[4 * i4 + q], hi[q], lo[q]);
+                const uint32_t off = umma::kmajor_offset(tid, 4 * i4, KP1) >> 2;
+                *reinterpret_cast<float4*>(sA + off) = make_float4(hi[0], hi[1], hi[2], hi[3]);
+                *reinterpret_cast<float4*>(sA + off + LO1 / 4) = make_float4(lo[0], lo[1], lo[2], lo[3]);
             }
         }
         umma::fence_async_smem();
@@ -152,6 +164,7 @@ __global__ void __launch_bounds__(128, 1) schwarz_local_tc_kernel(SchwarzArgs a,
             }
             umma::commit(bar1);
         }
+        if (tile + (int)gridDim.x < ntiles) tc_gather<NP>(a, r32, r, (tile + gridDim.x) * 128 + tid, x);
         bool ok = umma::mbar_wait(bar1, ph, kTcWaitLimit);
         if (__syncthreads_or(!ok)) { failed = true; break; }
         umma::fence_after_sync();
@@ -162,12 +175,13 @@ __global__ void __launch_bounds__(128, 1) schwarz_local_tc_kernel(SchwarzArgs a,
             umma::tmem_ld8(tD1 + lane_base + c8 * 8, h);
             umma::tmem_ld_wait();
 #pragma unroll
-            for (int q = 0; q < 8; q++) {
-                float hi, lo;
-                umma::split_tf32(h[q], hi, lo);
-                const uint32_t off = umma::kmajor_offset(tid, c8 * 8 + q, KP2) >> 2;
-                sA[off] = hi;
-                sA[off + LO2 / 4] = lo;
+            for (int q4 = 0; q4 < 2; q4++) {
+                float hi[4], lo[4];
+#pragma unroll
+                for (int q = 0; q < 4; q++) umma::split_tf32(h[4 * q4 + q], hi[q], lo[q]);
+                const uint32_t off = umma::kmajor_offset(tid, c8 * 8 + 4 * q4, KP2) >> 2;
+                *reinterpret_cast<float4*>(sA + off) = make_float4(hi[0], hi[1], hi[2], hi[3]);
+                *reinterpret_cast<float4*>(sA + off + LO2 / 4) = make_float4(lo[0], lo[1], lo[2], lo[3]);
             }
         }
         umma::fence_async_smem();
@@ -197,9 +211,13 @@ __global__ void __launch_bounds__(128, 1) schwarz_local_tc_kernel(SchwarzArgs a,
             float u[8];
             umma::tmem_ld8(tD2 + lane_base + c8 * 8, u);
             umma::tmem_ld_wait();
+            // F % 4 == 0: whole float4 groups (rows of F / 4 groups; the 16-byte
+            // stride of F floats between threads spreads a phase over all banks)
 #pragma unroll
-            for (int q = 0; q < 8; q++)
-                if (c8 * 8 + q < F) sU[tid * F + c8 * 8 + q] = u[q];
+            for (int q4 = 0; q4 < 2; q4++)
+                if (c8 * 8 + 4 * q4 < F)
+                    *reinterpret_cast<float4*>(sU + tid * F + c8 * 8 + 4 * q4) =
+                        make_float4(u[4 * q4], u[4 * q4 + 1], u[4 * q4 + 2], u[4 * q4 + 3]);
         }
         umma::fence_before_sync();
         __syncthreads();

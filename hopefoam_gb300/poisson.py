@@ -193,7 +193,7 @@ class PressureSolver:
         return z
 
 
-def train_learned_preconditioner(order, tau_coef=1.0, n_interior=2000, n_rhs=16, epochs=(15, 10), lr=(1e-3, 3e-4),
+def train_learned_preconditioner(order, tau_coef=1.0, n_interior=2000, n_rhs=16, epochs=(10, 10), lr=(1e-3, 3e-4),
                                  snapshots=(1, 2, 3, 5, 8, 13, 21, 34, 55, 89, 144, 233, 377), form="schwarz",
                                  hidden=None, seed=11, slope=None):
     """Trains the learned preconditioner on a small seeded Delaunay mesh from

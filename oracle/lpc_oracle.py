@@ -297,3 +297,51 @@ def schwarz_mlp_energy_gradients(W, r_ring, zb_ring, EToE, EToF, perm, S_apply_r
         h = bf16(h.astype(np.float32)).astype(np.float64)
         Bm = bf16(Bm.astype(np.float32)).astype(np.float64)
     return (2 * a / b) * (h.T @ A + Bm.T @ X), -(a * a) / b
+
+
+# ---------------------------------------------------------------------------
+# The same additive-Schwarz form without learning: W^T W = theta * C with C the
+# mean over interior patches of the inverse of the patch operator G_m S G_m^T
+# (the element and its three rotated neighbours, the gather order of
+# schwarz_gather), the classical overlapping-Schwarz local solve shared by all
+# patches.
+
+
+def schwarz_patch_inverse_mean(S_diag, S_off, EToE, EToF, ring, perm):
+    """C (4 Np x 4 Np) from the SPD operator's element blocks in reference node
+    order: S_diag (K, Np, Np), S_off (K, 3, Np, Np) coupling element k's rows
+    with neighbour EToE[k, f]'s columns.  Only patches with three neighbours
+    enter the mean."""
+    K, Np = S_diag.shape[0], ring.size
+    D = S_diag[:, ring][:, :, ring]
+    O = S_off[:, :, ring][:, :, :, ring]
+    F = 4 * Np
+    ar = np.arange(K)
+    interior = (EToE >= 0).all(1) & (EToE != ar[:, None]).all(1)
+    Sp = np.zeros((K, F, F))
+    Sp[:, :Np, :Np] = D
+    for f in range(3):
+        nb = EToE[:, f]
+        ok = (nb >= 0) & (nb != ar)
+        fn = np.where(ok, EToF[:, f], 0)
+        nbc = np.where(ok, nb, 0)
+        pm = perm[fn]
+        blk = O[:, f][ar[:, None], :, pm].transpose(0, 2, 1)
+        blk[~ok] = 0
+        Sp[:, :Np, (f + 1) * Np:(f + 2) * Np] = blk
+        Sp[:, (f + 1) * Np:(f + 2) * Np, :Np] = blk.transpose(0, 2, 1)
+        Dn = D[nbc][ar[:, None, None], pm[:, :, None], pm[:, None, :]]
+        Dn[~ok] = np.eye(Np)
+        Sp[:, (f + 1) * Np:(f + 2) * Np, (f + 1) * Np:(f + 2) * Np] = Dn
+    return np.linalg.inv(Sp[interior]).mean(0)
+
+
+def schwarz_weights_from(C, theta, rows):
+    """W (rows x F) with W^T W = theta C (C symmetric positive semi-definite)."""
+    lam, V = np.linalg.eigh(C)
+    F = C.shape[0]
+    W = np.zeros((rows, F), np.float32)
+    k = min(rows, F)
+    order = np.argsort(lam)[::-1][:k]
+    W[:k] = (np.sqrt(theta * np.maximum(lam[order], 0.0))[:, None] * V[:, order].T).astype(np.float32)
+    return W

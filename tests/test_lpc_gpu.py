@@ -286,3 +286,38 @@ def test_schwarz_mlp_training_and_solve(gpu_lib):
     # the coarse-space combination takes the linear form only
     with pytest.raises(L.DGError):
         ps.solve(b, rtol=1e-10, pc=L.DG_PC_LEARNED_MULTILEVEL, maxit=10)
+
+
+def test_learned_gains_over_same_form_without_learning(gpu_lib):
+    """What training adds: the learned Schwarz form against the same form with
+    a hand-built local map, W^T W = theta C, C the mean inverse of the
+    interior patch operators of this mesh (the classical overlapping-Schwarz
+    local solve shared by the patches, full rank, best theta of four), both
+    to 1e-10 with plain CG.  The learned weights come from the training mesh
+    (another mesh) and still need fewer iterations."""
+    from hopefoam_gb300 import _lib as L
+    from hopefoam_gb300.poisson import PressureSolver, poisson_rhs, train_learned_preconditioner
+    from oracle import lpc_oracle as lo
+
+    N = 3
+    mesh, ps, _, diag, off = _setup(n_interior=800, N=N, hidden=32, form="schwarz")
+    ring, perm = _ring_tools(N)
+    C = lo.schwarz_patch_inverse_mean(-diag, -off, mesh.EToE, mesh.EToF, ring, perm)
+    W, _, _ = train_learned_preconditioner(N, tau_coef=TAU, form="schwarz", hidden=32)
+    ps.lpc_set_weights(W)
+    b = poisson_rhs(mesh, N, seed=99)[0]
+    x, st = ps.solve(b, rtol=1e-10, pc=L.DG_PC_LEARNED_ONLY, maxit=5000)
+    _, stb = ps.solve(b, rtol=1e-10, pc=L.DG_PC_BLOCK_JACOBI, maxit=5000)
+    best = None
+    for theta in (0.125, 0.25, 0.5, 1.0):
+        p2 = PressureSolver(mesh, N, tau_coef=TAU)
+        p2.lpc_setup(hidden=64, seed=0, capacity=0, form="schwarz")
+        p2.lpc_set_weights(lo.schwarz_weights_from(C, theta, 64))
+        xh, sth = p2.solve(b, rtol=1e-10, pc=L.DG_PC_LEARNED_ONLY, maxit=5000)
+        p2.ctx.close()
+        assert sth["rel_residual"] <= 1e-10 and rel_l2(xh, x) < 1e-8
+        best = sth["iterations"] if best is None else min(best, sth["iterations"])
+    print("learned %d, same form without learning (best theta) %d, block Jacobi %d iterations" %
+          (st["iterations"], best, stb["iterations"]))
+    assert st["rel_residual"] <= 1e-10
+    assert st["iterations"] < 0.8 * best < 0.8 * stb["iterations"], (st["iterations"], best, stb["iterations"])

@@ -73,6 +73,27 @@ __device__ __forceinline__ void lim_prim(const double* a, double* p) {
 }
 
 // (1) cell averages, centres, A0 = 2/3 J (Trianglelimite.C:103-137); q: [K][4][Np]
+// warp-aligned element groups: 32 / Np whole elements per warp (Np <= 32),
+// lane q of an element handles its node q; lb is the lane of node 0
+struct LimLanes {
+    int k, q, lb;
+    bool act;
+};
+__device__ __forceinline__ LimLanes lim_lanes(int Np, int K) {
+    const int lane = threadIdx.x & 31, EW = 32 / Np;
+    const int ew = lane / Np;
+    LimLanes l;
+    l.q = lane - ew * Np;
+    l.lb = ew * Np;
+    l.k = (blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5)) * EW + ew;
+    l.act = ew < EW && l.k < K;
+    return l;
+}
+__host__ __device__ __forceinline__ unsigned lim_lane_blocks(int K, int Np) {
+    const int per_block = 4 * (32 / Np);  // 128 threads
+    return (unsigned)((K + per_block - 1) / per_block);
+}
+
 __global__ void lim_cells_kernel(LimArgs a, const double* __restrict__ q) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= a.K) return;
@@ -216,6 +237,97 @@ __global__ void lim_cv_kernel(LimArgs a, const double* __restrict__ q, const dou
             for (int m = 0; m < 8; m++) a.CV[(size_t)m * a.T + nc] = V[m];
     }
     for (int m = 0; m < 8; m++) a.CV[(size_t)m * a.T + k] = cv[m];
+}
+
+// (3) + (4) with a lane per face (lanes 4e .. 4e + 2 of a warp; lane 4e + 3
+// idle): CellA2 and the area-weighted face gradients, added by the face-0
+// lane in face order (the element-per-thread kernels' bits)
+__global__ void lim_cv_lane_kernel(LimArgs a, const double* __restrict__ q, const double* __restrict__ bnd) {
+    const int lane = threadIdx.x & 31, f = lane & 3, lb = lane & ~3;
+    const int k = (blockIdx.x * blockDim.x + threadIdx.x) >> 2;
+    const bool act = k < a.K && f < 3;
+    double a2t = 0;
+    if (act) {
+        int cn;
+        const int n = lim_nbr_cell(a, k, f, cn);
+        a2t = cn >= 0 ? a.A0[k] + a.A0[n] : a.A0[k] + a.A0[k];
+    }
+    double A2k = 0;
+    for (int g = 0; g < 3; g++) A2k += __shfl_sync(0xffffffffu, a2t, lb + g);
+    double tv[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    if (act) {
+        double V[8], A2;
+        int nc;
+        lim_face_grad(a, q, bnd, k, f, V, A2, nc);
+        for (int m = 0; m < 8; m++) tv[m] = A2 * V[m] / A2k;
+        if (nc >= a.K)
+            for (int m = 0; m < 8; m++) a.CV[(size_t)m * a.T + nc] = V[m];
+    }
+    double cv[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    for (int g = 0; g < 3; g++)
+#pragma unroll
+        for (int m = 0; m < 8; m++) cv[m] += __shfl_sync(0xffffffffu, tv[m], lb + g);
+    if (k < a.K && f == 0) {
+        a.A2c[k] = A2k;
+        for (int m = 0; m < 8; m++) a.CV[(size_t)m * a.T + k] = cv[m];
+    }
+}
+
+// (5) with the element's nodes on its lanes: lanes q < 4 form the weighted
+// gradient of variable q, every lane reconstructs its node
+__global__ void lim_reconstruct_lane_kernel(LimArgs a, double* __restrict__ q) {
+    const LimLanes l = lim_lanes(a.Np, a.K);
+    const int Np = a.Np, k = l.k;
+    const double eps = 1e-10, tol = 1e-2;
+    double Lm0 = 0, Lm1 = 0;  // this lane's variable m = q (q < 4)
+    if (l.act && l.q < 4) {
+        const int m = l.q;
+        int c[3];
+        for (int f = 0; f < 3; f++) {
+            int cn;
+            c[f] = lim_nbr_cell(a, k, f, cn);
+        }
+        double gg[3];
+        for (int i = 0; i < 3; i++) {
+            const double gx = a.CV[(size_t)(2 * m) * a.T + c[i]], gy = a.CV[(size_t)(2 * m + 1) * a.T + c[i]];
+            gg[i] = gx * gx + gy * gy;
+        }
+        const double fac = gg[0] * gg[0] + gg[1] * gg[1] + gg[2] * gg[2];
+        const double w1 = (gg[1] * gg[2] + eps) / (fac + 3 * eps);
+        const double w2 = (gg[0] * gg[2] + eps) / (fac + 3 * eps);
+        const double w3 = (gg[1] * gg[0] + eps) / (fac + 3 * eps);
+        Lm0 = w1 * a.CV[(size_t)(2 * m) * a.T + c[0]] + w2 * a.CV[(size_t)(2 * m) * a.T + c[1]] +
+              w3 * a.CV[(size_t)(2 * m) * a.T + c[2]];
+        Lm1 = w1 * a.CV[(size_t)(2 * m + 1) * a.T + c[0]] + w2 * a.CV[(size_t)(2 * m + 1) * a.T + c[1]] +
+              w3 * a.CV[(size_t)(2 * m + 1) * a.T + c[2]];
+    }
+    double L[4][2];
+#pragma unroll
+    for (int m = 0; m < 4; m++) {
+        L[m][0] = __shfl_sync(0xffffffffu, Lm0, l.lb + m);
+        L[m][1] = __shfl_sync(0xffffffffu, Lm1, l.lb + m);
+    }
+    if (!l.act) return;
+    const double ar = a.avg[k], a1 = a.avg[(size_t)1 * a.T + k], a2 = a.avg[(size_t)2 * a.T + k],
+                 a3 = a.avg[(size_t)3 * a.T + k];
+    const double U = a.prim[(size_t)1 * a.T + k], V = a.prim[(size_t)2 * a.T + k];
+    const int p = l.q;
+    const double dx = a.xn[(size_t)k * Np + p] - a.cx[k], dy = a.yn[(size_t)k * Np + p] - a.cy[k];
+    double du = dx * L[0][0] + dy * L[0][1];
+    const double du1 = dx * L[1][0] + dy * L[1][1];
+    const double du2 = dx * L[2][0] + dy * L[2][1];
+    const double du3 = dx * L[3][0] + dy * L[3][1];
+    double Lrho = ar + du;
+    for (int it = 0; it < 64 && Lrho < tol; it++) {  // the reference loops until positive
+        du *= 0.5;
+        Lrho = ar + du;
+    }
+    double* qk = q + (size_t)k * 4 * Np;
+    qk[p] = Lrho;
+    qk[Np + p] = a1 + ar * du1 + du * U;
+    qk[2 * Np + p] = a2 + ar * du2 + du * V;
+    const double dE = (1 / (kLimGamma - 1)) * du3 + 0.5 * du * (U * U + V * V) + ar * (U * du1 + V * du2);
+    qk[3 * Np + p] = a3 + dE;
 }
 
 // (5) weighted neighbour gradients and the linear reconstruction (Trianglelimite.C:705-858)
@@ -372,11 +484,20 @@ unsigned nblk(size_t n) { return (unsigned)((n + 127) / 128); }
 int run_limiter(dg_ctx* c, double* q, const double* bnd) {
     const LimArgs a = lim_args(c);
     cudaStream_t st = c->stream;
-    lim_cells_kernel<<<nblk(a.K), 128, 0, st>>>(a, q);
-    if (a.nb > 0) lim_ghost_kernel<<<nblk(a.nb), 128, 0, st>>>(a, bnd);
-    lim_a2_kernel<<<nblk(a.K), 128, 0, st>>>(a);
-    lim_cv_kernel<<<nblk(a.K), 128, 0, st>>>(a, q, bnd);
-    lim_reconstruct_kernel<<<nblk(a.K), 128, 0, st>>>(a, q);
+    // element groups on warp lanes (Np in 4..32: N = 2..6); element per thread otherwise
+    // (the element-per-thread kernels run in 32-thread blocks: a few thousand
+    // elements then cover every SM)
+    const bool lanes = a.Np >= 4 && a.Np <= 32;
+    lim_cells_kernel<<<(a.K + 31) / 32, 32, 0, st>>>(a, q);
+    if (a.nb > 0) lim_ghost_kernel<<<(a.nb + 31) / 32, 32, 0, st>>>(a, bnd);
+    if (lanes) {
+        lim_cv_lane_kernel<<<nblk((size_t)a.K * 4), 128, 0, st>>>(a, q, bnd);
+        lim_reconstruct_lane_kernel<<<lim_lane_blocks(a.K, a.Np), 128, 0, st>>>(a, q);
+    } else {
+        lim_a2_kernel<<<(a.K + 31) / 32, 32, 0, st>>>(a);
+        lim_cv_kernel<<<(a.K + 31) / 32, 32, 0, st>>>(a, q, bnd);
+        lim_reconstruct_kernel<<<(a.K + 31) / 32, 32, 0, st>>>(a, q);
+    }
     LIM_CUDA(c, cudaGetLastError());
     return DG_OK;
 }

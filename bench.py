@@ -516,7 +516,8 @@ def summary(line):
             "batched": {"value": ("value",), "frac": ("roofline", "frac"), "ms": ("ms",)},
             "shock": {"fp64_ms": ("fp64", "ms_per_step"), "split_ms": ("split", "ms_per_step"),
                       "cpu_ms": ("cpu_baseline", "ms_per_step")},
-            "ins": {"ms": ("ms_per_step",), "cpu_ms": ("cpu_baseline", "ms_per_step")},
+            "ins": {"ms": ("ms_per_step",), "mixed_ms": ("mixed_solves", "ms_per_step"),
+                    "cpu_ms": ("cpu_baseline", "ms_per_step")},
             "cylinder": {"ms": ("ms_per_step",), "cpu_ms": ("cpu_baseline", "ms_per_step"),
                          "vs_oracle": ("state_vs_oracle",)}}[k].items()}
     return out
@@ -720,6 +721,29 @@ def ins_bench(n=128, order=2, steps=4, warmup=2, with_cpu=True, cpu_steps=2):
                         "bytes_per_pcg_iteration": bytes_it,
                         "note": "PCG iteration bytes x iterations of the step's three solves / step time"}}
     g.close()
+    # the same steps with mixed-precision linear solves (FP32 operator on FP64
+    # offsets, FP64 vectors and recurrences, the same 1e-10 on the true residual)
+    try:
+        from hopefoam_gb300 import _lib as L
+
+        gm = ChorinSolver(mesh, order, nu=0.01, dt=1e-3, precision=L.DG_PREC_SPLIT)
+        pvm = PearsonVortex(gm)
+        gm.set_state(*pvm.initial_state())
+        tm = 0.0
+        for _ in range(warmup):
+            gm.step(pvm.bdata(tm), rtol=1e-10)
+            tm += gm.dt
+        stm = []
+        for _ in range(steps):
+            stm.append(gm.step(pvm.bdata(tm), rtol=1e-10))
+            tm += gm.dt
+        _, pm = gm.get_state()
+        out["mixed_solves"] = {"ms_per_step": float(np.mean([s["ms"] for s in stm])),
+                               "pressure_error_avg_max": pvm.pressure_error(pm, tm),
+                               "iterations_p": [s["iterations_p"] for s in stm]}
+        gm.close()
+    except Exception as exc:
+        out["mixed_solves"] = {"error": str(exc)}
     if with_cpu:
         from hopefoam_gb300.mesh import load_cubature
         from oracle import oracle

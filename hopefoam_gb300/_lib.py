@@ -92,6 +92,7 @@ SIGNATURES = {
     "dg_ins_last_error": (ctypes.c_char_p, [_vp]),
     "dg_ins_set_state": (ctypes.c_int, [_vp, _dp, _dp]),
     "dg_ins_get_state": (ctypes.c_int, [_vp, _dp, _dp]),
+    "dg_ins_set_precision": (ctypes.c_int, [_vp, ctypes.c_int]),
     "dg_ins_step": (ctypes.c_int, [_vp, ctypes.POINTER(InsBdata), ctypes.c_double, ctypes.c_int,
                                    ctypes.POINTER(InsStats)]),
     "dg_ins_operator": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.POINTER(InsBdata), _dp, _dp]),

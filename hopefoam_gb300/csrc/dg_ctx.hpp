@@ -105,7 +105,7 @@ void ipdg_teardown(dg_ctx* c);
 // FP64 block-Jacobi PCG with the context's SIPG operator on ring-order device
 // vectors (x: initial guess in, solution out)
 int ipdg_solve_device(dg_ctx* c, const double* b_dev, double* x_dev, double rtol, int maxit, int* iters,
-                      double* rel, int pc);
+                      double* rel_out, int pc, int precision);
 // the operator's device tables (null before dg_ipdg_setup), the boundary
 // types per slot and the host copy of the face coefficients as built
 const dgk::IpdgArgs* ipdg_args(dg_ctx* c);

@@ -346,6 +346,7 @@ struct dg_ins {
     double nu = 0, dt = 0, mass_coef = -1;
     int nstep = 0;
     int pc = DG_PC_MULTILEVEL;  // block Jacobi when the multilevel preconditioner cannot be built
+    int precision = DG_PREC_FP64;  // of the linear solves (dg_ins_set_precision)
     InsTables t{};
     InsSlots sl{};
     std::vector<void*> allocs;
@@ -488,10 +489,10 @@ int ins_step_n(dg_ins* s, const dg_ins_bdata* bd, double rtol, int maxit, dg_ins
         s->Pg = freed;
         s->nhist = std::min(s->nhist + 1, 3);
     }
-    int rc = ipdg_solve_device(s->cp, s->rhs, s->P, rtol, maxit, &itp, &relp, s->pc);
+    int rc = ipdg_solve_device(s->cp, s->rhs, s->P, rtol, maxit, &itp, &relp, s->pc, s->precision);
     if (rc == DG_ERR_UNSUPPORTED && s->pc == DG_PC_MULTILEVEL) {
         s->pc = DG_PC_BLOCK_JACOBI;  // no multilevel preconditioner on this mesh: block Jacobi
-        rc = ipdg_solve_device(s->cp, s->rhs, s->P, rtol, maxit, &itp, &relp, s->pc);
+        rc = ipdg_solve_device(s->cp, s->rhs, s->P, rtol, maxit, &itp, &relp, s->pc, s->precision);
     }
     if (rc) return insfail(s, rc, std::string("pressure solve: ") + s->cp->err);
     // 5: velocity correction
@@ -515,7 +516,7 @@ int ins_step_n(dg_ins* s, const dg_ins_bdata* bd, double rtol, int maxit, dg_ins
                                                                     s->nstep > 0 ? -1.0 : 0.0, 0.0, s->U + c * KN,
                                                                     s->Uo + c * KN, nullptr, s->sol + c * KN);
         INS_CUDA(s, cudaGetLastError());
-        rc = ipdg_solve_device(s->cu, s->rhs, s->sol + c * KN, rtol, maxit, &itu[c], &relu[c], s->pc);
+        rc = ipdg_solve_device(s->cu, s->rhs, s->sol + c * KN, rtol, maxit, &itu[c], &relu[c], s->pc, s->precision);
         if (rc) return insfail(s, rc, std::string("velocity solve: ") + s->cu->err);
     }
     cudaEventRecord(e1, st);
@@ -647,6 +648,12 @@ int dg_ins_create(const dg_mesh_desc* mesh, const dg_opts* opts, const int* u_ki
     for (double* p : {s->ubnd, s->ugrad}) cudaMemset(p, 0, 2 * nbf * sizeof(double));
     if (cudaDeviceSynchronize() != cudaSuccess) { dg_ins_destroy(s); return DG_ERR_CUDA; }
     *out = s;
+    return DG_OK;
+}
+
+int dg_ins_set_precision(dg_ins* s, int precision) {
+    if (!s || (precision != DG_PREC_FP64 && precision != DG_PREC_SPLIT)) return DG_ERR_ARG;
+    s->precision = precision;
     return DG_OK;
 }
 

@@ -895,10 +895,14 @@ int dg_pcg_solve_device(dg_ctx* c, const double* b_dev, double* x_dev, double rt
 
 }  // extern "C"
 
-// FP64 block-Jacobi PCG on ring-order device vectors (x holds the initial
-// guess and receives the solution); used by the incompressible step
+// PCG on ring-order device vectors (x holds the initial guess and receives
+// the solution); used by the incompressible step.  precision DG_PREC_FP64:
+// FP64 operator and blocks; DG_PREC_SPLIT: the mixed-precision iteration of
+// dg_pcg_solve (FP32 operator on FP64 offsets, FP32 blocks, FP64 vectors and
+// recurrences, true-residual replacement), ending on the true FP64 residual
 int ipdg_solve_device(dg_ctx* c, const double* b_dev, double* x_dev, double rtol, int maxit, int* iters,
-                      double* rel_out, int pc) {
+                      double* rel_out, int pc, int precision) {
+    if (precision != DG_PREC_FP64 && precision != DG_PREC_SPLIT) return ifail(c, DG_ERR_ARG, "unknown precision");
     if (!c->ipdg || !c->ipdg->ready) return ifail(c, DG_ERR_ARG, "dg_ipdg_setup not called");
     IpdgState* s = c->ipdg;
     const bool mgm = pc == DG_PC_MULTILEVEL;
@@ -925,19 +929,21 @@ int ipdg_solve_device(dg_ctx* c, const double* b_dev, double* x_dev, double rtol
         v.Ap = s->d_Ap;
         v.part = s->d_ppart;
         v.nmax = s->nmax;
+        const bool mixed = precision == DG_PREC_SPLIT;
         v.P32 = s->d_P32;
-        v.P64 = s->d_P64;
+        v.P64 = mixed ? nullptr : s->d_P64;
         v.zb = mgm ? s->d_zb : nullptr;
         v.mg = mgm ? &s->mg : nullptr;
         v.S = s->d_S;
-        v.dz = nullptr;
-        v.dp[0] = v.dp[1] = nullptr;
+        v.dz = mixed ? s->d_dz : nullptr;  // the FP32 apply stages from FP32 offset mirrors
+        v.dp[0] = mixed ? s->d_dp : nullptr;
+        v.dp[1] = mixed ? s->d_dp2 : nullptr;
         v.r32 = nullptr;
         v.x = s->d_x;
         rc = apply64(c, s->d_x, s->d_Ap);
         if (rc) return rc;
         IP_CUDA(c, launch_xmy(s->d_r, s->d_b, s->d_Ap, n, c->stream));
-        rc = run_cg(c, v, false, rtol * rtol * bb, maxit, s->d_b, 0, &total_it, &stop);
+        rc = run_cg(c, v, mixed, rtol * rtol * bb, maxit, s->d_b, mixed ? 4 : 0, &total_it, &stop);
         if (rc) return rc;
         rc = apply64(c, s->d_x, s->d_Ap);
         if (rc) return rc;

@@ -29,7 +29,7 @@ class ChorinSolver:
     zeroGradient; "outlet" -> U fixedGradient, p fixedValue (the tutorial's
     0/U and 0/p)."""
 
-    def __init__(self, mesh, order, nu=0.01, dt=1e-3, tau_coef=20.0, u_kind=None, p_kind=None):
+    def __init__(self, mesh, order, nu=0.01, dt=1e-3, tau_coef=20.0, u_kind=None, p_kind=None, precision=None):
         self.lib = L.lib()
         self.mesh, self.order, self.nu, self.dt = mesh, order, nu, dt
         kk, ff = boundary_faces(mesh)
@@ -59,6 +59,10 @@ class ChorinSolver:
         if rc != L.DG_OK:
             raise L.DGError(rc, "dg_ins_create")
         self.h = h
+        if precision is not None:  # arithmetic of the linear solves (FP64 by default)
+            rc = self.lib.dg_ins_set_precision(self.h, int(precision))
+            if rc != L.DG_OK:
+                raise L.DGError(rc, "dg_ins_set_precision")
         self.K = mesh.K
         self.Np = (order + 1) * (order + 2) // 2
         self.Nfp = order + 1

@@ -106,15 +106,15 @@ class PressureSolver:
         _check(self.ctx.h, self.ctx.lib.dg_lpc_add_residual(self.ctx.h, L.dptr(r)))
 
     def lpc_collect(self, rhs_list, snapshots=(1, 2, 3, 5, 8, 13, 21, 34, 55, 89, 144, 233), rtol=1e-10,
-                    precision=L.DG_PREC_SPLIT):
-        """Training residuals from this solver's own block-Jacobi PCG: for
+                    precision=L.DG_PREC_SPLIT, pc=L.DG_PC_BLOCK_JACOBI):
+        """Training residuals from this solver's own PCG (block Jacobi by
+        default; DG_PC_LEARNED_ONLY: the learned iteration's own iterates): for
         each right-hand side b, the residuals b - S x_j of the iterates after
         j iterations (j in `snapshots`).  Returns the number added."""
         n = 0
         for b in rhs_list:
             for j in snapshots:
-                xj, st = self.solve(b, rtol=rtol, maxit=int(j), pc=L.DG_PC_BLOCK_JACOBI, precision=precision,
-                                    raise_on_fail=False)
+                xj, st = self.solve(b, rtol=rtol, maxit=int(j), pc=pc, precision=precision, raise_on_fail=False)
                 if st["status"] not in (L.DG_OK, L.DG_ERR_NOT_CONVERGED):
                     _check(self.ctx.h, st["status"])
                 self.lpc_add_residual(b - self.apply(xj))

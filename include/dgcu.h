@@ -429,6 +429,10 @@ int dg_ins_set_state(dg_ins* ins, const double* U_host, const double* p_host);
 int dg_ins_get_state(dg_ins* ins, double* U_host, double* p_host);
 /* one step; the linear solves stop at rtol (relative residual) */
 int dg_ins_step(dg_ins* ins, const dg_ins_bdata* bd, double rtol, int maxit, dg_ins_stats* stats);
+/* arithmetic of the step's linear solves: DG_PREC_FP64 (default) or
+ * DG_PREC_SPLIT (FP32 operator on FP64 element offsets, FP64 vectors and
+ * recurrences, the same rtol on the true FP64 residual) */
+int dg_ins_set_precision(dg_ins* ins, int precision);
 /* one operator of the step alone (parity tests): op 0 div(U (x) U) with the
  * u_value of bd on u_kind 0 slots, 1 div U, 2 grad p, 3 curl curl U */
 int dg_ins_operator(dg_ins* ins, int op, const dg_ins_bdata* bd, const double* in_host, double* out_host);

@@ -149,3 +149,31 @@ def test_cylinder_steps_against_oracle(gpu_lib):
           (eu, ep, st["iterations_p"], st["iterations_u"]))
     assert np.abs(Ug).max() > 1e-4 and eu < 2e-7 and ep < 2e-7
     g.close()
+
+
+@pytest.mark.parametrize("N", [2, 3])
+def test_chorin_steps_mixed_precision_solves(gpu_lib, N):
+    """The step with mixed-precision linear solves (FP32 operator on FP64
+    offsets, FP64 vectors, the same 1e-10 on the true FP64 residual) against
+    the all-FP64 step: 20 Pearson-vortex steps agree to 1e-8 (both solves stop
+    at a relative residual of 1e-10, so their solutions differ at that level
+    times the systems' conditioning)."""
+    from hopefoam_gb300 import _lib as L
+    from hopefoam_gb300.ins import ChorinSolver, PearsonVortex
+
+    m = golden_mesh("pearson_0.25h")
+    res = []
+    for prec in (L.DG_PREC_FP64, L.DG_PREC_SPLIT):
+        g = ChorinSolver(m, N, nu=0.01, dt=1e-3, precision=prec)
+        pv = PearsonVortex(g)
+        g.set_state(*pv.initial_state())
+        t = 0.0
+        for _ in range(20):
+            st = g.step(pv.bdata(t), rtol=1e-10)
+            t += g.dt
+        assert st["rel_residual_p"] <= 1e-10 and st["rel_residual_u"] <= 1e-10
+        res.append(g.get_state())
+        g.close()
+    eu, ep = rel_l2(res[1][0], res[0][0]), rel_l2(res[1][1], res[0][1])
+    print("N = %d, 20 steps, mixed vs FP64 solves: U %.2e  p %.2e" % (N, eu, ep))
+    assert eu < 1e-8 and ep < 1e-8

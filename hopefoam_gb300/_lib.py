@@ -104,6 +104,7 @@ SIGNATURES = {
     "dg_lpc_setup": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_ulonglong, ctypes.c_int, ctypes.c_int]),
     "dg_lpc_add_residual": (ctypes.c_int, [_vp, _dp]),
     "dg_lpc_set_slope": (ctypes.c_int, [_vp, ctypes.c_double]),
+    "dg_lpc_set_coarse": (ctypes.c_int, [_vp, ctypes.c_int]),
     "dg_lpc_train": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_double, ctypes.c_ulonglong, _dp, _dp]),
     "dg_lpc_loss": (ctypes.c_int, [_vp, _dp, _dp, _dp]),
     "dg_lpc_energy_gradients": (ctypes.c_int, [_vp, _dp, _fp, _fp, _dp]),

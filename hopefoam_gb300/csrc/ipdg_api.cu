@@ -62,6 +62,7 @@ struct IpdgState {
     double* d_gvec = nullptr;         // training: output-gradient vector
     int* d_tcstatus = nullptr;        // timeout flag of the tensor-core local stage
     float* d_wpart = nullptr;         // two-layer form: per-CTA weight-gradient partials
+    bool lpc_coarse = false;          // training: z = learned local stage + the coarse-space correction
     float *d_W1 = nullptr, *d_W2 = nullptr, *d_m1 = nullptr, *d_v1 = nullptr, *d_m2 = nullptr, *d_v2 = nullptr;
     float *d_g1 = nullptr, *d_g2 = nullptr;
     __nv_bfloat16 *d_W1b = nullptr, *d_W2b = nullptr;
@@ -1009,14 +1010,24 @@ int lpc_forward_vec(dg_ctx* c, const double* r, bool with_bj_loss) {
     lpc_descr(c, net, fa);
     IP_CUDA(c, launch_bj(s->args, s->d_P32, r, s->d_zb, c->stream));
     if (with_bj_loss) {
-        IP_CUDA(c, launch_ipdg_apply(s->args, true, s->d_zb, s->d_w, c->stream));
-        IP_CUDA(c, launch_dot(r, s->d_zb, n, s->d_lpart + 2 * s->G, s->G, c->stream));
-        IP_CUDA(c, launch_dot(s->d_zb, s->d_w, n, s->d_lpart + 3 * s->G, s->G, c->stream));
+        // the reference loss: block Jacobi, with the coarse-space correction when training under it
+        const double* zref = s->d_zb;
+        if (s->lpc_coarse) {
+            IP_CUDA(c, launch_mg_correction(s->mg, r, s->d_zb, s->d_zt, nullptr, LPC_PCG_INIT, s->d_S, s->d_ppart,
+                                            s->nmax, nullptr, c->stream));
+            zref = s->d_zt;
+        }
+        IP_CUDA(c, launch_ipdg_apply(s->args, true, zref, s->d_w, c->stream));
+        IP_CUDA(c, launch_dot(r, zref, n, s->d_lpart + 2 * s->G, s->G, c->stream));
+        IP_CUDA(c, launch_dot(zref, s->d_w, n, s->d_lpart + 3 * s->G, s->G, c->stream));
     }
     if (schwarz_form(s->lpc_form)) {
         IP_CUDA(c, launch_schwarz_local(s->sw, r, nullptr, s->d_U, nullptr, c->stream));
         IP_CUDA(c, launch_schwarz_collect(s->sw, s->d_zb, s->d_U, nullptr, s->d_zt, nullptr, LPC_APPLY, nullptr,
                                           nullptr, c->stream));
+        if (s->lpc_coarse)  // z = learned local stage + P V(P^T r), in place (the preconditioner it is trained for)
+            IP_CUDA(c, launch_mg_correction(s->mg, r, s->d_zt, s->d_zt, nullptr, LPC_PCG_INIT, s->d_S, s->d_ppart,
+                                            s->nmax, nullptr, c->stream));
     } else {
         IP_CUDA(c, launch_lpc_features(fa, s->d_X, s->d_sc, c->stream));
         IP_CUDA(c, launch_lpc_forward(net, s->d_X, nullptr, K, s->d_Hs, s->d_y, s->d_lpart + 4 * s->G, s->G,
@@ -1230,6 +1241,20 @@ int dg_lpc_setup(dg_ctx* c, int hidden, unsigned long long seed, int capacity, i
     s->count = 0;
     s->adam_step = 0;
     s->lpc_ready = true;
+    return DG_OK;
+}
+
+int dg_lpc_set_coarse(dg_ctx* c, int on) {
+    if (!c) return DG_ERR_ARG;
+    if (!lpc_ok(c)) return ifail(c, DG_ERR_ARG, "dg_lpc_setup not called");
+    IpdgState* s = c->ipdg;
+    if (on && s->lpc_form != DG_LPC_SCHWARZ)
+        return ifail(c, DG_ERR_ARG, "training under the coarse space takes the linear Schwarz form");
+    if (on && !s->mg_ready) {
+        const int rc = mg_setup(c);
+        if (rc) return rc;
+    }
+    s->lpc_coarse = on != 0;
     return DG_OK;
 }
 

@@ -101,6 +101,11 @@ class PressureSolver:
         """Activation max(h, slope h) of the "mlp" form (0: relu, 1: linear)."""
         _check(self.ctx.h, self.ctx.lib.dg_lpc_set_slope(self.ctx.h, float(slope)))
 
+    def lpc_set_coarse(self, on=True):
+        """Train the learned local stage for DG_PC_LEARNED_MULTILEVEL (its loss
+        takes the coarse-space correction into account)."""
+        _check(self.ctx.h, self.ctx.lib.dg_lpc_set_coarse(self.ctx.h, 1 if on else 0))
+
     def lpc_add_residual(self, r):
         r = np.ascontiguousarray(r, np.float64).reshape(-1)
         _check(self.ctx.h, self.ctx.lib.dg_lpc_add_residual(self.ctx.h, L.dptr(r)))
@@ -195,7 +200,7 @@ class PressureSolver:
 
 def train_learned_preconditioner(order, tau_coef=1.0, n_interior=2000, n_rhs=16, epochs=(10, 10), lr=(1e-3, 3e-4),
                                  snapshots=(1, 2, 3, 5, 8, 13, 21, 34, 55, 89, 144, 233, 377), form="schwarz",
-                                 hidden=None, seed=11, slope=None):
+                                 hidden=None, seed=11, slope=None, coarse=False):
     """Trains the learned preconditioner on a small seeded Delaunay mesh from
     residuals of this solver's own block-Jacobi PCG (the network is local,
     so the weights transfer to larger meshes).  Returns (W1, W2, info); W2 is
@@ -210,6 +215,8 @@ def train_learned_preconditioner(order, tau_coef=1.0, n_interior=2000, n_rhs=16,
     ps.lpc_setup(hidden=hidden, seed=0, capacity=n_rhs * len(snapshots), form=form)
     if slope is not None:
         ps.lpc_set_slope(slope)
+    if coarse:
+        ps.lpc_set_coarse(True)
     rhs = [poisson_rhs(mesh, order, seed=100 + i)[0] for i in range(n_rhs)]
     n = ps.lpc_collect(rhs, snapshots=snapshots)
     losses = []
@@ -220,5 +227,7 @@ def train_learned_preconditioner(order, tau_coef=1.0, n_interior=2000, n_rhs=16,
             "seconds": time.perf_counter() - t0, "form": form, "hidden": ps.lpc_hidden}
     if slope is not None:
         info["slope"] = slope
+    if coarse:
+        info["coarse"] = True
     ps.ctx.close()
     return W1, W2, info

@@ -315,6 +315,11 @@ int dg_lpc_setup(dg_ctx* ctx, int hidden, unsigned long long seed, int capacity,
 /* Activation of DG_LPC_SCHWARZ_MLP: max(h, slope h), slope in [0, 1]
  * (default 0, relu; 1 makes M linear and symmetric). */
 int dg_lpc_set_slope(dg_ctx* ctx, double slope);
+/* Training objective of DG_LPC_SCHWARZ: on != 0 trains the local stage for
+ * DG_PC_LEARNED_MULTILEVEL (the loss takes z = the learned local stage plus
+ * the coarse-space correction of DG_PC_MULTILEVEL, which is built here if
+ * needed); 0 (default) for the learned stage alone. */
+int dg_lpc_set_coarse(dg_ctx* ctx, int on);
 int dg_lpc_add_residual(dg_ctx* ctx, const double* r_host);
 int dg_lpc_train(dg_ctx* ctx, int epochs, double lr, unsigned long long seed, double* final_loss,
                  double* final_loss_bj);

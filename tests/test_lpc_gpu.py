@@ -321,3 +321,24 @@ def test_learned_gains_over_same_form_without_learning(gpu_lib):
           (st["iterations"], best, stb["iterations"]))
     assert st["rel_residual"] <= 1e-10
     assert st["iterations"] < 0.8 * best < 0.8 * stb["iterations"], (st["iterations"], best, stb["iterations"])
+
+
+def test_learned_stage_trained_under_the_coarse_space(gpu_lib):
+    """Trained with the coarse-space correction in its loss, the learned local
+    stage under DG_PC_MULTILEVEL's correction needs about the multilevel
+    preconditioner's own iteration count (trained alone it needs more), at
+    the same solution."""
+    from hopefoam_gb300 import _lib as L
+    from hopefoam_gb300.poisson import poisson_rhs, train_learned_preconditioner
+
+    N = 3
+    mesh, ps, _, _, _ = _setup(n_interior=800, N=N, hidden=32, form="schwarz")
+    b = poisson_rhs(mesh, N, seed=99)[0]
+    xm, stm = ps.solve(b, rtol=1e-10, pc=L.DG_PC_MULTILEVEL, maxit=5000)
+    Wc, _, info = train_learned_preconditioner(N, tau_coef=TAU, coarse=True)
+    assert info["loss"] < info["loss_block_jacobi"]  # below the coarse-corrected block Jacobi's loss
+    ps.lpc_set_weights(Wc)
+    xl, stl = ps.solve(b, rtol=1e-10, pc=L.DG_PC_LEARNED_MULTILEVEL, maxit=5000)
+    print("multilevel %d, learned stage trained under it %d iterations" % (stm["iterations"], stl["iterations"]))
+    assert stl["rel_residual"] <= 1e-10 and stl["iterations"] <= 1.1 * stm["iterations"]
+    assert rel_l2(xl, xm) < 1e-8

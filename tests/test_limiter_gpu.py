@@ -37,8 +37,10 @@ def _box_case(N, seed=0):
     return m, ctx, orc, q, bnd, kinds, gref
 
 
-@pytest.mark.parametrize("N", [1, 2, 4])
+@pytest.mark.parametrize("N", [1, 2, 3, 4, 5, 6, 7])
 def test_limiter_against_oracle(gpu_lib, N):
+    """Every order: N = 2..6 run the lane kernels (a lane per face, per node),
+    N = 1 and 7 the element-per-thread kernels."""
     m, ctx, orc, q, bnd, kinds, gref = _box_case(N)
     ctx.upload(q)
     ctx.set_boundary_traces(bnd)

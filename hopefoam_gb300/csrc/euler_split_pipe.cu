@@ -96,6 +96,14 @@ __device__ __forceinline__ void pipe_body(const SplitArgs& sa, const int bid, co
     uint64_t* bar2 = bar1 + 1;  // [NBUF]
     uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bar1 + 3);
     uint64_t* bq = bar1 + 4;  // the FP64 tile copy has landed
+    // N = 3 (kArrive): every thread's operand writes of a volume pass after the
+    // first, or of the next tile's staging, are done -- every thread arrives,
+    // only the MMA-issuing thread waits, the other warps go on into the next
+    // pass (measured: N = 3 1.14 -> 1.05 ms per step; no change at N = 2;
+    // slower at N = 4, 5, where the warps that run ahead delay the issuing one)
+    constexpr bool kArrive = N == 3;
+    uint64_t* bready = bar1 + 5;
+    volatile int* sfail = reinterpret_cast<volatile int*>(bar1 + 6);  // a wait of that path timed out
     // reference state / metrics of tile parity b
     auto qbf = [&](int b) { return reinterpret_cast<float*>(smem + D::OFF_QB + b * D::QB_STRIDE); };
     auto qbd = [&](int b) {
@@ -221,6 +229,8 @@ __device__ __forceinline__ void pipe_body(const SplitArgs& sa, const int bid, co
         umma::mbar_init(bar1, 1);
         for (int b = 0; b < S::NBUF; b++) umma::mbar_init(bar2 + b, 1);
         umma::mbar_init(bq, 1);
+        umma::mbar_init(bready, S::THREADS);
+        *sfail = 0;
         umma::fence_mbar_init();
         if (t0 < ntiles) issue_q(t0);
     }
@@ -243,6 +253,7 @@ __device__ __forceinline__ void pipe_body(const SplitArgs& sa, const int bid, co
                        STRIDE_AC = S::AL_AC;
     uint32_t ph1 = 0;
     uint32_t ph2 = 0;  // bit b: phase parity of chunk buffer b's MMA barrier
+    uint32_t phr = 0;  // phase parity of bready
     bool failed = false;
     const int qd = warp & 3, sub = warp >> 2;
     const int my_e = 8 * qd + (lane >> 2), my_v = lane & 3;
@@ -667,11 +678,30 @@ __device__ __forceinline__ void pipe_body(const SplitArgs& sa, const int bid, co
                 if (n == 2) store_chunk(1, fr1, fs1);
                 umma::fence_async_smem();
                 umma::fence_before_sync();
-                if (__syncthreads_or(!okw)) { failed = true; break; }
-                umma::fence_after_sync();
-                if (tid == 0) {
-                    issue_mma(ch0, 0);
-                    if (n == 2) issue_mma(ch0 + 1, 1);
+                if (!kArrive || p == 0) {
+                    // (pass 0 staged tn's reference state, which every thread's later
+                    // slices read: always a CTA barrier)
+                    if (__syncthreads_or(!okw)) { failed = true; break; }
+                    umma::fence_after_sync();
+                    if (tid == 0) {
+                        issue_mma(ch0, 0);
+                        if (n == 2) issue_mma(ch0 + 1, 1);
+                    }
+                } else {
+                    if (!okw) *sfail = 1;
+                    umma::mbar_arrive(bready);
+                    if (tid == 0) {
+                        const bool okr = umma::mbar_wait(bready, phr, kWaitLimit);
+                        if (okr && !*sfail) {
+                            umma::fence_after_sync();
+                            issue_mma(ch0, 0);
+                            if (n == 2) issue_mma(ch0 + 1, 1);
+                        } else {
+                            *sfail = 1;
+                        }
+                    }
+                    phr ^= 1u;
+                    __syncwarp();
                 }
                 prev_n = n;
             }
@@ -710,14 +740,36 @@ __device__ __forceinline__ void pipe_body(const SplitArgs& sa, const int bid, co
         if constexpr (D::GATHER) umma::cp_async_wait_all();  // tn's neighbour traces (this thread's copies)
         umma::fence_async_smem();
         umma::fence_before_sync();
-        __syncthreads();
-        umma::fence_after_sync();
-        if (has_next) {
-            pq ^= 1;  // every thread waited for tn's tile copy in pass 0
+        if constexpr (kArrive && S::PAIR && D::NPASS > 1) {
+            // the issuing thread waits until every thread's staging of tn is written
+            // and its reads of D1 are done (sQ64 was read in pass 0, before its barrier)
+            umma::mbar_arrive(bready);
+            if (has_next) pq ^= 1;  // every thread waited for tn's tile copy in pass 0
             if (tid == 0) {
-                qpend = false;
-                if (tn + G < ntiles) issue_q(tn + G);  // sQ64 has been read by stage(tn)
-                issue_gemm1();                         // D1 has been read by the volume phase of t
+                const bool okr = umma::mbar_wait(bready, phr, kWaitLimit);
+                if (okr && !*sfail) {
+                    umma::fence_after_sync();
+                    if (has_next) {
+                        qpend = false;
+                        if (tn + G < ntiles) issue_q(tn + G);
+                        issue_gemm1();
+                    }
+                } else {
+                    *sfail = 1;
+                }
+            }
+            phr ^= 1u;
+            __syncwarp();
+        } else {
+            __syncthreads();
+            umma::fence_after_sync();
+            if (has_next) {
+                pq ^= 1;  // every thread waited for tn's tile copy in pass 0
+                if (tid == 0) {
+                    qpend = false;
+                    if (tn + G < ntiles) issue_q(tn + G);  // sQ64 has been read by stage(tn)
+                    issue_gemm1();                         // D1 has been read by the volume phase of t
+                }
             }
         }
         // the epilogue's RK register values and stage input (L2), loaded while the last MMAs run
@@ -751,7 +803,7 @@ __device__ __forceinline__ void pipe_body(const SplitArgs& sa, const int bid, co
                 okw = umma::mbar_wait(bar2, ph2 & 1u, kWaitLimit);
                 ph2 ^= 1u;
             }
-            if (__syncthreads_or(!okw)) { failed = true; break; }
+            if (__syncthreads_or(!okw || *sfail)) { failed = true; break; }
         }
         umma::fence_after_sync();
         // ---- (D) R (tensor memory) -> staging

@@ -119,6 +119,11 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* mbar, uint32_t phase, uint32
     return false;
 }
 
+// arrive once on an mbarrier (release semantics at CTA scope)
+__device__ __forceinline__ void mbar_arrive(uint64_t* mbar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(mbar)) : "memory");
+}
+
 // arrive once on an mbarrier and add `bytes` to the transaction count its
 // current phase waits for
 __device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* mbar, uint32_t bytes) {

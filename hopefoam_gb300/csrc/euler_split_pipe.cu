@@ -101,7 +101,10 @@ __device__ __forceinline__ void pipe_body(const SplitArgs& sa, const int bid, co
     // only the MMA-issuing thread waits, the other warps go on into the next
     // pass (measured: N = 3 1.14 -> 1.05 ms per step; no change at N = 2;
     // slower at N = 4, 5, where the warps that run ahead delay the issuing one)
-    constexpr bool kArrive = N == 3;
+    // (each part alone at N = 4, 5 measured slower too: passes 1.39 -> 1.43 and
+    // 1.79 -> 1.85 ms per step, end of staging 1.39 -> 1.40 and 1.79 -> 1.80)
+    constexpr bool kArrive = N == 3;      // the later volume passes
+    constexpr bool kArrivePost = N == 3;  // the end of the next tile's staging
     uint64_t* bready = bar1 + 5;
     volatile int* sfail = reinterpret_cast<volatile int*>(bar1 + 6);  // a wait of that path timed out
     // reference state / metrics of tile parity b
@@ -740,7 +743,7 @@ __device__ __forceinline__ void pipe_body(const SplitArgs& sa, const int bid, co
         if constexpr (D::GATHER) umma::cp_async_wait_all();  // tn's neighbour traces (this thread's copies)
         umma::fence_async_smem();
         umma::fence_before_sync();
-        if constexpr (kArrive && S::PAIR && D::NPASS > 1) {
+        if constexpr (kArrivePost && S::PAIR && D::NPASS > 1) {
             // the issuing thread waits until every thread's staging of tn is written
             // and its reads of D1 are done (sQ64 was read in pass 0, before its barrier)
             umma::mbar_arrive(bready);

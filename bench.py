@@ -1107,6 +1107,24 @@ def profile_target(name, small=False):
                          raise_on_fail=False)
         out.update({"K": mesh.K, "iterations": st["iterations"], "ms": st["ms"]})
         ps.ctx.close()
+    elif name == "learned_mlp":
+        # the two-layer form's tensor-core kernels: two applies and two
+        # energy-gradient evaluations with random weights
+        from hopefoam_gb300.mesh import delaunay_square
+        from hopefoam_gb300.poisson import PressureSolver
+
+        mesh = delaunay_square(12000 if small else 50000, seed=0)
+        ps = PressureSolver(mesh, 4, tau_coef=1.0)
+        ps.lpc_setup(hidden=128, seed=0, capacity=0, form="mlp")
+        rng = np.random.default_rng(0)
+        ps.lpc_set_weights((rng.standard_normal((128, 4 * ps.Np)) * 0.05).astype(np.float32))
+        r = rng.standard_normal(mesh.K * ps.Np)
+        for _ in range(2):
+            ps.lpc_apply(r)
+        for _ in range(2):
+            _, _, loss = ps.lpc_energy_gradients(r)
+        out.update({"K": mesh.K, "loss": loss})
+        ps.ctx.close()
     elif name == "ins":
         out.update(ins_bench(n=64 if small else 128, steps=2, warmup=1, with_cpu=False))
     elif name == "cylinder":
@@ -1140,7 +1158,8 @@ def profile_target(name, small=False):
     print(json.dumps(out))
 
 
-PROFILE_TARGETS = ("pcg", "multilevel", "learned", "learned_solve", "ins", "cylinder", "limiter", "batch", "split")
+PROFILE_TARGETS = ("pcg", "multilevel", "learned", "learned_solve", "learned_mlp", "ins", "cylinder", "limiter", "batch",
+                   "split")
 
 
 def _split_ready(ctx):

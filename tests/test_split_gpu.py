@@ -186,3 +186,64 @@ def test_split_n7_roe_shear_layer_many_tiles(gpu_lib):
     assert np.isfinite(qsp).all()
     assert err_rhs < TOL_RHS_SPLIT
     assert err < TOL_STEP_SPLIT_SHEAR
+
+
+def _totals(mesh, order, q):
+    """Domain integrals of the four conserved variables: sum_k J_k 1^T Mref q_k."""
+    from hopefoam_gb300 import euler
+
+    M = euler.reference_operators(order)["Mref"]
+    w = M.sum(axis=0)  # 1^T Mref
+    v = mesh.VXY
+    J = 0.25 * ((v[:, 1, 0] - v[:, 0, 0]) * (v[:, 2, 1] - v[:, 0, 1]) -
+                (v[:, 2, 0] - v[:, 0, 0]) * (v[:, 1, 1] - v[:, 0, 1]))
+    q = np.asarray(q).reshape(4, mesh.K, -1)
+    return np.einsum("k,vkp,p->v", J, q, w)
+
+
+@pytest.mark.parametrize("case", ["vortex_N5_K131072", "shear_N7_K1002528"])
+def test_conservation_at_full_size(gpu_lib, case):
+    """A size-independent property at the configured sizes: on a periodic
+    mesh the scheme conserves the domain integrals of the four conserved
+    variables (every face flux enters both elements with opposite signs).
+    FP64 path: to round-off (measured 1e-15 after 10 steps; bound 1e-14 per
+    step); split path: its FP32 face fluxes are evaluated by each side
+    against its own reference state and its GEMMs round in TF32 pieces, so
+    the totals move at FP32 round-off times dt (measured 6e-13 after 10 vortex
+    steps, 1.4e-11 after 3 shear-layer steps; bounds 1e-12 and 5e-11 per
+    step).  Drifts are measured against the largest total (the y-momentum
+    total is zero).  The vortex at the headline size (K = 131072, N = 5, LF),
+    the shear layer at the largest (K = 1,002,528, N = 7, Roe: split path
+    only, 3 steps)."""
+    from hopefoam_gb300 import _lib as L
+    from hopefoam_gb300 import euler
+    from hopefoam_gb300.mesh import periodic_square
+
+    if case.startswith("vortex"):
+        N, m = 5, periodic_square(256, 256, 10.0, 10.0, perturb=0.1, seed=0)
+        ops = euler.reference_operators(N)
+        x, y = euler.node_coords(m, ops["r"], ops["s"])
+        q = euler.isentropic_vortex(x, y, x0=5.0, y0=5.0)
+        flux, steps, precs = L.DG_FLUX_LF, 10, (L.DG_PREC_FP64, L.DG_PREC_SPLIT)
+    else:
+        N, m = 7, periodic_square(708, 708, 1.0, 1.0, seed=0)
+        ops = euler.reference_operators(N)
+        x, y = euler.node_coords(m, ops["r"], ops["s"])
+        q = euler.kelvin_helmholtz(x, y, seed=0)
+        flux, steps, precs = L.DG_FLUX_ROE, 3, (L.DG_PREC_SPLIT,)
+    t0 = _totals(m, N, q)
+    ctx = euler.EulerContext(m, N)
+    for prec in precs:
+        ctx.upload(q)
+        dt = ctx.cfl_dt(0.5)
+        ctx.lserk4(dt, steps, flux=flux, precision=prec)
+        t1 = _totals(m, N, ctx.download())
+        drift = np.abs(t1 - t0) / np.maximum(np.abs(t0), 1e-300)
+        print("%s %s: relative drift of the totals after %d steps %s" %
+              (case, "fp64" if prec == L.DG_PREC_FP64 else "split", steps, np.array2string(drift, precision=2)))
+        per_step = 1e-14 if prec == L.DG_PREC_FP64 else (1e-12 if case.startswith("vortex") else 5e-11)
+        tol = per_step * steps
+        # the vortex's y-momentum total is zero: compare it against the scale of the x-momentum total
+        scale = np.maximum(np.abs(t0), np.abs(t0[1]))
+        assert np.all(np.abs(t1 - t0) <= tol * scale), (case, prec, drift)
+    ctx.close()

@@ -29,6 +29,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <type_traits>
 #include <vector>
 
 #include "../../include/dgcu.h"
@@ -273,174 +274,332 @@ __global__ void __launch_bounds__(256, 4) ipdg_apply_kernel(IpdgArgs a, const do
     }
 }
 
-// Element-per-lane SIPG apply for the FP32 iterations of the PCG (N <= 5):
-// one thread holds one element's input offsets, its output rows and, face by
-// face, its neighbour's offsets in registers, and every reference table entry
-// is a kernel-parameter (constant-bank) operand of the FMA that uses it, so
-// the apply is FMAs plus the element's own loads.  The neighbour is read in
-// its relabelled numbering (the shared face is its face 0, traversed in this
-// element's direction: IpLaneTab::perm), so its face-0 tables serve every
-// face; the face coefficients fcl carry its gradients in that frame.  Same
-// operator, staging (p = z + beta p_old, offsets from the FP32 mirrors, FP64
-// offset differences across faces) and outputs as ipdg_apply_kernel; the sums
+// SIPG apply for the FP32 iterations of the PCG (N <= 5), in two passes with
+// one element per lane pair.  Every reference table entry is a
+// kernel-parameter (constant-bank) operand of the FMA that uses it, so the
+// arithmetic is FMAs plus the element's own loads.  The face terms need, on
+// each side of a face, the input's trace and normal derivative at the face's
+// Gauss points.  The first pass forms the input p = z + beta p_old (FP64,
+// written out for the element's rows, and as FP32 offsets from the element's
+// first-node value) and writes, for every element and face, the trace
+// (offset form) and the outward normal derivative at the Gauss points in the
+// element's own order: LaneFaceRec<N>::R floats per face.  The second pass
+// reads its own records and, per interior face, the neighbour's record of
+// the shared face (a contiguous 16-byte-aligned run instead of a gather of
+// the neighbour's nodes).  The neighbour traverses the shared face the other
+// way when rot is set (Gauss point g is its point Nfq-1-g), and its outward
+// normal is the negated one of this element, so the neighbour-side
+// derivative along this element's normal is minus its own.  Offsets between
+// the two elements' first-node values enter the jump as FP64 differences
+// rounded to FP32.  Same operator and outputs as ipdg_apply_kernel; the sums
 // run in another order, so results agree to FP32 round-off.
+// Both passes run two lanes per element: a CTA of 256 threads covers a tile
+// of 128 elements, its warps 0-3 take one half of the work of each element
+// (Gauss points in the first pass, output rows in the second) and warps 4-7
+// the other, so the half is uniform across a warp and every table entry
+// stays a constant-bank operand.
 template <int N>
-__global__ void __launch_bounds__(128, N <= 3 ? 4 : (N == 4 ? 3 : 2)) ipdg_apply_lane_kernel(IpdgArgs a, const __grid_constant__ IpLaneTab<N> T,
-                                                             const double* __restrict__ u, double* __restrict__ y,
-                                                             ApplyPcg pc) {
+struct LaneFaceRec {
+    static constexpr int Nfq = N + 2, R = lane_face_rec(N), ER = 3 * R, SR = ER + 1;  // SR: padded smem stride
+    static constexpr int GH = (Nfq + 1) / 2;                 // first pass: Gauss points [0, GH) | [GH, Nfq)
+    static constexpr int Np = (N + 1) * (N + 2) / 2, NH = (Np + 1) / 2;  // second pass: rows [0, NH) | [NH, Np)
+};
+
+template <int H>
+using HalfTag = std::integral_constant<int, H>;
+
+template <int N>
+__global__ void __launch_bounds__(256) ipdg_lane_trace_kernel(IpdgArgs a, const __grid_constant__ IpLaneTab<N> T,
+                                                              const double* __restrict__ u, ApplyPcg pc) {
     using L = IpLaneTab<N>;
-    constexpr int Np = L::Np, Nfp = L::Nfp, Nfq = L::Nfq, NB = 3 * N;
-    double beta = 0.0;
-    if (pc.S) {
-        if (pc.S->done) return;
-        beta = pc.S->beta;
-    }
+    using FR = LaneFaceRec<N>;
+    constexpr int Np = L::Np, Nfp = L::Nfp, Nfq = L::Nfq, NB = 3 * N, R = FR::R, ER = FR::ER, SR = FR::SR,
+                  GH = FR::GH;
+    if (pc.S->done) return;
+    const double beta = pc.S->beta;
     const bool has_beta = beta != 0.0;
     const float betaf = (float)beta;
     const double* __restrict__ p_old = pc.p_old;
     const float* __restrict__ dzv = pc.dz;
     const float* __restrict__ dpo = pc.dp_old;
-    const bool mass = a.mass_coef != 0.0;
     double* __restrict__ p_new = pc.p_new;
     float* __restrict__ dp_new = pc.dp_new;
-    // the tile's own values pass through shared memory so that every global
-    // access of the element's own rows is coalesced: p (FP64) for the first
-    // node and p.Ap, the FP32 offsets in, the outputs out
-    __shared__ double sp[128 * Np];
+    float* __restrict__ ftr = a.lane_ftr;
+    double* __restrict__ p0 = a.lane_p0;
     __shared__ float sd[128 * Np];
-    double dot = 0.0;
+    __shared__ float srec[128 * SR];
+    const int e = threadIdx.x & 127, h = threadIdx.x >> 7;
     const int ntiles = (a.K + 127) / 128;
     for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-        const int k0 = tile * 128, ne = min(128, a.K - k0);
+        const int k0 = tile * 128, ne = min(128, a.K - k0), nn = ne * Np;
         const size_t g0 = (size_t)k0 * Np;
-        for (int t = threadIdx.x; t < ne * Np; t += 128) {
-            const size_t i = g0 + t;
-            const double vp = has_beta ? fma(beta, p_old[i], u[i]) : u[i];
-            if (p_new) p_new[i] = vp;
-            sp[t] = vp;
-            float d = dzv[i];
-            if (has_beta) d = fmaf(betaf, dpo[i], d);
-            dp_new[i] = d;
-            sd[t] = d;
+        // node-parallel staging in batches of SB nodes per thread, every
+        // load of a batch issued before its first use
+        constexpr int J = (Np + 1) / 2, SB = 4;
+#pragma unroll
+        for (int j0 = 0; j0 < J; j0 += SB) {
+            double xu[SB], xp[SB];
+            float fz[SB], fp[SB];
+#pragma unroll
+            for (int j = 0; j < SB; j++) {
+                const int t = threadIdx.x + 256 * (j0 + j);
+                if (j0 + j < J && t < nn) {
+                    xu[j] = u[g0 + t];
+                    fz[j] = dzv[g0 + t];
+                    if (has_beta) {
+                        xp[j] = p_old[g0 + t];
+                        fp[j] = dpo[g0 + t];
+                    }
+                }
+            }
+#pragma unroll
+            for (int j = 0; j < SB; j++) {
+                const int t = threadIdx.x + 256 * (j0 + j);
+                if (j0 + j < J && t < nn) {
+                    const double vp = has_beta ? fma(beta, xp[j], xu[j]) : xu[j];
+                    if (p_new) p_new[g0 + t] = vp;
+                    const int e2 = t / Np;
+                    if (t == e2 * Np) p0[k0 + e2] = vp;
+                    const float d = has_beta ? fmaf(betaf, fp[j], fz[j]) : fz[j];
+                    dp_new[g0 + t] = d;
+                    sd[t] = d;
+                }
+            }
         }
         __syncthreads();
-        const int e = threadIdx.x;
-        const int k = k0 + e;
         if (e < ne) {
-        float us[Np];
+            const int k = k0 + e;
+            float us[Np];
 #pragma unroll
-        for (int p = 0; p < Np; p++) us[p] = sd[e * Np + p];
-        const double pd0 = sp[e * Np];
-        const float ub0 = (float)pd0;
-        // volume term J (c_rr Srr + c_rs Srs2 + c_ss Sss) u
-        const float* vc = a.o32.vc + (size_t)k * 3;
-        const float vrr = vc[0], vrs = vc[1], vss = vc[2];
-        float v[Np];
+            for (int p = 0; p < Np; p++) us[p] = sd[e * Np + p];
+            float* rec = srec + e * SR;
+            auto points = [&](auto hc) {
+                constexpr int g0h = decltype(hc)::value ? GH : 0, g1h = decltype(hc)::value ? Nfq : GH;
 #pragma unroll
-        for (int i = 0; i < Np; i++) {
-            float A = 0.f, B = 0.f, C = 0.f;
+                for (int f = 0; f < 3; f++) {
+                    const float2 f01 = *reinterpret_cast<const float2*>(a.o32.fc + ((size_t)k * 3 + f) * kFaceCoef);
 #pragma unroll
-            for (int p = 0; p < Np; p++) {
-                A = fmaf(T.Srr[i][p], us[p], A);
-                B = fmaf(T.Srs2[i][p], us[p], B);
-                C = fmaf(T.Sss[i][p], us[p], C);
-            }
-            v[i] = vrr * A + vrs * B + vss * C;
-        }
-        if (mass) {
-            const float mc = (float)(a.mass_coef * a.J[k]);
+                    for (int g = g0h; g < g1h; g++) {
+                        const int fg = f * Nfq + g;
+                        float ur = 0.f, usd = 0.f, um = 0.f;
 #pragma unroll
-            for (int i = 0; i < Np; i++) {
-                float m = T.mrow[i] * ub0;
+                        for (int p = 0; p < Np; p++) {
+                            ur = fmaf(T.DrfT[p][fg], us[p], ur);
+                            usd = fmaf(T.DsfT[p][fg], us[p], usd);
+                        }
 #pragma unroll
-                for (int p = 0; p < Np; p++) m = fmaf(T.Mr[i][p], us[p], m);
-                v[i] = fmaf(mc, m, v[i]);
-            }
-        }
-        // faces
+                        for (int j = 0; j < Nfp; j++) um = fmaf(T.If[g][j], us[(f * N + j) % NB], um);
+                        rec[f * R + g] = um;
+                        rec[f * R + Nfq + g] = f01.x * ur + f01.y * usd;
+                    }
+                    if (decltype(hc)::value) {
 #pragma unroll
-        for (int f = 0; f < 3; f++) {
-            const int c = a.conn[(size_t)k * 3 + f];
-            const float2* fcp = reinterpret_cast<const float2*>(a.fcl + ((size_t)k * 3 + f) * kFaceCoef);
-            const float2 f01 = fcp[0], f23 = fcp[1], f45 = fcp[2];
-            const bool interior = c >= 0;
-            float nb[Np];
-            float dc = 0.f;
-            if (interior) {
-                const int nbk = c >> 3, pid = 2 * (c & 3) + ((c >> 2) & 1);
-                const size_t nbase = (size_t)nbk * Np;
-#pragma unroll
-                for (int p = 0; p < Np; p++) {
-                    const size_t j = nbase + T.perm[pid][p];
-                    float d = dzv[j];
-                    if (has_beta) d = fmaf(betaf, dpo[j], d);
-                    nb[p] = d;
+                        for (int q = 2 * Nfq; q < R; q++) rec[f * R + q] = 0.f;
+                    }
                 }
-                dc = (float)(pd0 - (has_beta ? fma(beta, p_old[nbase], u[nbase]) : u[nbase]));
-            } else {
+            };
+            if (h == 0) points(HalfTag<0>{});
+            else points(HalfTag<1>{});
+        }
+        __syncthreads();
+        // records out, 16 bytes per store (ER is a multiple of 4)
+        float4* dst = reinterpret_cast<float4*>(ftr + (size_t)k0 * ER);
+        const int n4 = ne * (ER / 4);
 #pragma unroll
-                for (int p = 0; p < Np; p++) nb[p] = 0.f;
+        for (int j = 0; j < (ER / 4 + 1) / 2; j++) {
+            const int t4 = threadIdx.x + 256 * j;
+            if (t4 < n4) {
+                const int e2 = (4 * t4) / ER;
+                const float* src = srec + e2 * SR + (4 * t4 - e2 * ER);
+                dst[t4] = make_float4(src[0], src[1], src[2], src[3]);
+            }
+        }
+        __syncthreads();  // the next tile rewrites sd and srec
+    }
+}
+
+template <int N>
+__global__ void __launch_bounds__(256, N <= 4 ? 3 : 2) ipdg_lane_face_apply_kernel(IpdgArgs a,
+        const __grid_constant__ IpLaneTab<N> T, double* __restrict__ y, ApplyPcg pc) {
+    using L = IpLaneTab<N>;
+    using FR = LaneFaceRec<N>;
+    constexpr int Np = L::Np, Nfq = L::Nfq, NB = 3 * N, R = FR::R, ER = FR::ER, SR = FR::SR, NH = FR::NH;
+    if (pc.S->done) return;
+    const bool mass = a.mass_coef != 0.0;
+    const double* __restrict__ p_new = pc.p_new;
+    const float* __restrict__ dp_new = pc.dp_new;
+    const float* __restrict__ ftr = a.lane_ftr;
+    const double* __restrict__ p0 = a.lane_p0;
+    __shared__ float sd[128 * Np];
+    __shared__ float srec[128 * SR];
+    const int e = threadIdx.x & 127, h = threadIdx.x >> 7;
+    double dot = 0.0;
+    const int ntiles = (a.K + 127) / 128;
+    constexpr int J = (Np + 1) / 2, J4 = (ER / 4 + 1) / 2;
+    for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        const int k0 = tile * 128, ne = min(128, a.K - k0), nn = ne * Np, n4 = ne * (ER / 4);
+        const size_t g0 = (size_t)k0 * Np;
+        {
+            float xs[J];
+            float4 xr[J4];
+#pragma unroll
+            for (int j = 0; j < J; j++) {
+                const int t = threadIdx.x + 256 * j;
+                if (t < nn) xs[j] = dp_new[g0 + t];
+            }
+            const float4* src = reinterpret_cast<const float4*>(ftr + (size_t)k0 * ER);
+#pragma unroll
+            for (int j = 0; j < J4; j++) {
+                const int t4 = threadIdx.x + 256 * j;
+                if (t4 < n4) xr[j] = src[t4];
             }
 #pragma unroll
-            for (int g = 0; g < Nfq; g++) {
-                const int fg = f * Nfq + g;
-                float ur = 0.f, usd = 0.f, um = 0.f;
+            for (int j = 0; j < J; j++) {
+                const int t = threadIdx.x + 256 * j;
+                if (t < nn) sd[t] = xs[j];
+            }
 #pragma unroll
-                for (int p = 0; p < Np; p++) {
-                    ur = fmaf(T.DrfT[p][fg], us[p], ur);
-                    usd = fmaf(T.DsfT[p][fg], us[p], usd);
+            for (int j = 0; j < J4; j++) {
+                const int t4 = threadIdx.x + 256 * j;
+                if (t4 < n4) {
+                    const int e2 = (4 * t4) / ER;
+                    float* d = srec + e2 * SR + (4 * t4 - e2 * ER);
+                    d[0] = xr[j].x;
+                    d[1] = xr[j].y;
+                    d[2] = xr[j].z;
+                    d[3] = xr[j].w;
                 }
+            }
+        }
+        __syncthreads();
+        float vout[NH];
+        if (e < ne) {
+            const int k = k0 + e;
+            float us[Np];
 #pragma unroll
-                for (int j = 0; j < Nfp; j++) um = fmaf(T.If[g][j], us[(f * N + j) % NB], um);
-                const float dm = f01.x * ur + f01.y * usd;
-                float jump, dp;
-                if (interior) {
-                    float vr = 0.f, vs = 0.f, up = 0.f;
+            for (int p = 0; p < Np; p++) us[p] = sd[e * Np + p];
+            const double pd0 = p0[k];
+            const float ub0 = (float)pd0;
+            const float* vc = a.o32.vc + (size_t)k * 3;
+            const float vrr = vc[0], vrs = vc[1], vss = vc[2];
+            const float* rec = srec + e * SR;
+            auto rows = [&](auto hc) {
+                constexpr int i0 = decltype(hc)::value ? NH : 0, i1 = decltype(hc)::value ? Np : NH;
+                float v[NH];
+#pragma unroll
+                for (int i = i0; i < i1; i++) {
+                    float A = 0.f, B = 0.f, C = 0.f;
 #pragma unroll
                     for (int p = 0; p < Np; p++) {
-                        vr = fmaf(T.DrfT[p][g], nb[p], vr);
-                        vs = fmaf(T.DsfT[p][g], nb[p], vs);
+                        A = fmaf(T.Srr[i][p], us[p], A);
+                        B = fmaf(T.Srs2[i][p], us[p], B);
+                        C = fmaf(T.Sss[i][p], us[p], C);
+                    }
+                    v[i - i0] = vrr * A + vrs * B + vss * C;
+                }
+                if (mass) {
+                    const float mc = (float)(a.mass_coef * a.J[k]);
+#pragma unroll
+                    for (int i = i0; i < i1; i++) {
+                        float m = T.mrow[i] * ub0;
+#pragma unroll
+                        for (int p = 0; p < Np; p++) m = fmaf(T.Mr[i][p], us[p], m);
+                        v[i - i0] = fmaf(mc, m, v[i - i0]);
+                    }
+                }
+#pragma unroll
+                for (int f = 0; f < 3; f++) {
+                    const int c = a.conn[(size_t)k * 3 + f];
+                    const float2* fcp = reinterpret_cast<const float2*>(a.o32.fc + ((size_t)k * 3 + f) * kFaceCoef);
+                    const float2 f01 = fcp[0], f45 = fcp[2];
+                    const bool interior = c >= 0;
+                    const bool rot = (c >> 2) & 1;
+                    float nr[R];
+                    float dc = 0.f;
+                    if (interior) {
+                        const int nbk = c >> 3, fn = c & 3;
+                        const float4* src = reinterpret_cast<const float4*>(ftr + ((size_t)nbk * 3 + fn) * R);
+#pragma unroll
+                        for (int q = 0; q < R / 4; q++) {
+                            const float4 w = src[q];
+                            nr[4 * q] = w.x;
+                            nr[4 * q + 1] = w.y;
+                            nr[4 * q + 2] = w.z;
+                            nr[4 * q + 3] = w.w;
+                        }
+                        dc = (float)(pd0 - p0[nbk]);
+                    } else {
+#pragma unroll
+                        for (int q = 0; q < R; q++) nr[q] = 0.f;
                     }
 #pragma unroll
-                    for (int j = 0; j < Nfp; j++) up = fmaf(T.If[g][j], nb[j], up);
-                    dp = f23.x * vr + f23.y * vs;
-                    jump = (um - up) + dc;
-                } else {
-                    // Dirichlet face: u+ = -u-, so [u] = 2 u- (offset included)
-                    jump = 2.f * (um + ub0);
-                    dp = dm;
+                    for (int g = 0; g < Nfq; g++) {
+                        const int fg = f * Nfq + g;
+                        const float um = rec[f * R + g], dm = rec[f * R + Nfq + g];
+                        float jump, dp;
+                        if (interior) {
+                            const float up = rot ? nr[Nfq - 1 - g] : nr[g];
+                            dp = -(rot ? nr[2 * Nfq - 1 - g] : nr[Nfq + g]);
+                            jump = (um - up) + dc;
+                        } else {
+                            // Dirichlet face: u+ = -u-, so [u] = 2 u- (offset included)
+                            jump = 2.f * (um + ub0);
+                            dp = dm;
+                        }
+                        const float wJ = f45.y * T.fw[g];
+                        const float sigma = 0.5f * (dm + dp);
+                        const float cc2 = -0.5f * wJ * jump;
+                        const float c1 = wJ * (f45.x * jump - sigma);
+                        const float c2r = cc2 * f01.x, c2s = cc2 * f01.y;
+#pragma unroll
+                        for (int i = i0; i < i1; i++)
+                            v[i - i0] = fmaf(c2r, T.DrfT[i][fg], fmaf(c2s, T.DsfT[i][fg], v[i - i0]));
+#pragma unroll
+                        for (int d = 0; d <= N; d++) {
+                            const int i = (f * N + d) % NB;
+                            if (i >= i0 && i < i1) v[i - i0] = fmaf(c1, T.If[g][d], v[i - i0]);
+                        }
+                    }
                 }
-                const float wJ = f45.y * T.fw[g];
-                const float sigma = 0.5f * (dm + dp);
-                const float cc2 = -0.5f * wJ * jump;
-                const float c1 = wJ * (f45.x * jump - sigma);
-                const float c2r = cc2 * f01.x, c2s = cc2 * f01.y;
 #pragma unroll
-                for (int i = 0; i < Np; i++) v[i] = fmaf(c2r, T.DrfT[i][fg], fmaf(c2s, T.DsfT[i][fg], v[i]));
-#pragma unroll
-                for (int d = 0; d <= N; d++) v[(f * N + d) % NB] = fmaf(c1, T.If[g][d], v[(f * N + d) % NB]);
-            }
+                for (int i = i0; i < i1; i++) vout[i - i0] = v[i - i0];
+            };
+            if (h == 0) rows(HalfTag<0>{});
+            else rows(HalfTag<1>{});
         }
-        // this element's outputs over its own input row (read only by this thread)
+        __syncthreads();  // every lane has read sd and srec
+        if (e < ne) {
+            const int i0 = h ? NH : 0, i1 = h ? Np : NH;
 #pragma unroll
-        for (int i = 0; i < Np; i++) sd[e * Np + i] = v[i];
+            for (int i = 0; i < NH; i++)
+                if (i0 + i < i1) sd[e * Np + i0 + i] = vout[i];
         }
         __syncthreads();
-        for (int t = threadIdx.x; t < ne * Np; t += 128) {
-            const double out = (double)sd[t];
-            y[g0 + t] = out;
-            dot += out * sp[t];
+        {
+            double xp[J];
+#pragma unroll
+            for (int j = 0; j < J; j++) {
+                const int t = threadIdx.x + 256 * j;
+                if (t < nn) xp[j] = p_new[g0 + t];
+            }
+#pragma unroll
+            for (int j = 0; j < J; j++) {
+                const int t = threadIdx.x + 256 * j;
+                if (t < nn) {
+                    const double out = (double)sd[t];
+                    y[g0 + t] = out;
+                    dot += out * xp[j];
+                }
+            }
         }
-        __syncthreads();  // the next tile rewrites sp and sd
+        __syncthreads();  // the next tile rewrites sd and srec
     }
-    if (pc.S) {
-        double val[1] = {dot}, tot[1];
-        if (grid_sum<1>(val, pc.part, gridDim.x, &pc.S->counter, tot) && threadIdx.x == 0) {
-            const double pap = tot[0];
-            pc.S->pap = pap;
-            pc.S->alpha = pc.S->rz / pap;
-            if (!(pap > 0.0) || !(pc.S->alpha == pc.S->alpha)) pc.S->done = 2;
-        }
+    double val[1] = {dot}, tot[1];
+    if (grid_sum<1>(val, pc.part, gridDim.x, &pc.S->counter, tot) && threadIdx.x == 0) {
+        const double pap = tot[0];
+        pc.S->pap = pap;
+        pc.S->alpha = pc.S->rz / pap;
+        if (!(pap > 0.0) || !(pc.S->alpha == pc.S->alpha)) pc.S->done = 2;
     }
 }
 
@@ -930,10 +1089,13 @@ static cudaError_t apply_n(const IpdgArgs& a, bool fp32, const double* u, double
                            cudaStream_t s) {
     using D = IpDims<N>;
     if constexpr (N <= 5) {
-        if (fp32 && pc.dz && pc.S && a.lane_tab && a.fcl) {
+        if (fp32 && pc.dz && pc.S && pc.p_new && a.lane_tab && a.lane_ftr && a.lane_p0) {
             const int grid = std::max(1, std::min((a.K + 127) / 128, pcg_max_grid(a.K, N, a.sms)));
-            ipdg_apply_lane_kernel<N>
-                <<<grid, 128, 0, s>>>(a, *static_cast<const IpLaneTab<N>*>(a.lane_tab), u, y, pc);
+            const IpLaneTab<N>& tab = *static_cast<const IpLaneTab<N>*>(a.lane_tab);
+            ipdg_lane_trace_kernel<N><<<grid, 256, 0, s>>>(a, tab, u, pc);
+            const cudaError_t e = cudaGetLastError();
+            if (e != cudaSuccess) return e;
+            ipdg_lane_face_apply_kernel<N><<<grid, 256, 0, s>>>(a, tab, y, pc);
             return cudaGetLastError();
         }
     }

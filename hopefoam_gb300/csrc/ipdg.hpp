@@ -34,16 +34,22 @@ struct IpdgArgs {
     double mass_coef;    // S + mass_coef M (Helmholtz form); 0: the Laplacian alone
     IpdgOps<double> o64;
     IpdgOps<float> o32;
-    // element-per-lane apply (N <= 5, FP32 PCG iterations): the face
-    // coefficients with each neighbour's gradient terms taken in its
-    // relabelled frame (face shared with this element = its face 0, Gauss
-    // points in this element's order), and the host copy of the reference
-    // tables passed to that kernel by value (IpLaneTab<N>; null: not built)
-    const float* fcl;
+    // two-pass FP32 apply of the PCG iterations (N <= 5; null: not built):
+    // the host copy of the reference tables passed to its kernels by value
+    // (IpLaneTab<N>); per element and face, the input's trace and outward
+    // normal derivative at the face's Gauss points (lane_face_rec(N) floats,
+    // element's own point order); per element the FP64 value of the input at
+    // its first node
     const void* lane_tab;
+    float* lane_ftr;
+    double* lane_p0;
 };
 
 constexpr int kFaceCoef = 6;
+
+// floats per face record of the two-pass apply: Nfq traces, Nfq normal
+// derivatives, padded to 16 bytes
+constexpr int lane_face_rec(int N) { return (2 * (N + 2) + 3) / 4 * 4; }
 
 // reference tables of the element-per-lane apply, FP32, ring order; passed
 // as a kernel parameter so that every table read is a constant-bank operand
@@ -57,9 +63,6 @@ struct IpLaneTab {
     float Srr[Np][Np], Srs2[Np][Np], Sss[Np][Np];
     float Mr[Np][Np];
     float mrow[Np];
-    // ring position, in the neighbour's own numbering, of the node at ring
-    // position p of its relabelled numbering; index 2 fn + rot
-    unsigned char perm[6][Np];
 };
 
 // device-side CG state; the kernels read and update it, the host reads it

@@ -31,9 +31,7 @@ struct IpdgState {
     std::string mg_err;
     std::vector<void*> mg_allocs;
     std::vector<double> fc_host;  // face coefficients as built (boundary types reset sJ from it)
-    std::vector<double> fcl_host;  // the same with each neighbour's gradients in its relabelled frame
-    float* d_fcl = nullptr;
-    std::vector<unsigned char> lane_tab;  // IpLaneTab<N> of the element-per-lane apply (N <= 5)
+    std::vector<unsigned char> lane_tab;  // IpLaneTab<N> of the two-pass FP32 apply (N <= 5)
     std::vector<int> btype;       // per boundary slot: 0 fixesValue, 1 fixesGradient, 2 neither
     double* d_blocks = nullptr;  // FP64 inverse diagonal blocks (row-major per element)
     double* d_P64 = nullptr;     // the same, grouped layout of the element-aligned kernels
@@ -44,6 +42,8 @@ struct IpdgState {
     double* d_ppart = nullptr;  // [3][nmax] partials of the PCG grid-wide sums
     float *d_dz = nullptr, *d_dp = nullptr, *d_dp2 = nullptr;  // FP32 offset mirrors of z and p
     float* d_r32 = nullptr;      // FP32 copy of r (learned Schwarz mode)
+    float* d_lane_ftr = nullptr;  // face records of the two-pass FP32 apply (N <= 5)
+    double* d_lane_p0 = nullptr;  // first-node values of its input
     int nmax = 0;
     int sms = 1;
     PcgScalars* d_S = nullptr;
@@ -314,78 +314,6 @@ std::vector<int> rotation_perms(const dgb::RefOps& o) {
     return perm;
 }
 
-// Node permutation for a relabelling of a triangle's vertices (new vertex m
-// = old vertex sig[m]): perm[p] = old ring position of the node at ring
-// position p of the new numbering (matched by barycentric coordinates; the
-// node set is invariant under the triangle's symmetries).
-static std::vector<int> relabel_perm(const dgb::RefOps& o, const int sig[3]) {
-    const int Np = o.Np;
-    std::vector<int> perm(Np, -1);
-    auto bary = [&](int p, double* l) {
-        const double r = o.r[o.ring[p]], t = o.s[o.ring[p]];
-        l[0] = -(r + t) / 2;
-        l[1] = (1 + r) / 2;
-        l[2] = (1 + t) / 2;
-    };
-    for (int p = 0; p < Np; p++) {
-        double lp[3], want[3];
-        bary(p, lp);
-        for (int m = 0; m < 3; m++) want[sig[m]] = lp[m];
-        for (int q = 0; q < Np; q++) {
-            double l[3];
-            bary(q, l);
-            if (std::fabs(l[0] - want[0]) + std::fabs(l[1] - want[1]) + std::fabs(l[2] - want[2]) < 1e-9) {
-                perm[p] = q;
-                break;
-            }
-        }
-    }
-    return perm;
-}
-
-// vertex relabelling that makes a neighbour's face fn its face 0, traversed
-// in the direction of the element's own face (rot = 1: the neighbour
-// traverses the shared edge the other way)
-static void neighbour_relabelling(int fn, int rot, int sig[3]) {
-    if (rot) {
-        sig[0] = (fn + 1) % 3;
-        sig[1] = fn;
-    } else {
-        sig[0] = fn;
-        sig[1] = (fn + 1) % 3;
-    }
-    sig[2] = (fn + 2) % 3;
-}
-
-// face coefficients of the element-per-lane apply: fc with entries 2, 3
-// (n . grad r, n . grad s of the neighbour) in the neighbour's relabelled
-// frame
-static std::vector<double> lane_face_coefs(const dg_ctx* c, const std::vector<double>& fc) {
-    std::vector<double> fcl = fc;
-    for (int k = 0; k < c->K; k++) {
-        const double* g = &c->geo_host[4 * (size_t)k];
-        for (int f = 0; f < 3; f++) {
-            const int cn = c->conn_host[(size_t)k * 3 + f];
-            if (cn < 0) continue;
-            const int nb = cn >> 3, fn = cn & 3, rot = (cn >> 2) & 1;
-            double nx, ny, fsc;
-            face_normal(f, g[0], g[1], g[2], g[3], nx, ny, fsc);
-            int sig[3];
-            neighbour_relabelling(fn, rot, sig);
-            const double* V = &c->vxy_host[6 * (size_t)nb];
-            const double x0 = V[2 * sig[0]], y0 = V[2 * sig[0] + 1];
-            const double xr = 0.5 * (V[2 * sig[1]] - x0), yr = 0.5 * (V[2 * sig[1] + 1] - y0);
-            const double xs = 0.5 * (V[2 * sig[2]] - x0), ys = 0.5 * (V[2 * sig[2] + 1] - y0);
-            const double J = xr * ys - xs * yr;  // negative for a reflection
-            const double rx = ys / J, sx = -yr / J, ry = -xs / J, sy = xr / J;
-            double* out = &fcl[((size_t)k * 3 + f) * kFaceCoef];
-            out[2] = nx * rx + ny * ry;
-            out[3] = nx * sx + ny * sy;
-        }
-    }
-    return fcl;
-}
-
 template <int N>
 static void build_lane_tab(const dg_ctx* c, const std::vector<double>& DrfT, const std::vector<double>& DsfT,
                            const std::vector<double>& Srr, const std::vector<double>& Srs2,
@@ -412,13 +340,6 @@ static void build_lane_tab(const dg_ctx* c, const std::vector<double>& DrfT, con
         t.fw[g] = (float)o.fw[g];
         for (int j = 0; j < L::Nfp; j++) t.If[g][j] = (float)o.If[(size_t)g * L::Nfp + j];
     }
-    for (int fn = 0; fn < 3; fn++)
-        for (int rot = 0; rot < 2; rot++) {
-            int sig[3];
-            neighbour_relabelling(fn, rot, sig);
-            const std::vector<int> perm = relabel_perm(o, sig);
-            for (int p = 0; p < L::Np; p++) t.perm[2 * fn + rot][p] = (unsigned char)perm[p];
-        }
 }
 
 void ipdg_teardown(dg_ctx* c) {
@@ -599,7 +520,6 @@ int dg_ipdg_setup(dg_ctx* c, double tau_coef) {
         }
     s->fc_host = fc;
     s->btype.assign(c->nb, 0);
-    s->fcl_host = lane_face_coefs(c, fc);
     switch (c->N) {
         case 1: build_lane_tab<1>(c, DrfT, DsfT, Srr, Srs2, Sss, Mr, mrow, s->lane_tab); break;
         case 2: build_lane_tab<2>(c, DrfT, DsfT, Srr, Srs2, Sss, Mr, mrow, s->lane_tab); break;
@@ -639,7 +559,6 @@ int dg_ipdg_setup(dg_ctx* c, double tau_coef) {
     rc |= iupload(c, s, (float**)&o32.fw, f32(o.fw));
     rc |= iupload(c, s, (float**)&o32.fc, f32(fc));
     rc |= iupload(c, s, (float**)&o32.vc, f32(vc));
-    rc |= iupload(c, s, &s->d_fcl, f32(s->fcl_host));
     const size_t n = (size_t)K * Np;
     rc |= ialloc(c, s, &s->d_blocks, n * Np);
     const size_t ng = grouped_blocks_size(K, Np);
@@ -655,6 +574,10 @@ int dg_ipdg_setup(dg_ctx* c, double tau_coef) {
     rc |= ialloc(c, s, &s->d_r32, n);
     rc |= ialloc(c, s, &s->d_dp, n);
     rc |= ialloc(c, s, &s->d_dp2, n);
+    if (!s->lane_tab.empty()) {
+        rc |= ialloc(c, s, &s->d_lane_ftr, (size_t)K * 3 * lane_face_rec(c->N));
+        rc |= ialloc(c, s, &s->d_lane_p0, (size_t)K);
+    }
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
@@ -681,8 +604,9 @@ int dg_ipdg_setup(dg_ctx* c, double tau_coef) {
     a.mass_coef = 0.0;
     a.o64 = o64;
     a.o32 = o32;
-    a.fcl = s->d_fcl;
     a.lane_tab = s->lane_tab.empty() ? nullptr : s->lane_tab.data();
+    a.lane_ftr = s->d_lane_ftr;
+    a.lane_p0 = s->d_lane_p0;
     rc = build_blocks(c);
     if (rc) return rc;
     s->ready = true;
@@ -714,12 +638,8 @@ int dg_ipdg_set_boundary_types(dg_ctx* c, const int* btype) {
         }
     const size_t nfc = fc.size();
     std::vector<float> fc32(fc.begin(), fc.end());
-    std::vector<double> fcl = s->fcl_host;
-    for (size_t i = 5; i < nfc; i += kFaceCoef) fcl[i] = fc[i];  // the same face weights
-    std::vector<float> fcl32(fcl.begin(), fcl.end());
     IP_CUDA(c, cudaMemcpyAsync((void*)s->o64h.fc, fc.data(), nfc * sizeof(double), cudaMemcpyHostToDevice, c->stream));
     IP_CUDA(c, cudaMemcpyAsync((void*)s->o32h.fc, fc32.data(), nfc * sizeof(float), cudaMemcpyHostToDevice, c->stream));
-    IP_CUDA(c, cudaMemcpyAsync(s->d_fcl, fcl32.data(), nfc * sizeof(float), cudaMemcpyHostToDevice, c->stream));
     IP_CUDA(c, cudaStreamSynchronize(c->stream));
     s->mg_ready = false;
     return build_blocks(c);

@@ -199,7 +199,7 @@ class PressureSolver:
 
 
 def train_learned_preconditioner(order, tau_coef=1.0, n_interior=2000, n_rhs=16, epochs=(10, 10), lr=(1e-3, 3e-4),
-                                 snapshots=(1, 2, 3, 5, 8, 13, 21, 34, 55, 89, 144, 233, 377), form="schwarz",
+                                 snapshots=(1, 2, 3, 5, 8, 13, 21, 34, 55, 89, 144, 233, 377, 610, 987), form="schwarz",
                                  hidden=None, seed=11, slope=None, coarse=False):
     """Trains the learned preconditioner on a small seeded Delaunay mesh from
     residuals of this solver's own block-Jacobi PCG (the network is local,

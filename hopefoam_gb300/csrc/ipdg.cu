@@ -289,10 +289,12 @@ __global__ void __launch_bounds__(256, 4) ipdg_apply_kernel(IpdgArgs a, const do
 // the neighbour's nodes).  The neighbour traverses the shared face the other
 // way when rot is set (Gauss point g is its point Nfq-1-g), and its outward
 // normal is the negated one of this element, so the neighbour-side
-// derivative along this element's normal is minus its own.  Offsets between
-// the two elements' first-node values enter the jump as FP64 differences
-// rounded to FP32.  Same operator and outputs as ipdg_apply_kernel; the sums
-// run in another order, so results agree to FP32 round-off.
+// derivative along this element's normal is minus its own.  The offset
+// between the two elements' first-node values enters the jump; each value is
+// kept as an FP32 pair (hi, lo) and the offset formed as (hi - hi') + (lo -
+// lo') in FP32 (within about one FP32 rounding of the exact difference, with
+// no FP64 work per face).  Same operator and outputs as ipdg_apply_kernel; the
+// sums run in another order, so results agree to FP32 round-off.
 // Both passes run two lanes per element: a CTA of 256 threads covers a tile
 // of 128 elements, its warps 0-3 take one half of the work of each element
 // (Gauss points in the first pass, output rows in the second) and warps 4-7
@@ -325,9 +327,10 @@ __global__ void __launch_bounds__(256) ipdg_lane_trace_kernel(IpdgArgs a, const 
     double* __restrict__ p_new = pc.p_new;
     float* __restrict__ dp_new = pc.dp_new;
     float* __restrict__ ftr = a.lane_ftr;
-    double* __restrict__ p0 = a.lane_p0;
+    float2* __restrict__ p0 = a.lane_p0;
     __shared__ float sd[128 * Np];
     __shared__ float srec[128 * SR];
+    __shared__ double sp0[128];
     const int e = threadIdx.x & 127, h = threadIdx.x >> 7;
     const int ntiles = (a.K + 127) / 128;
     for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
@@ -359,7 +362,7 @@ __global__ void __launch_bounds__(256) ipdg_lane_trace_kernel(IpdgArgs a, const 
                     const double vp = has_beta ? fma(beta, xp[j], xu[j]) : xu[j];
                     if (p_new) p_new[g0 + t] = vp;
                     const int e2 = t / Np;
-                    if (t == e2 * Np) p0[k0 + e2] = vp;
+                    if (t == e2 * Np) sp0[e2] = vp;
                     const float d = has_beta ? fmaf(betaf, fp[j], fz[j]) : fz[j];
                     dp_new[g0 + t] = d;
                     sd[t] = d;
@@ -369,6 +372,11 @@ __global__ void __launch_bounds__(256) ipdg_lane_trace_kernel(IpdgArgs a, const 
         __syncthreads();
         if (e < ne) {
             const int k = k0 + e;
+            if (h == 0) {
+                const double v0 = sp0[e];
+                const float hi = (float)v0;
+                p0[k] = make_float2(hi, (float)(v0 - (double)hi));
+            }
             float us[Np];
 #pragma unroll
             for (int p = 0; p < Np; p++) us[p] = sd[e * Np + p];
@@ -429,7 +437,7 @@ __global__ void __launch_bounds__(256, N <= 4 ? 3 : 2) ipdg_lane_face_apply_kern
     const double* __restrict__ p_new = pc.p_new;
     const float* __restrict__ dp_new = pc.dp_new;
     const float* __restrict__ ftr = a.lane_ftr;
-    const double* __restrict__ p0 = a.lane_p0;
+    const float2* __restrict__ p0 = a.lane_p0;
     __shared__ float sd[128 * Np];
     __shared__ float srec[128 * SR];
     const int e = threadIdx.x & 127, h = threadIdx.x >> 7;
@@ -478,8 +486,8 @@ __global__ void __launch_bounds__(256, N <= 4 ? 3 : 2) ipdg_lane_face_apply_kern
             float us[Np];
 #pragma unroll
             for (int p = 0; p < Np; p++) us[p] = sd[e * Np + p];
-            const double pd0 = p0[k];
-            const float ub0 = (float)pd0;
+            const float2 pd0 = p0[k];
+            const float ub0 = pd0.x;
             const float* vc = a.o32.vc + (size_t)k * 3;
             const float vrr = vc[0], vrs = vc[1], vss = vc[2];
             const float* rec = srec + e * SR;
@@ -527,7 +535,8 @@ __global__ void __launch_bounds__(256, N <= 4 ? 3 : 2) ipdg_lane_face_apply_kern
                             nr[4 * q + 2] = w.z;
                             nr[4 * q + 3] = w.w;
                         }
-                        dc = (float)(pd0 - p0[nbk]);
+                        const float2 pn = p0[nbk];
+                        dc = (pd0.x - pn.x) + (pd0.y - pn.y);
                     } else {
 #pragma unroll
                         for (int q = 0; q < R; q++) nr[q] = 0.f;
@@ -745,6 +754,16 @@ __device__ __forceinline__ void row_of(int& e, int& i) {
 __device__ __forceinline__ float fma_t(float a, float b, float c) { return fmaf(a, b, c); }
 __device__ __forceinline__ double fma_t(double a, double b, double c) { return fma(a, b, c); }
 
+// FP32 offset mirror of z (value minus the element's row-0 value, lane lb of
+// the warp-aligned layout).  With FP32 blocks z is an FP32 product widened to
+// FP64, and the difference of two FP32 values rounded once to FP32 equals the
+// FP32 subtraction: no FP64 work.  Warp-uniform flags (every lane shuffles).
+__device__ __forceinline__ float mirror_offset(bool want, bool fp64_blocks, double z, float zf, int lb) {
+    if (!want) return 0.f;
+    if (fp64_blocks) return (float)(z - __shfl_sync(0xffffffffu, z, lb));
+    return zf - __shfl_sync(0xffffffffu, zf, lb);
+}
+
 // this thread's row of its element's inverse block (grouped layout), loaded
 // ahead of the residual it multiplies
 template <int NP, typename PT>
@@ -796,6 +815,7 @@ __global__ void __launch_bounds__(RowDims<NP>::THREADS) pcg_init_kernel(PcgVecs 
             const double ri = act ? v.r[idx] : 0.0;
             const float r32 = (float)ri;
             double z = 0;
+            float zf = 0.f;  // the FP32 product (FP32 blocks)
             if (v.P64) {
                 double s = 0;
                 const double* col = v.P64 + (size_t)grp * NP * EB * NP + e * NP + i;
@@ -815,8 +835,9 @@ __global__ void __launch_bounds__(RowDims<NP>::THREADS) pcg_init_kernel(PcgVecs 
                     if (act) s = fmaf(prow[j], rj, s);
                 }
                 z = (double)s;
+                zf = s;
             }
-            const double z0 = __shfl_sync(0xffffffffu, z, lb);
+            const float dzi = mirror_offset(v.dz != nullptr, v.P64 != nullptr, z, zf, lb);
             if (act) {
                 if (v.zb) v.zb[idx] = z;
                 else {
@@ -824,7 +845,7 @@ __global__ void __launch_bounds__(RowDims<NP>::THREADS) pcg_init_kernel(PcgVecs 
                     rz += ri * z;
                 }
                 if (v.r32) v.r32[idx] = r32;
-                if (v.dz) v.dz[idx] = (float)(z - z0);  // learned mode: the mirror of P r
+                if (v.dz) v.dz[idx] = dzi;  // learned mode: the mirror of P r
                 rr += ri * ri;
             }
         }
@@ -941,6 +962,7 @@ __global__ void __launch_bounds__(RowDims<NP>::THREADS) pcg_update_kernel(PcgVec
             }
             const float r32 = (float)ri;
             double z = 0;
+            float zf = 0.f;  // the FP32 product (FP32 blocks)
             if (v.P64) {
                 double s = 0;
                 const double* col = v.P64 + (size_t)grp * NP * EB * NP + e * NP + i;
@@ -958,8 +980,9 @@ __global__ void __launch_bounds__(RowDims<NP>::THREADS) pcg_update_kernel(PcgVec
                     if (act) s = fmaf(prow[j], rj, s);
                 }
                 z = (double)s;
+                zf = s;
             }
-            const double z0 = __shfl_sync(0xffffffffu, z, lb);
+            const float dzi = mirror_offset(v.dz != nullptr, v.P64 != nullptr, z, zf, lb);
             if (act) {
                 rr += ri * ri;
                 if (v.r32) v.r32[idx] = r32;
@@ -971,7 +994,7 @@ __global__ void __launch_bounds__(RowDims<NP>::THREADS) pcg_update_kernel(PcgVec
                     v.z[idx] = z;
                     rz += ri * z;
                 }
-                if (v.dz) v.dz[idx] = (float)(z - z0);  // learned mode: the mirror of P r
+                if (v.dz) v.dz[idx] = dzi;  // learned mode: the mirror of P r
             }
         }
     } else {

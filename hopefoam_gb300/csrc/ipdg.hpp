@@ -38,11 +38,11 @@ struct IpdgArgs {
     // the host copy of the reference tables passed to its kernels by value
     // (IpLaneTab<N>); per element and face, the input's trace and outward
     // normal derivative at the face's Gauss points (lane_face_rec(N) floats,
-    // element's own point order); per element the FP64 value of the input at
-    // its first node
+    // element's own point order); per element the input's value at its first
+    // node as an FP32 pair (hi = the value rounded, lo = the rest rounded)
     const void* lane_tab;
     float* lane_ftr;
-    double* lane_p0;
+    float2* lane_p0;
 };
 
 constexpr int kFaceCoef = 6;

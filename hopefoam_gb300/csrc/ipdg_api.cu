@@ -43,7 +43,7 @@ struct IpdgState {
     float *d_dz = nullptr, *d_dp = nullptr, *d_dp2 = nullptr;  // FP32 offset mirrors of z and p
     float* d_r32 = nullptr;      // FP32 copy of r (learned Schwarz mode)
     float* d_lane_ftr = nullptr;  // face records of the two-pass FP32 apply (N <= 5)
-    double* d_lane_p0 = nullptr;  // first-node values of its input
+    float2* d_lane_p0 = nullptr;  // first-node values of its input (FP32 pairs)
     int nmax = 0;
     int sms = 1;
     PcgScalars* d_S = nullptr;

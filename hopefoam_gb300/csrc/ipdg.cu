@@ -440,6 +440,7 @@ __global__ void __launch_bounds__(256, N <= 4 ? 3 : 2) ipdg_lane_face_apply_kern
     const float2* __restrict__ p0 = a.lane_p0;
     __shared__ float sd[128 * Np];
     __shared__ float srec[128 * SR];
+    __shared__ float sout[128 * Np];
     const int e = threadIdx.x & 127, h = threadIdx.x >> 7;
     double dot = 0.0;
     const int ntiles = (a.K + 127) / 128;
@@ -480,7 +481,6 @@ __global__ void __launch_bounds__(256, N <= 4 ? 3 : 2) ipdg_lane_face_apply_kern
             }
         }
         __syncthreads();
-        float vout[NH];
         if (e < ne) {
             const int k = k0 + e;
             float us[Np];
@@ -571,17 +571,10 @@ __global__ void __launch_bounds__(256, N <= 4 ? 3 : 2) ipdg_lane_face_apply_kern
                     }
                 }
 #pragma unroll
-                for (int i = i0; i < i1; i++) vout[i - i0] = v[i - i0];
+                for (int i = i0; i < i1; i++) sout[e * Np + i] = v[i - i0];
             };
             if (h == 0) rows(HalfTag<0>{});
             else rows(HalfTag<1>{});
-        }
-        __syncthreads();  // every lane has read sd and srec
-        if (e < ne) {
-            const int i0 = h ? NH : 0, i1 = h ? Np : NH;
-#pragma unroll
-            for (int i = 0; i < NH; i++)
-                if (i0 + i < i1) sd[e * Np + i0 + i] = vout[i];
         }
         __syncthreads();
         {
@@ -595,7 +588,7 @@ __global__ void __launch_bounds__(256, N <= 4 ? 3 : 2) ipdg_lane_face_apply_kern
             for (int j = 0; j < J; j++) {
                 const int t = threadIdx.x + 256 * j;
                 if (t < nn) {
-                    const double out = (double)sd[t];
+                    const double out = (double)sout[t];
                     y[g0 + t] = out;
                     dot += out * xp[j];
                 }

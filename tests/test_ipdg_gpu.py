@@ -81,6 +81,29 @@ def test_pcg_reaches_tolerance_and_matches_oracle(gpu_lib, precision):
     assert rel_l2(x, xo) < 1e-8
 
 
+@pytest.mark.parametrize("N", [1, 2, 3, 4, 5])
+def test_mixed_pcg_every_lane_order(gpu_lib, N):
+    """Mixed-precision PCG at every order of the two-pass FP32 apply (N <= 5):
+    the true FP64 residual reaches 1e-10, the solution matches the FP64 solve
+    to 1e-8, and the FP32 operator costs at most a quarter more
+    iterations than the FP64 one (a wrong face exchange would not converge
+    or would need many more)."""
+    from hopefoam_gb300 import _lib as L
+    from hopefoam_gb300.mesh import delaunay_square
+
+    m = delaunay_square(300, seed=13)
+    ps, orc, diag, off = _setup(m, N, tau=1.0)
+    b = np.random.default_rng(N).standard_normal(m.K * ps.Np)
+    x64, st64 = ps.solve(b, rtol=1e-10, precision=L.DG_PREC_FP64)
+    xmx, stmx = ps.solve(b, rtol=1e-10, precision=L.DG_PREC_SPLIT)
+    print("N=%d K=%d: FP64 %d its, mixed %d its" % (N, m.K, st64["iterations"], stmx["iterations"]))
+    assert stmx["rel_residual"] <= 1e-10
+    r = b - (-orc.blk_apply(diag, off, xmx))
+    assert np.linalg.norm(r) / np.linalg.norm(b) < 2e-10
+    assert rel_l2(xmx, x64) < 1e-8
+    assert stmx["iterations"] <= 1.25 * st64["iterations"] + 20
+
+
 def test_pcg_errors(gpu_lib):
     from hopefoam_gb300 import _lib as L
     from hopefoam_gb300.mesh import delaunay_square
